@@ -1,0 +1,177 @@
+/*
+ * ocl_gb300.h -- C ABI of the GB300 drop-cutter / push-cutter library.
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or torch types cross it.
+ * The C++ facade (opencamlib_gb300/include/ocl/) and the Python binding
+ * (opencamlib_gb300/__init__.py) are thin callers of these entry points.
+ *
+ * Each entry point replaces one step of the reference library's hot path
+ * (paths relative to the opencamlib source tree):
+ *
+ *   ocl_gb300_mesh_create   STLSurf + BatchDropCutter::setSTL / BatchPushCutter::setSTL
+ *                           (src/geo/stlsurf.cpp:32-42, src/dropcutter/batchdropcutter.cpp:54-61,
+ *                            src/algo/batchpushcutter.cpp:55-70): triangles are uploaded once,
+ *                           normals/bboxes precomputed, the KD order (src/common/kdtree.hpp:141-210)
+ *                           recorded for tie-breaking, and the XY cell index built on the device.
+ *   ocl_gb300_drop          BatchDropCutter::run() -> dropCutter5
+ *                           (src/dropcutter/batchdropcutter.cpp:187-231).
+ *   ocl_gb300_push          BatchPushCutter::run() -> pushCutter3
+ *                           (src/algo/batchpushcutter.cpp:136-188) incl. Fiber::addInterval
+ *                           (src/algo/fiber.cpp:58-93).
+ *   ocl_gb300_path_drop     PathDropCutter::run() (src/dropcutter/pathdropcutter.cpp:54-80).
+ *   ocl_gb300_adaptive_path_drop
+ *                           AdaptivePathDropCutter::run()
+ *                           (src/dropcutter/adaptivepathdropcutter.cpp:53-94).
+ *
+ * Errors: the reference reports nothing (asserts compiled out, std::cout);
+ * here every entry returns an int status and ocl_gb300_last_error() gives the
+ * message of the last failure on the calling thread.
+ */
+#ifndef OCL_GB300_H
+#define OCL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define OCL_GB300_OK                 0
+#define OCL_GB300_BAD_ARG            1
+#define OCL_GB300_UNSUPPORTED_CUTTER 2
+#define OCL_GB300_OOM                3
+#define OCL_GB300_DEVICE_ERROR       4
+#define OCL_GB300_ITER_LIMIT         5  /* a capped device loop ran out (Brent, candidate lists) */
+#define OCL_GB300_NO_DEVICE          6
+#define OCL_GB300_CAPACITY           7  /* caller buffer too small; needed size reported */
+
+/* ---- CC types: numeric values of ocl::CCType (src/geo/ccpoint.hpp:33-39) */
+enum ocl_gb300_cctype {
+    OCL_CC_NONE = 0, OCL_CC_VERTEX, OCL_CC_VERTEX_CYL,
+    OCL_CC_EDGE, OCL_CC_EDGE_HORIZ, OCL_CC_EDGE_SHAFT,
+    OCL_CC_EDGE_HORIZ_CYL, OCL_CC_EDGE_HORIZ_TOR, OCL_CC_EDGE_BALL,
+    OCL_CC_EDGE_POS, OCL_CC_EDGE_NEG, OCL_CC_EDGE_CYL, OCL_CC_EDGE_CONE, OCL_CC_EDGE_CONE_BASE,
+    OCL_CC_FACET, OCL_CC_FACET_TIP, OCL_CC_FACET_CYL,
+    OCL_CC_ERROR
+};
+
+/* ---- cutter description ---------------------------------------------- */
+enum ocl_gb300_cutter_kind {
+    OCL_CUTTER_CYL = 1,       /* CylCutter(d, l)            src/cutters/cylcutter.cpp:39-46  */
+    OCL_CUTTER_BALL = 2,      /* BallCutter(d, l)           src/cutters/ballcutter.cpp:38-45 */
+    OCL_CUTTER_BULL = 3,      /* BullCutter(d, r, l)        src/cutters/bullcutter.cpp:38-47 */
+    OCL_CUTTER_CONE = 4,      /* ConeCutter(d, angle, l=10) src/cutters/conecutter.cpp:39-49 */
+    OCL_CUTTER_COMPOSITE = 5  /* CompositeCutter::addCutter src/cutters/compositecutter.cpp:43-51 */
+};
+
+/* One basic (non-composite) cutter, by its constructor arguments. */
+typedef struct ocl_gb300_subcutter {
+    int32_t kind;            /* OCL_CUTTER_CYL .. OCL_CUTTER_CONE */
+    int32_t reserved;
+    double diameter;
+    double corner_radius;    /* BullCutter corner radius r */
+    double angle;            /* ConeCutter half-angle, radians */
+    double length;           /* constructor length argument */
+    /* composite only: addCutter(c, radius, height, zoffset) */
+    double radius;
+    double height;
+    double zoffset;
+} ocl_gb300_subcutter;
+
+#define OCL_GB300_MAX_SUB 4
+
+typedef struct ocl_gb300_cutter {
+    int32_t kind;            /* OCL_CUTTER_* */
+    int32_t nsub;            /* composite: number of sub-cutters (1..4) */
+    ocl_gb300_subcutter base;                  /* kind != COMPOSITE */
+    ocl_gb300_subcutter sub[OCL_GB300_MAX_SUB]; /* kind == COMPOSITE, in addCutter order */
+    double composite_length; /* CompositeCutter::length (set by the preset constructors) */
+} ocl_gb300_cutter;
+
+/* ---- meshes ------------------------------------------------------------ */
+typedef struct ocl_gb300_mesh_s* ocl_gb300_mesh;
+
+/* tris: ntri x 9 doubles (p0.xyz, p1.xyz, p2.xyz), in STLSurf insertion order.
+ * bucket_size: the KD-tree bucket size the reference would use (default 1);
+ * it fixes the candidate visit order used to break exact ties. */
+int ocl_gb300_mesh_create(const double* tris, uint64_t ntri, uint32_t bucket_size,
+                          ocl_gb300_mesh* out);
+int ocl_gb300_mesh_release(ocl_gb300_mesh mesh);
+uint64_t ocl_gb300_mesh_size(ocl_gb300_mesh mesh);
+/* Mesh bbox [minx maxx miny maxy minz maxz] (Bbox::operator[] order, src/geo/bbox.cpp:113-139). */
+int ocl_gb300_mesh_bbox(ocl_gb300_mesh mesh, double bb[6]);
+
+/* ---- drop-cutter ------------------------------------------------------- */
+/* Precision modes. */
+#define OCL_GB300_PREC_FP64   0   /* every candidate pair evaluated in FP64 */
+#define OCL_GB300_PREC_MIXED  1   /* FP32 screen on local coordinates + FP64 refine (default) */
+
+typedef struct ocl_gb300_stats {
+    uint64_t pairs;          /* exact-overlap (CL, triangle) pairs, sum_cl |S(cl)| */
+    uint64_t refined;        /* pairs evaluated in FP64 */
+    uint64_t iter_limit_hits;/* capped loops that ran out (0 on success) */
+    double   kernel_ms;      /* device time of the drop kernels (CUDA events) */
+    double   total_ms;       /* wall time of the call incl. copies */
+} ocl_gb300_stats;
+
+/* Host buffers: cl_xyz (M x 3) in; z_out (M), cc_out (M x 3), type_out (M) out.
+ * z_out starts from cl z (the reference lifts it: liftZ, src/geo/clpoint.cpp:79-99).
+ * stats may be NULL. */
+int ocl_gb300_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
+                   const double* cl_xyz, uint64_t M, int precision,
+                   double* z_out, double* cc_out, int32_t* type_out,
+                   ocl_gb300_stats* stats);
+
+/* Same with device buffers (cudaStream_t passed as void*); no host sync unless stats != NULL. */
+int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
+                          const double* d_cl_xyz, uint64_t M, int precision,
+                          double* d_z_out, double* d_cc_out, int32_t* d_type_out,
+                          void* stream, ocl_gb300_stats* stats);
+
+/* ---- push-cutter ------------------------------------------------------- */
+#define OCL_GB300_XFIBER 0
+#define OCL_GB300_YFIBER 1
+
+/* fibers: F x 6 doubles (p1.xyz, p2.xyz), all X- or all Y-fibers (dir).
+ * Output: offsets (F+1): intervals of fiber f are [offsets[f], offsets[f+1]),
+ * sorted by lower t.  Per interval i: ival[2i]=lower, ival[2i+1]=upper,
+ * cc[6i..6i+2]=lower_cc, cc[6i+3..6i+5]=upper_cc, cctype[2i]/[2i+1].
+ * If cap is too small OCL_GB300_CAPACITY is returned, offsets is complete. */
+int ocl_gb300_push(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, int dir,
+                   const double* fibers, uint64_t F,
+                   uint64_t* offsets, double* ival, double* cc, int32_t* cctype,
+                   uint64_t cap, ocl_gb300_stats* stats);
+
+/* ---- paths -------------------------------------------------------------- */
+/* A path is S spans x 11 doubles: [type, p1.xyz, p2.xyz, c.xyz, dir]
+ * type 0 = Line(p1,p2), 1 = Arc(p1,p2,c,dir) (src/geo/path.hpp:43-114). */
+#define OCL_GB300_SPAN_DOUBLES 11
+
+/* PathDropCutter: uniform sampling, z starts at min_z.  Output points are
+ * written to xyz (cap x 3), cc, type; *count is the number produced. */
+int ocl_gb300_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
+                        const double* spans, uint64_t S, double sampling, double min_z,
+                        double* xyz, double* cc, int32_t* type, uint64_t cap,
+                        uint64_t* count, ocl_gb300_stats* stats);
+
+/* AdaptivePathDropCutter: bisection while step > sampling or (not flat and
+ * step > min_sampling).  z starts from the path points (the reference does
+ * not apply setZ).  Output in the reference's depth-first order. */
+int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
+                                 const double* spans, uint64_t S, double sampling,
+                                 double min_sampling, double cos_limit,
+                                 double* xyz, double* cc, int32_t* type, uint64_t cap,
+                                 uint64_t* count, ocl_gb300_stats* stats);
+
+/* ---- misc ----------------------------------------------------------------- */
+const char* ocl_gb300_last_error(void);
+const char* ocl_gb300_version(void);
+/* 1 if a CUDA device is usable, else 0 (no compute). */
+int ocl_gb300_device_available(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCL_GB300_H */

@@ -1,0 +1,53 @@
+"""ctypes mirror of the C ABI structures and constants in include/ocl_gb300.h."""
+from __future__ import annotations
+
+import ctypes as C
+
+OK = 0
+BAD_ARG = 1
+UNSUPPORTED_CUTTER = 2
+OOM = 3
+DEVICE_ERROR = 4
+ITER_LIMIT = 5
+NO_DEVICE = 6
+CAPACITY = 7
+
+STATUS_NAMES = {OK: "OK", BAD_ARG: "BAD_ARG", UNSUPPORTED_CUTTER: "UNSUPPORTED_CUTTER", OOM: "OOM",
+                DEVICE_ERROR: "DEVICE_ERROR", ITER_LIMIT: "ITER_LIMIT", NO_DEVICE: "NO_DEVICE",
+                CAPACITY: "CAPACITY"}
+
+CUTTER_CYL = 1
+CUTTER_BALL = 2
+CUTTER_BULL = 3
+CUTTER_CONE = 4
+CUTTER_COMPOSITE = 5
+MAX_SUB = 4
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+XFIBER = 0
+YFIBER = 1
+
+SPAN_DOUBLES = 11
+
+# ocl::CCType numeric values (src/geo/ccpoint.hpp:33-39)
+CCTYPE_NAMES = ["NONE", "VERTEX", "VERTEX_CYL", "EDGE", "EDGE_HORIZ", "EDGE_SHAFT", "EDGE_HORIZ_CYL",
+                "EDGE_HORIZ_TOR", "EDGE_BALL", "EDGE_POS", "EDGE_NEG", "EDGE_CYL", "EDGE_CONE",
+                "EDGE_CONE_BASE", "FACET", "FACET_TIP", "FACET_CYL", "ERROR"]
+
+
+class SubCutter(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("diameter", C.c_double),
+                ("corner_radius", C.c_double), ("angle", C.c_double), ("length", C.c_double),
+                ("radius", C.c_double), ("height", C.c_double), ("zoffset", C.c_double)]
+
+
+class CutterDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nsub", C.c_int32), ("base", SubCutter),
+                ("sub", SubCutter * MAX_SUB), ("composite_length", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("pairs", C.c_uint64), ("refined", C.c_uint64), ("iter_limit_hits", C.c_uint64),
+                ("kernel_ms", C.c_double), ("total_ms", C.c_double)]

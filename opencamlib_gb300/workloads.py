@@ -1,0 +1,237 @@
+"""Seeded synthetic meshes, CL rasters, fibers and paths.
+
+No public dataset is involved in the drop-/push-cutter benchmarks, so these
+generators define the workloads.  All randomness comes from splitmix64
+(output k of stream `seed` is mix(seed + (k+1)*golden)), so every output is
+a pure function of (seed, index) and identical on any host; uniforms are
+(x >> 11) * 2**-53 and normals use Box-Muller.
+
+Workloads (sizes as used by the tests and the benchmark):
+  heightfield_c1   128x128-vertex bump field on [0,100]^2 -> 32,258 triangles
+  mesh_c2          512x1024 jittered bump field + hemisphere r=30 + 2-triangle
+                   plate -> exactly 1,048,576 triangles
+  raster           CL points on a regular xy raster at a given start z
+  sphere_torus     sphere-on-plate + torus (R=25, r=8) for the push-cutter
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, start: int = 0) -> np.ndarray:
+    """Outputs start..start+n-1 of the splitmix64 stream with this seed."""
+    with np.errstate(over="ignore"):
+        k = np.arange(start + 1, start + n + 1, dtype=np.uint64)
+        z = np.uint64(seed) + k * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform(seed: int, n: int, start: int = 0) -> np.ndarray:
+    """U[0,1) doubles from the top 53 bits."""
+    return (splitmix64(seed, n, start) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def normal(seed: int, n: int, start: int = 0) -> np.ndarray:
+    """N(0,1) by Box-Muller from consecutive uniform pairs."""
+    u = uniform(seed, 2 * n, 2 * start)
+    u1 = 1.0 - u[0::2]
+    u2 = u[1::2]
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+
+
+def bumps(seed: int, count: int = 8):
+    """Gaussian bump parameters, drawn per bump in the order (A, sigma, cx, cy):
+    A ~ U[2,15] mm, sigma ~ U[5,20] mm, centre ~ U[0,100]^2."""
+    u = uniform(seed, 4 * count).reshape(count, 4)
+    A = 2.0 + 13.0 * u[:, 0]
+    s = 5.0 + 15.0 * u[:, 1]
+    cx = 100.0 * u[:, 2]
+    cy = 100.0 * u[:, 3]
+    return A, s, cx, cy
+
+
+def bump_height(x, y, params, base: float = 10.0):
+    A, s, cx, cy = params
+    z = np.full(np.broadcast(x, y).shape, base, dtype=np.float64)
+    for k in range(len(A)):
+        z = z + A[k] * np.exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * s[k] ** 2))
+    return z
+
+
+def grid_triangles(X: np.ndarray, Y: np.ndarray, Z: np.ndarray) -> np.ndarray:
+    """Triangulate a vertex grid (arrays indexed [j, i], i along x).  Cell
+    (i, j) gives (p00, p10, p11) and (p00, p11, p01); cells in row-major order
+    (j outer, i inner)."""
+    P = np.stack([X, Y, Z], axis=-1)
+    p00 = P[:-1, :-1]
+    p10 = P[:-1, 1:]
+    p11 = P[1:, 1:]
+    p01 = P[1:, :-1]
+    t1 = np.concatenate([p00, p10, p11], axis=-1)
+    t2 = np.concatenate([p00, p11, p01], axis=-1)
+    return np.stack([t1, t2], axis=2).reshape(-1, 9)
+
+
+def heightfield(nx: int, ny: int, seed: int = 1, jitter: float = 0.0, jitter_seed: int = 2,
+                size: float = 100.0, nbumps: int = 8) -> np.ndarray:
+    """Bump heightfield with nx x ny vertices over [0,size]^2."""
+    xs = np.linspace(0.0, size, nx)
+    ys = np.linspace(0.0, size, ny)
+    X, Y = np.meshgrid(xs, ys)
+    Z = bump_height(X, Y, bumps(seed, nbumps))
+    if jitter > 0.0:
+        n = nx * ny
+        g = normal(jitter_seed, 3 * n).reshape(3, ny, nx) * jitter
+        X = X + g[0]
+        Y = Y + g[1]
+        Z = Z + g[2]
+    return grid_triangles(X, Y, Z)
+
+
+def heightfield_c1() -> np.ndarray:
+    """128x128 vertices on [0,100]^2 (h = 100/127): 32,258 triangles."""
+    return heightfield(128, 128, seed=1)
+
+
+def hemisphere(cx: float, cy: float, cz: float, r: float, naz: int = 52, nrings: int = 30) -> np.ndarray:
+    """Upper hemisphere: a pole fan of naz triangles, then nrings-1 bands of
+    2*naz triangles; ring k at polar angle k*(pi/2)/nrings."""
+    tris = []
+    th = np.arange(nrings + 1) * (math.pi / 2.0) / nrings
+    ph = 2.0 * math.pi * np.arange(naz) / naz
+
+    def v(k, m):
+        m = m % naz
+        return (cx + r * math.sin(th[k]) * math.cos(ph[m]), cy + r * math.sin(th[k]) * math.sin(ph[m]),
+                cz + r * math.cos(th[k]))
+
+    pole = (cx, cy, cz + r)
+    for m in range(naz):
+        tris.append(pole + v(1, m) + v(1, m + 1))
+    for k in range(1, nrings):
+        for m in range(naz):
+            a, b, c, d = v(k, m), v(k, m + 1), v(k + 1, m + 1), v(k + 1, m)
+            tris.append(a + d + c)
+            tris.append(a + c + b)
+    return np.array(tris, dtype=np.float64)
+
+
+def plate(z: float, x0: float = 0.0, x1: float = 100.0, y0: float = 0.0, y1: float = 100.0) -> np.ndarray:
+    return np.array([[x0, y0, z, x1, y0, z, x1, y1, z], [x0, y0, z, x1, y1, z, x0, y1, z]], dtype=np.float64)
+
+
+def mesh_c2() -> np.ndarray:
+    """Exactly 1,048,576 triangles: 512x1024-vertex bump field with vertex
+    jitter N(0, 0.01 mm) on x, y and z (1,045,506 triangles), a hemisphere
+    r=30 centred (50,50,10) with 52 azimuth x 30 rings (3,068 triangles) and
+    a 2-triangle plate at z=10 over [0,100]^2."""
+    hf = heightfield(512, 1024, seed=1, jitter=0.01, jitter_seed=2)
+    hs = hemisphere(50.0, 50.0, 10.0, 30.0)
+    t = np.concatenate([hf, hs, plate(10.0)], axis=0)
+    assert t.shape[0] == 1 << 20
+    return t
+
+
+def raster(nx: int, ny: int, step: float, z0: float = -50.0, x0: float = 0.0, y0: float = 0.0) -> np.ndarray:
+    """CL points x = x0 + step*i, y = y0 + step*j (j outer, i inner)."""
+    xs = x0 + step * np.arange(nx)
+    ys = y0 + step * np.arange(ny)
+    X, Y = np.meshgrid(xs, ys)
+    return np.stack([X.ravel(), Y.ravel(), np.full(X.size, z0)], axis=1)
+
+
+def raster_c1() -> np.ndarray:
+    return raster(200, 200, 0.5)
+
+
+def raster_c2() -> np.ndarray:
+    return raster(1000, 1000, 0.1)
+
+
+def subsample(n_total: int, n: int, seed: int) -> np.ndarray:
+    """Seeded sample of n distinct indices out of n_total, sorted."""
+    key = splitmix64(seed, n_total)
+    return np.sort(np.argsort(key, kind="stable")[:n])
+
+
+def torus(cx, cy, cz, R, r, nu, nv) -> np.ndarray:
+    """Torus around the z axis, nu x nv quads -> 2*nu*nv triangles."""
+    u = 2.0 * math.pi * np.arange(nu) / nu
+    w = 2.0 * math.pi * np.arange(nv) / nv
+    U, W = np.meshgrid(u, w, indexing="ij")
+    X = cx + (R + r * np.cos(W)) * np.cos(U)
+    Y = cy + (R + r * np.cos(W)) * np.sin(U)
+    Z = cz + r * np.sin(W)
+    P = np.stack([X, Y, Z], axis=-1)
+    Pn = np.roll(P, -1, axis=0)
+    Pm = np.roll(P, -1, axis=1)
+    Pnm = np.roll(Pn, -1, axis=1)
+    t1 = np.concatenate([P, Pn, Pnm], axis=-1)
+    t2 = np.concatenate([P, Pnm, Pm], axis=-1)
+    return np.stack([t1, t2], axis=2).reshape(-1, 9)
+
+
+def sphere(cx, cy, cz, r, naz, nrings) -> np.ndarray:
+    """Full UV sphere: two pole fans and nrings-2 bands."""
+    tris = []
+    th = np.arange(nrings + 1) * math.pi / nrings
+    ph = 2.0 * math.pi * np.arange(naz) / naz
+    ct, st = np.cos(th), np.sin(th)
+    cp, sp = np.cos(ph), np.sin(ph)
+
+    def v(k, m):
+        m = m % naz
+        return (cx + r * st[k] * cp[m], cy + r * st[k] * sp[m], cz + r * ct[k])
+
+    for m in range(naz):
+        tris.append((cx, cy, cz + r) + v(1, m) + v(1, m + 1))
+    for k in range(1, nrings - 1):
+        for m in range(naz):
+            a, b, c, d = v(k, m), v(k, m + 1), v(k + 1, m + 1), v(k + 1, m)
+            tris.append(a + d + c)
+            tris.append(a + c + b)
+    for m in range(naz):
+        tris.append((cx, cy, cz - r) + v(nrings - 1, m + 1) + v(nrings - 1, m))
+    return np.array(tris, dtype=np.float64)
+
+
+def sphere_torus(scale: int = 1) -> np.ndarray:
+    """Sphere-on-plate (sphere r=20 at (50,50,20), plate z=0 over [0,100]^2)
+    plus a torus R=25, r=8 around the sphere at z=8.  scale=1 gives ~500k
+    triangles; smaller scales give test-sized meshes."""
+    if scale == 1:
+        s = sphere(50.0, 50.0, 20.0, 20.0, 400, 300)
+        t = torus(50.0, 50.0, 8.0, 25.0, 8.0, 520, 250)
+    else:
+        s = sphere(50.0, 50.0, 20.0, 20.0, 24 * scale, 16 * scale)
+        t = torus(50.0, 50.0, 8.0, 25.0, 8.0, 32 * scale, 12 * scale)
+    return np.concatenate([s, t, plate(0.0)], axis=0)
+
+
+def fibers(direction: int, z: float, lo: float, hi: float, n: int, ext_lo: float, ext_hi: float) -> np.ndarray:
+    """n fibers at height z, evenly spaced over [lo, hi] across, spanning
+    [ext_lo, ext_hi] along (direction 0 = X-fibers, 1 = Y-fibers)."""
+    c = np.linspace(lo, hi, n)
+    f = np.zeros((n, 6))
+    if direction == 0:
+        f[:, 0] = ext_lo
+        f[:, 3] = ext_hi
+        f[:, 1] = c
+        f[:, 4] = c
+    else:
+        f[:, 1] = ext_lo
+        f[:, 4] = ext_hi
+        f[:, 0] = c
+        f[:, 3] = c
+    f[:, 2] = z
+    f[:, 5] = z
+    return f

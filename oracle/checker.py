@@ -1,0 +1,217 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes access to the CPU checkers.
+
+`port` is _build/liboclport.so (the C restatement in ocl_oracle.c, built on
+every machine); `ref` is _ref/liboclref.so (the reference's own sources,
+built only where the reference tree is present).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from opencamlib_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "liboclport.so")
+REF_SO = os.path.join(HERE, "_ref", "liboclref.so")
+
+_libs = {}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_long)
+_i64p = C.POINTER(C.c_int64)
+
+
+def build(ref: bool = True, quiet: bool = True) -> None:
+    """make port (and ref when the reference tree exists)."""
+    targets = ["port"] + (["ref"] if ref else [])
+    out = subprocess.run(["make", "-s", "-j8", *targets], cwd=HERE, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+
+
+def available(which: str) -> bool:
+    return os.path.exists(PORT_SO if which == "port" else REF_SO)
+
+
+def _lib(which: str):
+    if which in _libs:
+        return _libs[which]
+    path = PORT_SO if which == "port" else REF_SO
+    if not os.path.exists(path):
+        raise FileNotFoundError(path)
+    L = C.CDLL(path)
+    p = "oracle_" if which == "port" else "ref_"
+    cd = C.POINTER(_abi.CutterDesc)
+    f = getattr(L, p + "drop")
+    f.argtypes = [_dp, C.c_long, cd, _dp, C.c_long, C.c_int, C.c_uint, _dp, _dp, _ip, _lp]
+    f.restype = C.c_int
+    f = getattr(L, p + "push")
+    f.argtypes = [_dp, C.c_long, cd, C.c_int, _dp, C.c_long, C.c_int, C.c_uint, _ip, _dp, _dp, _ip,
+                  C.c_long, _lp]
+    f.restype = C.c_long
+    f = getattr(L, p + "pdc")
+    f.argtypes = [_dp, C.c_long, cd, _dp, C.c_long, C.c_double, C.c_double, C.c_int, C.c_uint, _dp, _dp,
+                  _ip, C.c_long]
+    f.restype = C.c_long
+    f = getattr(L, p + "apdc")
+    f.argtypes = [_dp, C.c_long, cd, _dp, C.c_long, C.c_double, C.c_double, C.c_double, C.c_uint, _dp,
+                  _dp, _ip, C.c_long]
+    f.restype = C.c_long
+    f = getattr(L, p + "kd_order")
+    f.argtypes = [_dp, C.c_long, C.c_uint, C.c_int, _i64p]
+    f.restype = C.c_int
+    if which == "port":
+        L.oracle_overlap_pairs.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long, C.c_int]
+        L.oracle_overlap_pairs.restype = C.c_long
+        L.oracle_cutter_fields.argtypes = [cd, _dp]
+        L.oracle_cutter_fields.restype = C.c_int
+    else:
+        L.ref_preset_fields.argtypes = [C.c_int, _dp, _dp]
+        L.ref_preset_fields.restype = C.c_int
+    _libs[which] = L
+    return L
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+def drop(tris, cutter, cl, which="port", nthreads=0, bucket=1):
+    """BatchDropCutter::run(); returns (z, cc[M,3], type[M], ncalls)."""
+    L = _lib(which)
+    tris = _d(tris).reshape(-1, 9)
+    cl = _d(cl).reshape(-1, 3)
+    M = cl.shape[0]
+    z = np.empty(M)
+    cc = np.empty((M, 3))
+    ty = np.empty(M, dtype=np.int32)
+    nc = C.c_long(0)
+    desc = cutter.desc() if hasattr(cutter, "desc") else cutter
+    fn = getattr(L, ("oracle_" if which == "port" else "ref_") + "drop")
+    st = fn(_ptr(tris), tris.shape[0], C.byref(desc), _ptr(cl), M, nthreads, bucket, _ptr(z), _ptr(cc),
+            _ptr(ty, _ip), C.byref(nc))
+    if st != 0:
+        raise RuntimeError(f"{which} drop failed: {st}")
+    return z, cc, ty, nc.value
+
+
+def push(tris, cutter, direction, fibers, which="port", nthreads=0, bucket=1):
+    """BatchPushCutter::run(); returns a list (per fiber) of interval records
+    (lower, upper, lower_cc[3], upper_cc[3], lower_type, upper_type) in the
+    reference's vector order, and ncalls."""
+    L = _lib(which)
+    tris = _d(tris).reshape(-1, 9)
+    fib = _d(fibers).reshape(-1, 6)
+    F = fib.shape[0]
+    counts = np.zeros(F, dtype=np.int32)
+    desc = cutter.desc() if hasattr(cutter, "desc") else cutter
+    fn = getattr(L, ("oracle_" if which == "port" else "ref_") + "push")
+    cap = max(16, 8 * F)
+    nc = C.c_long(0)
+    while True:
+        iv = np.empty(2 * cap)
+        cc = np.empty(6 * cap)
+        ty = np.empty(2 * cap, dtype=np.int32)
+        total = fn(_ptr(tris), tris.shape[0], C.byref(desc), direction, _ptr(fib), F, nthreads, bucket,
+                   _ptr(counts, _ip), _ptr(iv), _ptr(cc), _ptr(ty, _ip), cap, C.byref(nc))
+        if total < 0:
+            raise RuntimeError(f"{which} push failed: {total}")
+        if total <= cap:
+            break
+        cap = total
+    out = []
+    k = 0
+    for f in range(F):
+        rec = []
+        for _ in range(counts[f]):
+            rec.append((iv[2 * k], iv[2 * k + 1], cc[6 * k:6 * k + 3].copy(), cc[6 * k + 3:6 * k + 6].copy(),
+                        int(ty[2 * k]), int(ty[2 * k + 1])))
+            k += 1
+        out.append(rec)
+    return out, nc.value
+
+
+def pdc(tris, cutter, spans, sampling, minz, which="port", nthreads=0, bucket=1):
+    L = _lib(which)
+    tris = _d(tris).reshape(-1, 9)
+    spans = _d(spans).reshape(-1, _abi.SPAN_DOUBLES)
+    desc = cutter.desc() if hasattr(cutter, "desc") else cutter
+    fn = getattr(L, ("oracle_" if which == "port" else "ref_") + "pdc")
+    cap = 1024
+    while True:
+        xyz = np.empty((cap, 3))
+        cc = np.empty((cap, 3))
+        ty = np.empty(cap, dtype=np.int32)
+        n = fn(_ptr(tris), tris.shape[0], C.byref(desc), _ptr(spans), spans.shape[0], sampling, minz, nthreads,
+               bucket, _ptr(xyz), _ptr(cc), _ptr(ty, _ip), cap)
+        if n < 0:
+            raise RuntimeError(f"{which} pdc failed: {n}")
+        if n <= cap:
+            return xyz[:n], cc[:n], ty[:n]
+        cap = n
+
+
+def apdc(tris, cutter, spans, sampling, min_sampling, cos_limit=0.999, which="port", bucket=1):
+    L = _lib(which)
+    tris = _d(tris).reshape(-1, 9)
+    spans = _d(spans).reshape(-1, _abi.SPAN_DOUBLES)
+    desc = cutter.desc() if hasattr(cutter, "desc") else cutter
+    fn = getattr(L, ("oracle_" if which == "port" else "ref_") + "apdc")
+    cap = 4096
+    while True:
+        xyz = np.empty((cap, 3))
+        cc = np.empty((cap, 3))
+        ty = np.empty(cap, dtype=np.int32)
+        n = fn(_ptr(tris), tris.shape[0], C.byref(desc), _ptr(spans), spans.shape[0], sampling, min_sampling,
+               cos_limit, bucket, _ptr(xyz), _ptr(cc), _ptr(ty, _ip), cap)
+        if n < 0:
+            raise RuntimeError(f"{which} apdc failed: {n}")
+        if n <= cap:
+            return xyz[:n], cc[:n], ty[:n]
+        cap = n
+
+
+def kd_order(tris, which="port", bucket=1, dims=0):
+    L = _lib(which)
+    tris = _d(tris).reshape(-1, 9)
+    order = np.empty(tris.shape[0], dtype=np.int64)
+    fn = getattr(L, ("oracle_" if which == "port" else "ref_") + "kd_order")
+    st = fn(_ptr(tris), tris.shape[0], bucket, dims, _ptr(order, _i64p))
+    if st != 0:
+        raise RuntimeError(f"{which} kd_order failed: {st}")
+    return order
+
+
+def overlap_pairs(tris, radius, cl, nthreads=0):
+    L = _lib("port")
+    tris = _d(tris).reshape(-1, 9)
+    cl = _d(cl).reshape(-1, 3)
+    return L.oracle_overlap_pairs(_ptr(tris), tris.shape[0], radius, _ptr(cl), cl.shape[0], nthreads)
+
+
+def cutter_fields(cutter):
+    L = _lib("port")
+    out = np.zeros(4 + 9 * _abi.MAX_SUB)
+    desc = cutter.desc()
+    if L.oracle_cutter_fields(C.byref(desc), _ptr(out)) != 0:
+        raise RuntimeError("bad cutter")
+    return out
+
+
+def ref_preset_fields(preset: int, args):
+    L = _lib("ref")
+    a = _d(list(args) + [0.0] * (4 - len(args)))
+    out = np.zeros(4 + 9 * _abi.MAX_SUB)
+    if L.ref_preset_fields(preset, _ptr(a), _ptr(out)) != 0:
+        raise RuntimeError("bad preset")
+    return out

@@ -1,0 +1,82 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the reference's own drop-cutter / push-cutter / path code (compiled
+unmodified into oracle/_ref/liboclref.so by oracle/Makefile) on small seeded
+cases and stores inputs and outputs as .npz files.  Needs the reference
+source tree (oracle/Makefile REF_SRC); the fixtures are committed so that
+the GPU tests run without it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import checker as ck  # noqa: E402
+from opencamlib_gb300 import workloads as w  # noqa: E402
+from tests.golden.cases import CUTTERS, degenerate_mesh, degenerate_points, path_spans  # noqa: E402
+
+
+def drop_case(name, tris, cl):
+    out = {"tris": tris, "cl": cl}
+    for cname, make in CUTTERS.items():
+        z, cc, ty, _ = ck.drop(tris, make(), cl, "ref", nthreads=1)
+        out[f"{cname}_z"] = z
+        out[f"{cname}_cc"] = cc
+        out[f"{cname}_type"] = ty
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def push_case(name, tris, fib_x, fib_y):
+    out = {"tris": tris, "fib_x": fib_x, "fib_y": fib_y}
+    for cname, make in CUTTERS.items():
+        for d, fib in ((0, fib_x), (1, fib_y)):
+            res, _ = ck.push(tris, make(), d, fib, "ref", nthreads=1)
+            counts = np.array([len(r) for r in res], dtype=np.int32)
+            flat = [iv for r in res for iv in r]
+            out[f"{cname}_{d}_counts"] = counts
+            out[f"{cname}_{d}_ival"] = np.array([[iv[0], iv[1]] for iv in flat]).reshape(-1, 2)
+            out[f"{cname}_{d}_cc"] = np.array([np.concatenate([iv[2], iv[3]]) for iv in flat]).reshape(-1, 6)
+            out[f"{cname}_{d}_type"] = np.array([[iv[4], iv[5]] for iv in flat], dtype=np.int32).reshape(-1, 2)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def path_case(name, tris, spans):
+    out = {"tris": tris, "spans": spans}
+    for cname, make in CUTTERS.items():
+        xyz, cc, ty = ck.pdc(tris, make(), spans, 0.37, -5.0, "ref", nthreads=1)
+        out[f"{cname}_pdc_xyz"], out[f"{cname}_pdc_cc"], out[f"{cname}_pdc_type"] = xyz, cc, ty
+        xyz, cc, ty = ck.apdc(tris, make(), spans, 0.8, 0.05, 0.999, "ref")
+        out[f"{cname}_apdc_xyz"], out[f"{cname}_apdc_cc"], out[f"{cname}_apdc_type"] = xyz, cc, ty
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
+def main():
+    ck.build(ref=True)
+    if not ck.available("ref"):
+        raise SystemExit("reference library not built (reference sources missing)")
+    hf = w.heightfield(24, 24, seed=1)
+    cl = w.raster(40, 40, 100.0 / 39.0, z0=-50.0)
+    cl[:, 0] += 0.013
+    cl[:, 1] += 0.007
+    drop_case("drop_heightfield", hf, cl)
+    drop_case("drop_degenerate", degenerate_mesh(), degenerate_points())
+    fx = np.concatenate([w.fibers(0, z, -5.0, 105.0, 29, -10.0, 110.0) for z in (11.0, 13.3, 17.1)])
+    fy = np.concatenate([w.fibers(1, z, -5.0, 105.0, 29, -10.0, 110.0) for z in (11.0, 13.3, 17.1)])
+    push_case("push_heightfield", hf, fx, fy)
+    path_case("path_heightfield", hf, path_spans())
+    orders = {f"dims{d}_b{b}": ck.kd_order(hf, "ref", b, d) for d in (0, 1, 2) for b in (1, 3)}
+    np.savez_compressed(os.path.join(HERE, "kd_order.npz"), tris=hf, **orders)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
