@@ -109,10 +109,13 @@ int ocl_gb300_mesh_bbox(ocl_gb300_mesh mesh, double bb[6]);
 #define OCL_GB300_PREC_MIXED  1   /* FP32 screen on local coordinates + FP64 refine (default) */
 
 typedef struct ocl_gb300_stats {
-    uint64_t pairs;          /* exact-overlap (CL, triangle) pairs, sum_cl |S(cl)| */
-    uint64_t refined;        /* pairs evaluated in FP64 */
+    uint64_t pairs;          /* FP64 path: exact-overlap (CL, triangle) pairs, sum_cl |S(cl)| */
+    uint64_t refined;        /* triangles evaluated in FP64 by the refinement stage */
     uint64_t iter_limit_hits;/* capped loops that ran out (0 on success) */
-    double   kernel_ms;      /* device time of the drop kernels (CUDA events) */
+    uint64_t fallback;       /* CL points redone in plain FP64 (candidate list overflow) */
+    uint64_t violations;     /* FP64 results below a certified FP32 bound (always 0) */
+    uint64_t screened;       /* FP32 whole-triangle screens */
+    double   kernel_ms;      /* device time of the call's kernels (CUDA events) */
     double   total_ms;       /* wall time of the call incl. copies */
 } ocl_gb300_stats;
 
@@ -136,7 +139,8 @@ int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
 
 /* fibers: F x 6 doubles (p1.xyz, p2.xyz), all X- or all Y-fibers (dir).
  * Output: offsets (F+1): intervals of fiber f are [offsets[f], offsets[f+1]),
- * sorted by lower t.  Per interval i: ival[2i]=lower, ival[2i+1]=upper,
+ * in the order Fiber::ints holds them after the reference's merges.
+ * Per interval i: ival[2i]=lower, ival[2i+1]=upper,
  * cc[6i..6i+2]=lower_cc, cc[6i+3..6i+5]=upper_cc, cctype[2i]/[2i+1].
  * If cap is too small OCL_GB300_CAPACITY is returned, offsets is complete. */
 int ocl_gb300_push(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, int dir,

@@ -1,0 +1,213 @@
+"""ctypes binding of libocl_gb300.so (the C ABI in include/ocl_gb300.h).
+
+The library is the only compute path: there is no CPU fallback.  Loading
+fails loudly when the library has not been built, and every call that
+needs a GPU fails with NO_DEVICE when none is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libocl_gb300.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_u64p = C.POINTER(C.c_uint64)
+
+# every entry point declared in include/ocl_gb300.h
+EXPORTS = [
+    "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
+    "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_push", "ocl_gb300_path_drop",
+    "ocl_gb300_adaptive_path_drop", "ocl_gb300_last_error", "ocl_gb300_version", "ocl_gb300_device_available",
+]
+
+_lib = None
+
+
+class OclError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OclError(_abi.NO_DEVICE, f"CUDA library not built: {LIB_PATH} (run __graft_entry__.build())")
+    L = C.CDLL(LIB_PATH)
+    cd = C.POINTER(_abi.CutterDesc)
+    st = C.POINTER(_abi.Stats)
+    L.ocl_gb300_mesh_create.argtypes = [_dp, C.c_uint64, C.c_uint32, C.POINTER(C.c_void_p)]
+    L.ocl_gb300_mesh_release.argtypes = [C.c_void_p]
+    L.ocl_gb300_mesh_size.argtypes = [C.c_void_p]
+    L.ocl_gb300_mesh_size.restype = C.c_uint64
+    L.ocl_gb300_mesh_bbox.argtypes = [C.c_void_p, _dp]
+    L.ocl_gb300_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_int, _dp, _dp, _ip, st]
+    L.ocl_gb300_drop_device.argtypes = [C.c_void_p, cd, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, st]
+    L.ocl_gb300_push.argtypes = [C.c_void_p, cd, C.c_int, _dp, C.c_uint64, _u64p, _dp, _dp, _ip, C.c_uint64, st]
+    L.ocl_gb300_path_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, C.c_double, _dp, _dp, _ip,
+                                      C.c_uint64, _u64p, st]
+    L.ocl_gb300_adaptive_path_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, C.c_double, C.c_double,
+                                               _dp, _dp, _ip, C.c_uint64, _u64p, st]
+    L.ocl_gb300_last_error.restype = C.c_char_p
+    L.ocl_gb300_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != 0:
+        raise OclError(status, lib().ocl_gb300_last_error().decode())
+
+
+def device_available() -> bool:
+    return bool(lib().ocl_gb300_device_available())
+
+
+def _d(a, cols):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a.reshape(-1, cols)
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t)
+
+
+PRECISION = {"fp64": _abi.PREC_FP64, "mixed": _abi.PREC_MIXED}
+
+
+class DeviceMesh:
+    """A triangle surface resident in device memory (STLSurf + the setSTL
+    indexes of the reference), built once and shared by all operations."""
+
+    def __init__(self, tris, bucket_size: int = 1):
+        t = _d(tris, 9)
+        self._tris = t
+        h = C.c_void_p()
+        check(lib().ocl_gb300_mesh_create(_p(t), t.shape[0], bucket_size, C.byref(h)))
+        self._h = h
+        self.bucket_size = bucket_size
+
+    def __len__(self):
+        return int(lib().ocl_gb300_mesh_size(self._h))
+
+    def bbox(self):
+        b = np.zeros(6)
+        check(lib().ocl_gb300_mesh_bbox(self._h, _p(b)))
+        return b
+
+    def release(self):
+        if getattr(self, "_h", None):
+            lib().ocl_gb300_mesh_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def drop(self, cutter, cl, precision: str = "mixed"):
+        """BatchDropCutter::run over CL points (M x 3); returns z, cc (M x 3),
+        cc type (M) and the call's Stats."""
+        cl = _d(cl, 3)
+        M = cl.shape[0]
+        z = np.empty(M)
+        cc = np.empty((M, 3))
+        ty = np.empty(M, dtype=np.int32)
+        st = _abi.Stats()
+        desc = cutter.desc()
+        check(lib().ocl_gb300_drop(self._h, C.byref(desc), _p(cl), M, PRECISION[precision], _p(z), _p(cc),
+                                   _p(ty, _ip), C.byref(st)))
+        return z, cc, ty, st
+
+    def drop_device(self, cutter, d_cl, M, d_z, d_cc, d_type, stream=0, precision: str = "mixed", stats=True):
+        """Device-pointer variant (pointers as ints)."""
+        st = _abi.Stats() if stats else None
+        desc = cutter.desc()
+        check(lib().ocl_gb300_drop_device(self._h, C.byref(desc), C.c_void_p(d_cl), M, PRECISION[precision],
+                                          C.c_void_p(d_z), C.c_void_p(d_cc), C.c_void_p(d_type), C.c_void_p(stream),
+                                          C.byref(st) if st is not None else None))
+        return st
+
+    def push(self, cutter, direction: int, fibers):
+        """BatchPushCutter::run over fibers (F x 6).  Returns per-fiber lists of
+        (lower, upper, lower_cc, upper_cc, lower_type, upper_type) sorted by
+        lower, and the Stats."""
+        fib = _d(fibers, 6)
+        F = fib.shape[0]
+        offsets = np.zeros(F + 1, dtype=np.uint64)
+        cap = max(64, 4 * F)
+        desc = cutter.desc()
+        while True:
+            iv = np.empty(2 * cap)
+            cc = np.empty(6 * cap)
+            ty = np.empty(2 * cap, dtype=np.int32)
+            st = _abi.Stats()
+            status = lib().ocl_gb300_push(self._h, C.byref(desc), direction, _p(fib), F, _p(offsets, _u64p), _p(iv),
+                                          _p(cc), _p(ty, _ip), cap, C.byref(st))
+            if status == _abi.CAPACITY:
+                cap = int(offsets[-1]) + 16
+                continue
+            check(status)
+            break
+        out = []
+        for f in range(F):
+            rec = []
+            for k in range(int(offsets[f]), int(offsets[f + 1])):
+                rec.append((iv[2 * k], iv[2 * k + 1], cc[6 * k:6 * k + 3].copy(), cc[6 * k + 3:6 * k + 6].copy(),
+                            int(ty[2 * k]), int(ty[2 * k + 1])))
+            out.append(rec)
+        return out, st
+
+    def path_drop(self, cutter, spans, sampling, min_z):
+        spans = _d(spans, _abi.SPAN_DOUBLES)
+        cap = 4096
+        desc = cutter.desc()
+        while True:
+            xyz = np.empty((cap, 3))
+            cc = np.empty((cap, 3))
+            ty = np.empty(cap, dtype=np.int32)
+            n = C.c_uint64(0)
+            st = _abi.Stats()
+            status = lib().ocl_gb300_path_drop(self._h, C.byref(desc), _p(spans), spans.shape[0], sampling, min_z,
+                                               _p(xyz), _p(cc), _p(ty, _ip), cap, C.byref(n), C.byref(st))
+            if status == _abi.CAPACITY:
+                cap = int(n.value)
+                continue
+            check(status)
+            k = int(n.value)
+            return xyz[:k], cc[:k], ty[:k], st
+
+    def adaptive_path_drop(self, cutter, spans, sampling, min_sampling, cos_limit=0.999):
+        spans = _d(spans, _abi.SPAN_DOUBLES)
+        cap = 4096
+        desc = cutter.desc()
+        while True:
+            xyz = np.empty((cap, 3))
+            cc = np.empty((cap, 3))
+            ty = np.empty(cap, dtype=np.int32)
+            n = C.c_uint64(0)
+            st = _abi.Stats()
+            status = lib().ocl_gb300_adaptive_path_drop(self._h, C.byref(desc), _p(spans), spans.shape[0], sampling,
+                                                        min_sampling, cos_limit, _p(xyz), _p(cc), _p(ty, _ip), cap,
+                                                        C.byref(n), C.byref(st))
+            if status == _abi.CAPACITY:
+                cap = int(n.value)
+                continue
+            check(status)
+            k = int(n.value)
+            return xyz[:k], cc[:k], ty[:k], st

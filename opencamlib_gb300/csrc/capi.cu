@@ -1,0 +1,327 @@
+// capi.cu -- the extern "C" entry points declared in include/ocl_gb300.h,
+// cutter parameter derivation and error reporting.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "drop.cuh"
+#include "geom64.cuh"
+#include "mesh.cuh"
+#include "util.cuh"
+
+namespace oclg {
+
+static thread_local std::string tl_error;
+std::string& last_error_ref() { return tl_error; }
+void set_error(const std::string& msg) { tl_error = msg; }
+
+int mesh_create(const double* tris, uint64_t n, unsigned bucket, Mesh** out);
+void mesh_destroy(Mesh* m);
+int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t F, uint64_t* offsets, double* ival,
+             double* cc, int32_t* cctype, uint64_t cap, ocl_gb300_stats* stats);
+int path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, double sampling, double min_z,
+                  double* xyz, double* cc, int32_t* type, uint64_t cap, uint64_t* count, ocl_gb300_stats* stats);
+int adaptive_path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, double sampling,
+                           double min_sampling, double cos_limit, double* xyz, double* cc, int32_t* type,
+                           uint64_t cap, uint64_t* count, ocl_gb300_stats* stats);
+
+// Constructors of the basic cutters (cylcutter.cpp:39-46, ballcutter.cpp:38-45,
+// bullcutter.cpp:38-47, conecutter.cpp:39-49); compiled with
+// -ffp-contract=off, so derived lengths equal the reference's doubles.
+static int make_basic(const ocl_gb300_subcutter& s, BasicP& b) {
+    std::memset(&b, 0, sizeof(b));
+    b.kind = s.kind;
+    const double d = s.diameter, l = s.length;
+    if (!(d > 0.0) || !std::isfinite(d) || !std::isfinite(l)) return OCL_GB300_BAD_ARG;
+    switch (s.kind) {
+    case OCL_CUTTER_CYL:
+        if (!(l > 0.0)) return OCL_GB300_BAD_ARG;
+        b.diameter = d; b.radius = d / 2.0; b.length = l;
+        b.xy_normal_length = b.radius; b.normal_length = 0.0; b.center_height = 0.0;
+        return OCL_GB300_OK;
+    case OCL_CUTTER_BALL:
+        if (!(l > 0.0)) return OCL_GB300_BAD_ARG;
+        b.diameter = d; b.radius = d / 2.0; b.length = l;
+        b.normal_length = b.radius; b.xy_normal_length = 0.0; b.center_height = b.radius;
+        return OCL_GB300_OK;
+    case OCL_CUTTER_BULL:
+        if (!(l > 0.0) || !(s.corner_radius > 0.0) || !(d / 2.0 - s.corner_radius > 0.0)) return OCL_GB300_BAD_ARG;
+        b.diameter = d; b.radius = d / 2.0; b.radius1 = d / 2.0 - s.corner_radius; b.radius2 = s.corner_radius;
+        b.length = l; b.xy_normal_length = b.radius1; b.normal_length = b.radius2; b.center_height = b.radius2;
+        return OCL_GB300_OK;
+    case OCL_CUTTER_CONE:
+        if (!(s.angle > 0.0) || !(s.angle < 1.5707963267948966)) return OCL_GB300_BAD_ARG;
+        b.diameter = d; b.radius = d / 2.0; b.angle = s.angle; b.tan_angle = std::tan(s.angle);
+        b.length = b.radius / std::tan(b.angle) + l;
+        b.center_height = b.radius / std::tan(b.angle);
+        b.xy_normal_length = b.radius; b.normal_length = 0.0;
+        return OCL_GB300_OK;
+    }
+    return OCL_GB300_UNSUPPORTED_CUTTER;
+}
+
+int make_cutter_params(const ocl_gb300_cutter& in, CutterP& cp) {
+    std::memset(&cp, 0, sizeof(cp));
+    cp.kind = in.kind;
+    if (in.kind != OCL_CUTTER_COMPOSITE) {
+        int st = make_basic(in.base, cp.b);
+        if (st) return st;
+        cp.radius = cp.b.radius;
+        cp.length = cp.b.length;
+        return OCL_GB300_OK;
+    }
+    // CompositeCutter::addCutter (compositecutter.cpp:43-51)
+    if (in.nsub < 1 || in.nsub > OCL_GB300_MAX_SUB) return OCL_GB300_BAD_ARG;
+    cp.nsub = in.nsub;
+    cp.radius = 0;
+    for (int n = 0; n < in.nsub; ++n) {
+        int st = make_basic(in.sub[n], cp.sub[n]);
+        if (st) return st;
+        cp.radiusvec[n] = in.sub[n].radius;
+        cp.heightvec[n] = in.sub[n].height;
+        cp.zoffset[n] = in.sub[n].zoffset;
+        if (in.sub[n].radius > cp.radius) cp.radius = in.sub[n].radius;
+    }
+    if (!(cp.radius > 0.0)) return OCL_GB300_BAD_ARG;
+    cp.length = in.composite_length;
+    return OCL_GB300_OK;
+}
+
+static double height_basic_host(const BasicP& c, double r) {
+    switch (c.kind) {
+    case OCL_CUTTER_CYL: return (r <= c.radius) ? 0.0 : -1.0;
+    case OCL_CUTTER_BALL: return c.radius - std::sqrt(c.radius * c.radius - r * r);
+    case OCL_CUTTER_BULL:
+        if (r <= c.radius1) return 0.0;
+        if (r <= c.radius) return c.radius2 - std::sqrt(c.radius2 * c.radius2 - (r - c.radius1) * (r - c.radius1));
+        return -1;
+    case OCL_CUTTER_CONE: return r / c.tan_angle;
+    }
+    return -1;
+}
+
+double height_host(const CutterP& c, double r) {
+    if (c.kind != OCL_CUTTER_COMPOSITE) return height_basic_host(c.b, r);
+    int idx = 0;
+    for (int n = 0; n < c.nsub; ++n) {
+        double lo = (n == 0) ? -1E-6 : c.radiusvec[n - 1] - 1E-6;
+        double hi = c.radiusvec[n] + 1e-6;
+        if (lo <= r && r <= hi) { idx = n; break; }
+    }
+    return height_basic_host(c.sub[idx], r) + c.zoffset[idx];
+}
+
+void fill_prof(const CutterP& cp, Prof32& prof, float* hlb, bool& composite) {
+    std::memset(&prof, 0, sizeof(prof));
+    composite = cp.kind == OCL_CUTTER_COMPOSITE;
+    const BasicP& b = cp.b;
+    prof.kind = composite ? 0 : b.kind;
+    prof.R = (float)cp.radius;
+    if (!composite) {
+        prof.r1 = (float)b.radius1;
+        prof.r2 = (float)b.radius2;
+        prof.inv_tan = b.kind == OCL_CUTTER_CONE ? (float)(1.0 / b.tan_angle) : 0.0f;
+        prof.center_height = (float)b.center_height;
+        prof.length = (float)b.length;
+        prof.xynl = (float)b.xy_normal_length;
+        prof.nl = (float)b.normal_length;
+    }
+    // hlb[k] <= min over r in [k R / N, R] of height(r), built from the top
+    // down with dense samples per bin, minus a small margin.
+    const double R = cp.radius;
+    double run = 1e300;
+    for (int k = HLB_N - 1; k >= 0; --k) {
+        double r0 = R * k / HLB_N, r1 = R * (k + 1) / HLB_N;
+        for (int s = 0; s <= 16; ++s) {
+            double r = r0 + (r1 - r0) * s / 16.0;
+            if (r > R) r = R;
+            double h = height_host(cp, r);
+            if (cp.kind == OCL_CUTTER_CYL || (cp.kind != OCL_CUTTER_COMPOSITE && b.kind == OCL_CUTTER_CYL)) h = 0.0;
+            if (std::isfinite(h)) run = std::min(run, h);
+        }
+        double v = run - 1e-6 * (1.0 + R);
+        hlb[k] = (float)std::nextafter((float)v, -3.0e38f);
+    }
+}
+
+}  // namespace oclg
+
+using namespace oclg;
+
+struct ocl_gb300_mesh_s {
+    Mesh* m;
+};
+
+extern "C" {
+
+const char* ocl_gb300_last_error(void) { return tl_error.c_str(); }
+const char* ocl_gb300_version(void) { return "opencamlib_gb300 0.1 (sm_103a)"; }
+
+int ocl_gb300_device_available(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n > 0 ? 1 : 0;
+}
+
+static int need_device() {
+    if (!ocl_gb300_device_available()) {
+        set_error("no CUDA device available");
+        return OCL_GB300_NO_DEVICE;
+    }
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_mesh_create(const double* tris, uint64_t ntri, uint32_t bucket_size, ocl_gb300_mesh* out) {
+    if (!out) {
+        set_error("null output handle");
+        return OCL_GB300_BAD_ARG;
+    }
+    *out = nullptr;
+    int st = need_device();
+    if (st) return st;
+    Mesh* m = nullptr;
+    st = mesh_create(tris, ntri, bucket_size, &m);
+    if (st) return st;
+    *out = new ocl_gb300_mesh_s{m};
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_mesh_release(ocl_gb300_mesh mesh) {
+    if (!mesh) return OCL_GB300_BAD_ARG;
+    mesh_destroy(mesh->m);
+    delete mesh;
+    return OCL_GB300_OK;
+}
+
+uint64_t ocl_gb300_mesh_size(ocl_gb300_mesh mesh) { return mesh ? mesh->m->n : 0; }
+
+int ocl_gb300_mesh_bbox(ocl_gb300_mesh mesh, double bb[6]) {
+    if (!mesh || !bb) return OCL_GB300_BAD_ARG;
+    std::memcpy(bb, mesh->m->bb, 6 * sizeof(double));
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* d_cl_xyz, uint64_t M,
+                          int precision, double* d_z_out, double* d_cc_out, int32_t* d_type_out, void* stream,
+                          ocl_gb300_stats* stats) {
+    if (!mesh || !cutter) {
+        set_error("null mesh or cutter");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (M > 0 && (!d_cl_xyz || !d_z_out || !d_cc_out || !d_type_out)) {
+        set_error("null buffer");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (precision != OCL_GB300_PREC_FP64 && precision != OCL_GB300_PREC_MIXED) {
+        set_error("unknown precision mode");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = make_cutter_params(*cutter, cp);
+    if (st) {
+        set_error(st == OCL_GB300_UNSUPPORTED_CUTTER ? "unsupported cutter kind" : "invalid cutter parameters");
+        return st;
+    }
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return drop_run(*mesh->m, cp, d_cl_xyz, M, precision, d_z_out, d_cc_out, d_type_out, (cudaStream_t)stream, stats);
+}
+
+int ocl_gb300_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* cl_xyz, uint64_t M,
+                   int precision, double* z_out, double* cc_out, int32_t* type_out, ocl_gb300_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (M == 0) {
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return mesh && cutter ? OCL_GB300_OK : OCL_GB300_BAD_ARG;
+    }
+    if (!cl_xyz || !z_out || !cc_out || !type_out) {
+        set_error("null buffer");
+        return OCL_GB300_BAD_ARG;
+    }
+    DevBuf<double> dcl(3 * M), dz(M), dcc(3 * M);
+    DevBuf<int32_t> dty(M);
+    if (!dcl.ok() || !dz.ok() || !dcc.ok() || !dty.ok()) return OCL_GB300_OOM;
+    cudaStream_t s = 0;
+    CK(cudaMemcpyAsync(dcl.p, cl_xyz, 3 * M * sizeof(double), cudaMemcpyHostToDevice, s));
+    int st = ocl_gb300_drop_device(mesh, cutter, dcl.p, M, precision, dz.p, dcc.p, dty.p, s, stats);
+    if (st) return st;
+    CK(cudaMemcpyAsync(z_out, dz.p, M * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cc_out, dcc.p, 3 * M * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(type_out, dty.p, M * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (stats)
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return OCL_GB300_OK;
+}
+
+static int cutter_or_error(const ocl_gb300_cutter* cutter, CutterP& cp) {
+    if (!cutter) {
+        set_error("null cutter");
+        return OCL_GB300_BAD_ARG;
+    }
+    int st = make_cutter_params(*cutter, cp);
+    if (st) set_error(st == OCL_GB300_UNSUPPORTED_CUTTER ? "unsupported cutter kind" : "invalid cutter parameters");
+    return st;
+}
+
+int ocl_gb300_push(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, int dir, const double* fibers, uint64_t F,
+                   uint64_t* offsets, double* ival, double* cc, int32_t* cctype, uint64_t cap,
+                   ocl_gb300_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!mesh || !offsets || (F > 0 && !fibers) || (cap > 0 && (!ival || !cc || !cctype))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (dir != OCL_GB300_XFIBER && dir != OCL_GB300_YFIBER) {
+        set_error("dir must be OCL_GB300_XFIBER or OCL_GB300_YFIBER");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = cutter_or_error(cutter, cp);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    st = push_run(*mesh->m, cp, dir, fibers, F, offsets, ival, cc, cctype, cap, stats);
+    if (stats)
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+int ocl_gb300_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* spans, uint64_t S,
+                        double sampling, double min_z, double* xyz, double* cc, int32_t* type, uint64_t cap,
+                        uint64_t* count, ocl_gb300_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!mesh || !count || (S > 0 && !spans) || (cap > 0 && (!xyz || !cc || !type))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = cutter_or_error(cutter, cp);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    st = path_drop_run(*mesh->m, cp, spans, S, sampling, min_z, xyz, cc, type, cap, count, stats);
+    if (stats)
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* spans,
+                                 uint64_t S, double sampling, double min_sampling, double cos_limit, double* xyz,
+                                 double* cc, int32_t* type, uint64_t cap, uint64_t* count, ocl_gb300_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!mesh || !count || (S > 0 && !spans) || (cap > 0 && (!xyz || !cc || !type))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = cutter_or_error(cutter, cp);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    st = adaptive_path_drop_run(*mesh->m, cp, spans, S, sampling, min_sampling, cos_limit, xyz, cc, type, cap, count,
+                                stats);
+    if (stats)
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,604 @@
+// drop.cu -- BatchDropCutter on the GPU.
+//
+// Pipeline for M CL points against a device-resident mesh:
+//   1. CL points are ordered along a Morton curve, so a warp's 32 lanes hold
+//      32 neighbouring points (lanes = CL points).
+//   2. Mixed precision:
+//      k_drop_screen  one warp per 32 points streams the grid cells under the
+//                     warp's footprint, centre rows first.  Cells and then
+//                     triangles are rejected with an FP32 upper bound
+//                     (bbox max z minus a lower bound of the cutter profile at
+//                     the bbox distance); survivors get the FP32
+//                     whole-triangle screen [lo, hi].  A lane keeps a running
+//                     certified lower bound and a short list of triangles whose
+//                     hi reaches it.
+//      k_drop_refine  one thread per point evaluates its listed triangles in
+//                     FP64 with the reference semantics and keeps the highest
+//                     contact (ties: the reference's KD visit order).
+//      k_drop_kd      points whose list overflowed are redone in plain FP64.
+//   3. Plain FP64 (OCL_GB300_PREC_FP64): k_drop_kd for every point; it runs
+//      the reference's KD search and evaluates every exact-overlap pair in FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include <cub/cub.cuh>
+
+#include "drop.cuh"
+#include "geom64.cuh"
+#include "util.cuh"
+
+namespace oclg {
+
+// ---------------------------------------------------------------------------
+// Morton ordering of the CL points
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+    x &= 0xFFFF;
+    x = (x | (x << 8)) & 0x00FF00FF;
+    x = (x | (x << 4)) & 0x0F0F0F0F;
+    x = (x | (x << 2)) & 0x33333333;
+    x = (x | (x << 1)) & 0x55555555;
+    return x;
+}
+
+__global__ void k_morton(const double* cl, uint64_t M, double x0, double y0, double sx, double sy, uint32_t* keys,
+                         uint32_t* idx) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    double fx = (cl[3 * i] - x0) * sx, fy = (cl[3 * i + 1] - y0) * sy;
+    uint32_t qx = (uint32_t)fmin(fmax(fx, 0.0), 65535.0);
+    uint32_t qy = (uint32_t)fmin(fmax(fy, 0.0), 65535.0);
+    keys[i] = spread16(qx) | (spread16(qy) << 1);
+    idx[i] = (uint32_t)i;
+}
+
+__global__ void k_gather_cl(const double* cl, const uint32_t* perm, uint64_t M, double* out) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    uint32_t j = perm[i];
+    out[3 * i] = cl[3 * j];
+    out[3 * i + 1] = cl[3 * j + 1];
+    out[3 * i + 2] = cl[3 * j + 2];
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_mind(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_maxd(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// k-th element of the centre-out sequence over [lo, hi] starting at c.
+__device__ __forceinline__ int centre_out(int k, int c, int lo, int hi) {
+    // sequence c, c+1, c-1, c+2, c-2, ... skipping values outside [lo, hi]
+    int up = hi - c, dn = c - lo;
+    int m = min(up, dn);
+    if (k <= 2 * m) {
+        if (k == 0) return c;
+        int s = (k + 1) / 2;
+        return (k & 1) ? c + s : c - s;
+    }
+    int rest = k - 2 * m;
+    return (up > dn) ? c + m + rest : c - m - rest;
+}
+
+// Query rectangle of a warp in cell coordinates; returns false if empty.
+__device__ __forceinline__ bool warp_rect(const GridP& g, double xmin, double xmax, double ymin, double ymax,
+                                          double reach, int& c0, int& c1, int& r0, int& r1) {
+    double a0 = floor((xmin - reach - g.x0) * g.inv_cs), a1 = floor((xmax + reach - g.x0) * g.inv_cs);
+    double b0 = floor((ymin - reach - g.y0) * g.inv_cs), b1 = floor((ymax + reach - g.y0) * g.inv_cs);
+    if (a1 < 0 || b1 < 0 || a0 > g.ncol - 1 || b0 > g.nrow - 1) return false;
+    c0 = (int)fmax(a0, 0.0);
+    c1 = (int)fmin(a1, (double)(g.ncol - 1));
+    r0 = (int)fmax(b0, 0.0);
+    r1 = (int)fmin(b1, (double)(g.nrow - 1));
+    return true;
+}
+
+__device__ __forceinline__ float hlb_at(const float* hlb, float d, float inv_step) {
+    int k = (int)(fmaxf(d, 0.0f) * inv_step);
+    k = min(k, HLB_N - 1);
+    return hlb[k];
+}
+
+struct Best64 {
+    double z;
+    double cx, cy, cz;
+    int type;
+    uint32_t rank;
+};
+__device__ __forceinline__ void merge_best(Best64& b, const CL64& c, uint32_t rank) {
+    if (c.z > b.z || (c.z == b.z && rank < b.rank)) {
+        b.z = c.z;
+        b.cx = c.cc.x;
+        b.cy = c.cc.y;
+        b.cz = c.cc.z;
+        b.type = c.type;
+        b.rank = rank;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plain FP64 kernel: the reference's own algorithm on the device.  A warp of
+// 32 CL points walks the KD tree of the mesh (KDTree::search_node,
+// common/kdtree.hpp:273-304) with one visit mask per node, so each lane sees
+// exactly its own candidates in the reference's visit order; every candidate
+// that overlaps (MillingCutter::overlaps) and is not below the running z is
+// dropped in FP64 against that running z (BatchDropCutter::dropCutter5,
+// dropcutter/batchdropcutter.cpp:187-231).  Used for OCL_GB300_PREC_FP64 and
+// for the points the mixed path hands back.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_drop_kd(const DropCtx* __restrict__ ctxp, const uint32_t* __restrict__ list,
+                                                 int nlist) {
+    const DropCtx& ctx = *ctxp;
+    __shared__ uint2 s_stack[4][KD_STACK];
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int base = warp * 32;
+    if (base >= nlist) return;
+    const bool active = base + lane < nlist;
+    const uint32_t i = list ? list[active ? base + lane : base] : (uint32_t)(active ? base + lane : base);
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const double R = ctx.cp.radius;
+    // KDTree::search_cutter_overlap box (kdtree.hpp:130-135), XY dimensions
+    const double bb[4] = {x - R, x + R, y - R, y + R};
+    CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
+    unsigned long long pairs = 0;
+    int capped = 0;
+    uint2* st = s_stack[wl];
+    const unsigned amask = __ballot_sync(0xffffffffu, active);
+    int sp = 0;
+    if (ctx.kd_nodes && amask) {
+        if (lane == 0) st[0] = make_uint2(0u, amask);
+        sp = 1;
+    }
+    __syncwarp();
+    while (sp > 0) {
+        --sp;
+        const uint2 e = st[sp];
+        __syncwarp();
+        const KDNodeD nd = ctx.kd_nodes[e.x];
+        const bool in = (e.y >> lane) & 1u;
+        if (nd.leaf_begin >= 0) {
+            for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
+                if (!in) continue;
+                const int32_t tri = ctx.kd_order[k];
+                const Tri64& t = ctx.t64[tri];
+                if (overlaps64(R, x, y, t)) {
+                    ++pairs;
+                    if (cl.z < t.bb[5]) drop_triangle64(ctx.cp, cl, t, ctx.t32[tri].flags, &capped);
+                }
+            }
+            continue;
+        }
+        bool vh, vl;
+        if ((nd.dim & 1) == 0) {
+            const bool only_lo = nd.cut > bb[nd.dim + 1];
+            vh = in && !only_lo && nd.hi >= 0;
+            vl = in && nd.lo >= 0;
+        } else {
+            const bool only_hi = nd.cut < bb[nd.dim - 1];
+            vh = in && nd.hi >= 0;
+            vl = in && !only_hi && nd.lo >= 0;
+        }
+        const unsigned mh = __ballot_sync(0xffffffffu, vh), ml = __ballot_sync(0xffffffffu, vl);
+        if (lane == 0) {
+            if (ml) st[sp] = make_uint2((unsigned)nd.lo, ml);
+            if (mh) st[sp + (ml ? 1 : 0)] = make_uint2((unsigned)nd.hi, mh);
+        }
+        sp += (ml ? 1 : 0) + (mh ? 1 : 0);
+        __syncwarp();
+    }
+    if (active) {
+        uint32_t o = ctx.perm[i];
+        ctx.out_z[o] = cl.z;
+        ctx.out_cc[3 * o] = cl.cc.x;
+        ctx.out_cc[3 * o + 1] = cl.cc.y;
+        ctx.out_cc[3 * o + 2] = cl.cc.z;
+        ctx.out_type[o] = cl.type;
+    }
+    for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    for (int o = 16; o > 0; o >>= 1) capped += __shfl_xor_sync(0xffffffffu, capped, o);
+    if (lane == 0) {
+        atomicAdd(&ctx.counters[C_PAIRS], pairs);
+        if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 screen
+// ---------------------------------------------------------------------------
+constexpr int SCREEN_WARPS = 4;
+
+enum ScanPhase { PH_SINGLE = 0, PH_LOWER = 1, PH_THRESH = 2, PH_COLLECT = 3 };
+
+struct LaneState {
+    float blo;       // certified lower bound of the final height
+    float qthr;      // lowest branch threshold of a relevant cone triangle
+    float thr;       // collection threshold (PH_COLLECT)
+    int nc;
+    bool overflow;
+    bool chain;      // a collected triangle's branch depends on uncollected ones
+    unsigned long long screened;
+};
+
+struct ScanShared {
+    float hlb[HLB_N];
+    Entry ent[SCREEN_WARPS][32];
+    uint32_t tri[SCREEN_WARPS][CAND_K][32];
+    float hi[SCREEN_WARPS][CAND_K][32];
+};
+
+// One pass over the cells under the warp's footprint (centre rows first).
+__device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
+                                           float cx, float cy, float z0l, int c0, int c1, int r0, int r1, int rc,
+                                           int cc) {
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const GridP& g = ctx.g;
+    const float R = ctx.prof.R;
+    const float gd = ctx.guard;
+    const float Rg = R + gd;
+    const float inv_step = (float)HLB_N / R;
+    const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
+    for (int kr = 0; kr < nr; ++kr) {
+        const int r = centre_out(kr, rc, r0, r1);
+        for (int kc = 0; kc < ncl; ++kc) {
+            const int c = centre_out(kc, cc, c0, c1);
+            const Cell cell = ctx.cells[r * g.ncol + c];
+            if (cell.count == 0) continue;
+            // the threshold below which a triangle is of no interest in this phase
+            const float cut = (phase == PH_COLLECT) ? ls.thr : ls.blo;
+            float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
+            float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
+            float d = sqrtf(dx * dx + dy * dy);
+            bool pass = active && d <= Rg && cell.maxz - hlb_at(sh.hlb, d - gd, inv_step) >= cut - gd;
+            if (!__any_sync(0xffffffffu, pass)) continue;
+            for (uint32_t j0 = 0; j0 < cell.count; j0 += 32) {
+                const int nj = min(32, (int)(cell.count - j0));
+                __syncwarp();
+                if (lane < nj) sh.ent[wl][lane] = ctx.entries[cell.start + j0 + lane];
+                __syncwarp();
+                for (int jj = 0; jj < nj; ++jj) {
+                    const Entry e = sh.ent[wl][jj];
+                    if (e.col != max((int)e.tcol0, c0) || r != max((int)e.trow0, r0)) continue;
+                    const float cut2 = (phase == PH_COLLECT) ? ls.thr : ls.blo;
+                    float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                    float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                    float de = sqrtf(ex * ex + ey * ey);
+                    float ub = e.maxz - hlb_at(sh.hlb, de - gd, inv_step);
+                    bool p1 = active && de <= Rg && ub >= cut2 - gd && ub > z0l - gd;
+                    if (!__any_sync(0xffffffffu, p1)) continue;
+                    if (!p1) continue;
+                    float lo = NEG_INF32, hi = ub + gd, qt = 3.0e38f;
+                    if (!ctx.composite_screen) {
+                        const Tri32 t = ctx.t32[e.tri];
+                        Iv v = screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt);
+                        ++ls.screened;
+                        lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
+                        hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, hi) : NEG_INF32;
+                        if (qt < 3.0e38f) qt = qt + t.v0[2] - ctx.E;
+                    }
+                    if (phase == PH_SINGLE || phase == PH_LOWER) {
+                        if (lo > ls.blo) ls.blo = lo;
+                    }
+                    if (phase == PH_THRESH) {
+                        if (hi >= ls.blo - gd && qt < ls.qthr) ls.qthr = qt;
+                        continue;
+                    }
+                    if (phase == PH_LOWER) continue;
+                    // collect (PH_SINGLE: lazily pruned against the rising bound)
+                    const float keep = (phase == PH_COLLECT) ? ls.thr : ls.blo;
+                    if (!(hi >= keep - gd && hi > z0l - gd) || ls.overflow) continue;
+                    if (phase == PH_COLLECT && qt < ls.thr - gd) ls.chain = true;
+                    if (ls.nc == CAND_K) {
+                        int w = 0;
+                        for (int q = 0; q < CAND_K; ++q) {
+                            float hq = sh.hi[wl][q][lane];
+                            if (hq >= keep - gd) {
+                                sh.tri[wl][w][lane] = sh.tri[wl][q][lane];
+                                sh.hi[wl][w][lane] = hq;
+                                ++w;
+                            }
+                        }
+                        ls.nc = w;
+                    }
+                    if (ls.nc < CAND_K) {
+                        sh.tri[wl][ls.nc][lane] = (uint32_t)e.tri;
+                        sh.hi[wl][ls.nc][lane] = hi;
+                        ++ls.nc;
+                    } else {
+                        ls.overflow = true;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// quirky: the cutter's per-triangle effect depends on the running height
+// (cone tip/rim short-circuits), so the collection threshold is closed over
+// the branch thresholds of the relevant triangles (three passes).
+template <bool QUIRKY>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const DropCtx* __restrict__ ctxp) {
+    const DropCtx& ctx = *ctxp;
+    __shared__ ScanShared sh;
+    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int base = (blockIdx.x * SCREEN_WARPS + wl) * 32;
+    if (base >= ctx.M) return;
+    const bool active = base + lane < ctx.M;
+    const uint32_t i = (uint32_t)(active ? base + lane : base);
+    const GridP& g = ctx.g;
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
+    const float z0l = __double2float_rd(z0 - g.oz);
+    const float gd = ctx.guard;
+    LaneState ls;
+    ls.blo = z0l;
+    ls.qthr = 3.0e38f;
+    ls.thr = 0.0f;
+    ls.nc = 0;
+    ls.overflow = false;
+    ls.chain = false;
+    ls.screened = 0;
+    double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
+    double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
+    int c0, c1, r0, r1;
+    if (warp_rect(g, xmin, xmax, ymin, ymax, ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius), c0, c1, r0, r1)) {
+        const int rc = clampi((int)floor((0.5 * (ymin + ymax) - g.y0) * g.inv_cs), r0, r1);
+        const int cc = clampi((int)floor((0.5 * (xmin + xmax) - g.x0) * g.inv_cs), c0, c1);
+        if (!QUIRKY) {
+            scan_cells(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            ls.thr = ls.blo;
+        } else {
+            scan_cells(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            ls.thr = fminf(ls.blo, ls.qthr);
+            scan_cells(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+        }
+    } else {
+        ls.thr = ls.blo;
+    }
+    __syncwarp();
+    if (active) {
+        if (ls.overflow || ls.chain) {
+            ctx.ncand[i] = 0xFF;
+        } else {
+            int w = 0;
+            for (int q = 0; q < ls.nc; ++q) {
+                float hq = sh.hi[wl][q][lane];
+                if (hq >= ls.thr - gd) ctx.cand[(size_t)i * CAND_K + w++] = sh.tri[wl][q][lane];
+            }
+            ctx.ncand[i] = (uint8_t)w;
+        }
+        ctx.blo[i] = ls.blo;
+    }
+    unsigned long long scr = ls.screened;
+    for (int o = 16; o > 0; o >>= 1) scr += __shfl_xor_sync(0xffffffffu, scr, o);
+    if (lane == 0 && scr) atomicAdd(&ctx.counters[C_SCREENED], scr);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 refinement: one thread per CL point folds its candidates in the
+// reference's visit order (ascending KD rank) against a running height, as
+// dropCutter5 does over its KD candidates.  Triangles left out can neither
+// reach the final height nor change a branch choice of a collected triangle.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_drop_refine(const DropCtx* __restrict__ ctxp) {
+    const DropCtx& ctx = *ctxp;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)ctx.M) return;
+    const int n = ctx.ncand[i];
+    if (n == 0xFF) return;  // handed to the plain path
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const double R = ctx.cp.radius;
+    uint32_t tri[CAND_K], rank[CAND_K];
+    for (int q = 0; q < n; ++q) {
+        tri[q] = ctx.cand[(size_t)i * CAND_K + q];
+        rank[q] = ctx.t32[tri[q]].kd_rank;
+    }
+    // insertion sort by KD rank
+    for (int a = 1; a < n; ++a) {
+        uint32_t t = tri[a], rk = rank[a];
+        int b = a - 1;
+        while (b >= 0 && rank[b] > rk) {
+            tri[b + 1] = tri[b];
+            rank[b + 1] = rank[b];
+            --b;
+        }
+        tri[b + 1] = t;
+        rank[b + 1] = rk;
+    }
+    CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
+    int capped = 0;
+    for (int q = 0; q < n; ++q) {
+        const Tri64& t = ctx.t64[tri[q]];
+        if (overlaps64(R, x, y, t) && cl.z < t.bb[5]) drop_triangle64(ctx.cp, cl, t, ctx.t32[tri[q]].flags, &capped);
+    }
+    const uint32_t o = ctx.perm[i];
+    ctx.out_z[o] = cl.z;
+    ctx.out_cc[3 * o] = cl.cc.x;
+    ctx.out_cc[3 * o + 1] = cl.cc.y;
+    ctx.out_cc[3 * o + 2] = cl.cc.z;
+    ctx.out_type[o] = cl.type;
+    // self-check: the FP64 result may not fall below the certified FP32 bound
+    const double lb = (double)ctx.blo[i] + ctx.g.oz;
+    if (cl.z < lb - 1e-9 * (1.0 + fabs(lb))) atomicAdd(&ctx.counters[C_VIOLATION], 1ull);
+    if (n) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)n);
+    if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+}
+
+__global__ void k_collect_overflow(const uint8_t* ncand, int M, uint32_t* list, unsigned long long* counter) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    if (ncand[i] == 0xFF) {
+        unsigned long long slot = atomicAdd(counter, 1ull);
+        list[slot] = (uint32_t)i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+// Cutters whose per-triangle drop depends on the running height: the cone
+// (tip/rim short-circuit) and composites.
+static bool quirky_cutter(const CutterP& cp) {
+    if (cp.kind == OCL_CUTTER_CONE) return true;
+    if (cp.kind == OCL_CUTTER_COMPOSITE) return true;
+    return false;
+}
+
+struct DropWork {
+    DevBuf<uint32_t> keys, keys2, perm0, perm;
+    DevBuf<double> cls;
+    DevBuf<uint32_t> cand;
+    DevBuf<uint8_t> ncand;
+    DevBuf<float> blo;
+    DevBuf<uint32_t> list;
+    DevBuf<unsigned long long> counters;
+    DevBuf<uint8_t> sort_tmp;
+    DevBuf<DropCtx> ctx;
+    DropCtx* host_ctx = nullptr;  // pinned staging copy of the launch context
+    size_t cap = 0;
+    bool ensure(size_t M, size_t sort_bytes) {
+        if (M > cap || !counters.p) {
+            size_t c = std::max<size_t>(M, 1024);
+            if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
+                !cand.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) ||
+                !counters.alloc(C_NCOUNTERS + 1) || !ctx.alloc(1))
+                return false;
+            cap = c;
+        }
+        if (sort_bytes > sort_tmp.n && !sort_tmp.alloc(sort_bytes)) return false;
+        return true;
+    }
+};
+
+static thread_local DropWork* tl_work = nullptr;
+
+int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
+             int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats) {
+    if (M == 0) return OCL_GB300_OK;
+    if (M >= (1ull << 31)) {
+        set_error("too many CL points");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (!tl_work) tl_work = new DropWork();
+    DropWork& w = *tl_work;
+    size_t sort_bytes = 0;
+    CK(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, w.keys.p, w.keys2.p, w.perm0.p, w.perm.p, (int64_t)M, 0,
+                                       32, stream));
+    if (!w.ensure(M, sort_bytes)) return OCL_GB300_OOM;
+
+    if (!w.host_ctx) {
+        if (cudaMallocHost(&w.host_ctx, sizeof(DropCtx)) != cudaSuccess) return OCL_GB300_OOM;
+    }
+    // the previous call's copy of the context must have left the staging buffer
+    CK(cudaStreamSynchronize(stream));
+    DropCtx* h = w.host_ctx;
+    std::memset(h, 0, sizeof(DropCtx));
+    h->cp = cp;
+    h->g = m.grid;
+    h->cells = m.d_cells;
+    h->entries = m.d_entries;
+    h->t64 = m.d_t64;
+    h->t32 = m.d_t32;
+    h->cl = w.cls.p;
+    h->perm = w.perm.p;
+    h->M = (int)M;
+    h->out_z = d_z;
+    h->out_cc = d_cc;
+    h->out_type = d_type;
+    h->cand = w.cand.p;
+    h->ncand = w.ncand.p;
+    h->blo = w.blo.p;
+    h->counters = w.counters.p;
+    h->kd_nodes = m.drop_kd.d_nodes;
+    h->kd_order = m.drop_kd.d_order;
+    bool composite = false;
+    fill_prof(cp, h->prof, h->hlb, composite);
+    h->composite_screen = composite;
+    double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
+    double maxabs = half + cp.radius + 1.0;
+    h->E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
+    h->guard = 4.0f * h->E + 1e-5f * (float)cp.radius;
+
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, stream));
+    CK(cudaMemcpyAsync(w.ctx.p, h, sizeof(DropCtx), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(w.counters.p, 0, (C_NCOUNTERS + 1) * sizeof(unsigned long long), stream));
+    const int TB = 256;
+    const unsigned nb = (unsigned)((M + TB - 1) / TB);
+    double ex = std::max(m.bb[1] - m.bb[0], 1e-9), ey = std::max(m.bb[3] - m.bb[2], 1e-9);
+    double sx = 65535.0 / (ex + 2 * cp.radius), sy = 65535.0 / (ey + 2 * cp.radius);
+    k_morton<<<nb, TB, 0, stream>>>(d_cl, M, m.bb[0] - cp.radius, m.bb[2] - cp.radius, sx, sy, w.keys.p, w.perm0.p);
+    CK(cub::DeviceRadixSort::SortPairs(w.sort_tmp.p, sort_bytes, w.keys.p, w.keys2.p, w.perm0.p, w.perm.p,
+                                       (int64_t)M, 0, 32, stream));
+    k_gather_cl<<<nb, TB, 0, stream>>>(d_cl, w.perm.p, M, w.cls.p);
+    if (m.n == 0) {
+        // empty surface: every point keeps its z, CC stays NONE
+        CK(cudaMemsetAsync(w.ncand.p, 0, M, stream));
+        CK(cudaMemsetAsync(w.blo.p, 0xFF, M * sizeof(float), stream));
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(w.ctx.p);
+    } else if (precision == OCL_GB300_PREC_FP64) {
+        const unsigned warps = (unsigned)((M + 31) / 32);
+        k_drop_kd<<<(warps + 3) / 4, 128, 0, stream>>>(w.ctx.p, nullptr, (int)M);
+    } else {
+        const unsigned warps = (unsigned)((M + 31) / 32);
+        const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
+        if (quirky_cutter(cp))
+            k_drop_screen<true><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(w.ctx.p);
+        else
+            k_drop_screen<false><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(w.ctx.p);
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(w.ctx.p);
+        k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
+        unsigned long long nover = 0;
+        CK(cudaMemcpyAsync(&nover, w.counters.p + C_FALLBACK, sizeof(nover), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (nover > 0) {
+            const unsigned warps2 = (unsigned)((nover + 31) / 32);
+            k_drop_kd<<<(warps2 + 3) / 4, 128, 0, stream>>>(w.ctx.p, w.list.p, (int)nover);
+        }
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e1, stream));
+    if (stats) {
+        unsigned long long c[C_NCOUNTERS];
+        CK(cudaMemcpyAsync(c, w.counters.p, sizeof(c), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats->pairs = c[C_PAIRS];
+        stats->refined = c[C_REFINED];
+        stats->iter_limit_hits = c[C_CAPPED];
+        stats->kernel_ms = ms;
+        stats->fallback = c[C_FALLBACK];
+        stats->violations = c[C_VIOLATION];
+        stats->screened = c[C_SCREENED];
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return OCL_GB300_OK;
+}
+
+}  // namespace oclg

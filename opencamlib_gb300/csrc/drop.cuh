@@ -1,0 +1,59 @@
+// drop.cuh -- drop-cutter launch interface.
+#pragma once
+#include "geom32.cuh"
+#include "mesh.cuh"
+
+namespace oclg {
+
+constexpr int HLB_N = 256;   // entries of the height lower-bound table
+constexpr int CAND_K = 24;   // refinement candidates kept per CL point
+
+enum Counter {
+    C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)
+    C_REFINED = 1,    // FP64 triangle evaluations in the refinement stage
+    C_FALLBACK = 2,   // CL points whose candidate list overflowed
+    C_VIOLATION = 3,  // FP64 result below a certified FP32 lower bound (must stay 0)
+    C_CAPPED = 4,     // Brent solves that hit the iteration cap
+    C_SCREENED = 5,   // FP32 whole-triangle screens
+    C_NCOUNTERS = 8
+};
+
+struct DropCtx {
+    CutterP cp;
+    Prof32 prof;
+    GridP g;
+    const Cell* cells;
+    const Entry* entries;
+    const Tri64* t64;
+    const Tri32* t32;
+    const KDNodeD* kd_nodes;  // XY KD tree of the plain path
+    const int32_t* kd_order;
+    const double* cl;       // sorted CL points (M x 3)
+    const uint32_t* perm;   // sorted -> caller index
+    int M;
+    double* out_z;
+    double* out_cc;
+    int32_t* out_type;
+    uint32_t* cand;         // M x CAND_K candidate triangles
+    uint8_t* ncand;         // per CL: count, or 0xFF = overflow
+    float* blo;             // per CL: certified lower bound (local frame)
+    unsigned long long* counters;
+    float E;                // FP32 position error budget
+    float guard;            // margin for the bound tests
+    bool composite_screen;  // composite cutter: no FP32 whole-triangle screen
+    float hlb[HLB_N];       // lower bound of height(r) on [k R / HLB_N, R]
+};
+
+struct DropWork;
+int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
+             int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats);
+
+// Cutter parameters from the ABI description (the reference constructors'
+// arithmetic); returns an OCL_GB300_* status.
+int make_cutter_params(const ocl_gb300_cutter& in, CutterP& cp);
+// FP32 profile and the height lower-bound table for the screen.
+void fill_prof(const CutterP& cp, Prof32& prof, float* hlb, bool& composite);
+// Host FP64 cutter height(r) (same arithmetic as the device).
+double height_host(const CutterP& cp, double r);
+
+}  // namespace oclg

@@ -1,0 +1,328 @@
+// geom32.cuh -- FP32 screening of (CL point, triangle) pairs.
+//
+// For one triangle the screen returns an interval [lo, hi] that contains the
+// triangle's FP64 drop contribution as the reference defines it
+// (MillingCutter::dropCutter, cutters/millingcutter.cpp:386-409: the facet
+// contact when it lifts, else the best vertex/edge contact):
+//   lo = -inf unless some contact is certain; hi = -inf when none is possible.
+// Coordinates are local to the triangle's first vertex, so FP32 only carries
+// differences of nearby points.  Every predicate that decides validity
+// (point in triangle, CC inside an edge, distance <= radius) is evaluated
+// with a margin: a clear decision is kept, a marginal one widens [lo, hi] to
+// cover both outcomes.  Monotone functions (the cutter profile height(r)) are
+// evaluated at the ends of the input's error interval instead of through a
+// derivative.  The error budget E0 bounds the absolute position error of the
+// local coordinates; it is set per mesh from its extent.
+#pragma once
+#include "common.cuh"
+
+namespace oclg {
+
+#define NEG_INF32 (-3.0e38f)
+
+struct Iv {
+    float lo, hi;
+};
+__device__ __forceinline__ Iv iv_none() { return Iv{NEG_INF32, NEG_INF32}; }
+__device__ __forceinline__ void iv_max(Iv& a, Iv b) {
+    a.lo = fmaxf(a.lo, b.lo);
+    a.hi = fmaxf(a.hi, b.hi);
+}
+
+// FP32 copy of the cutter profile.
+struct Prof32 {
+    int kind;
+    float R, r1, r2, inv_tan, center_height, length;
+    float xynl, nl;  // xy_normal_length, normal_length
+};
+
+// height(r) in FP32 for r in [0, R] (monotone non-decreasing in r).
+__device__ __forceinline__ float h32(const Prof32& c, float r) {
+    r = fmaxf(r, 0.0f);
+    switch (c.kind) {
+    case OCL_CUTTER_CYL: return 0.0f;
+    case OCL_CUTTER_BALL: {
+        float a = fmaxf(c.R * c.R - r * r, 0.0f);
+        return c.R - sqrtf(a);
+    }
+    case OCL_CUTTER_BULL: {
+        if (r <= c.r1) return 0.0f;
+        float q = fminf(r - c.r1, c.r2);
+        return c.r2 - sqrtf(fmaxf(c.r2 * c.r2 - q * q, 0.0f));
+    }
+    case OCL_CUTTER_CONE: return r * c.inv_tan;
+    }
+    return 0.0f;
+}
+// derivative h'(r) (>= 0), used for the edge maximisation.
+__device__ __forceinline__ float dh32(const Prof32& c, float r) {
+    switch (c.kind) {
+    case OCL_CUTTER_BALL: {
+        float a = fmaxf(c.R * c.R - r * r, 1e-30f);
+        return r * rsqrtf(a);
+    }
+    case OCL_CUTTER_BULL: {
+        if (r <= c.r1) return 0.0f;
+        float q = r - c.r1;
+        float a = fmaxf(c.r2 * c.r2 - q * q, 1e-30f);
+        return q * rsqrtf(a);
+    }
+    case OCL_CUTTER_CONE: return c.inv_tan;
+    }
+    return 0.0f;
+}
+
+// Vertex drop of one vertex at local (dx, dy) from the CL point, height pz.
+__device__ __forceinline__ Iv vertex32(const Prof32& c, float dx, float dy, float pz, float E) {
+    float q = sqrtf(dx * dx + dy * dy);
+    float qlo = q - E, qhi = q + E;
+    if (qlo > c.R) return iv_none();
+    Iv r;
+    r.hi = pz - h32(c, fmaxf(qlo, 0.0f)) + E;
+    if (c.kind == OCL_CUTTER_CYL) {
+        r.lo = (qhi < c.R) ? pz - E : NEG_INF32;
+    } else {
+        r.lo = (qhi <= c.R) ? pz - h32(c, qhi) - E : NEG_INF32;
+    }
+    return r;
+}
+
+// Barycentric position of local point (x, y) in the triangle (0, e1, e2):
+// returns 1 = clearly inside, -1 = clearly outside, 0 = marginal.
+__device__ __forceinline__ int inside32(const Tri32& t, float x, float y, float eps_b) {
+    float det = t.e1[0] * t.e2[1] - t.e1[1] * t.e2[0];
+    float inv = 1.0f / det;
+    float u = (x * t.e2[1] - y * t.e2[0]) * inv;
+    float v = (t.e1[0] * y - t.e1[1] * x) * inv;
+    float w = 1.0f - u - v;
+    float m = fminf(u, fminf(v, w));
+    if (m > eps_b) return 1;
+    if (m < -eps_b) return -1;
+    return 0;
+}
+
+// Combine a candidate contact of value [vlo, vhi] with its validity state.
+__device__ __forceinline__ Iv gate(int state, float vlo, float vhi) {
+    if (state > 0) return Iv{vlo, vhi};
+    if (state < 0) return iv_none();
+    return Iv{NEG_INF32, vhi};
+}
+
+// Facet contact for cylindrical/spherical/toroidal cutters
+// (MillingCutter::facetDrop, millingcutter.cpp:51-75), local frame.
+__device__ __forceinline__ Iv facet32(const Prof32& c, const Tri32& t, float wx, float wy, float E, float eps_b) {
+    uint32_t mode = t.flags & TF_FACET_MASK;
+    if (mode == TF_FACET_NONE) return iv_none();
+    if (mode == TF_FACET_HORIZ) {
+        int s = inside32(t, wx, wy, eps_b);
+        return gate(s, -E, E);
+    }
+    float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
+    float xyl = sqrtf(nx * nx + ny * ny);
+    float xnx = nx / xyl, xny = ny / xyl;
+    float rvx = c.xynl * xnx + c.nl * nx;
+    float rvy = c.xynl * xny + c.nl * ny;
+    float rvz = c.nl * nz;
+    float ccx = wx - rvx, ccy = wy - rvy;
+    float zc = -(nx * ccx + ny * ccy) / nz;
+    float tip = zc + rvz - c.center_height;
+    float err = E * (2.0f + (fabsf(nx) + fabsf(ny)) / nz);
+    int s = inside32(t, ccx, ccy, eps_b);
+    return gate(s, tip - err, tip + err);
+}
+
+// Edge contact in the canonical frame for one edge a->b (local coords).
+// Cyl/ball/cone use the reference's closed forms (cylcutter.cpp:52-70,
+// ballcutter.cpp:50-63, conecutter.cpp:109-135); for the bull the contact is
+// the maximum of the concave function f(u) = z(u) - height(rho(u)) along the
+// edge line, which is what the offset-ellipse solve of bullcutter.cpp:82-105
+// finds; it is bracketed by bisection on f'.
+__device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float bx, float by, float bz, float wx, float wy,
+                     float E, bool horiz) {
+    float dx = bx - ax, dy = by - ay;
+    float L = sqrtf(dx * dx + dy * dy);
+    float ux = dx / L, uy = dy / L;
+    // CL relative to a
+    float px = wx - ax, py = wy - ay;
+    float d = fabsf(ux * py - uy * px);  // distance CL -> line
+    if (d - E > c.R) return iv_none();
+    float along = ux * px + uy * py;  // projection of CL on the line, from a
+    float u1 = -along;                // a in canonical coordinates
+    float u2 = L - along;             // b
+    float m = (bz - az) / L;          // dz/du
+    float dm = fminf(d, c.R);
+    float s2 = c.R * c.R - dm * dm;
+    float s = sqrtf(fmaxf(s2, 0.0f));
+    float ccu, clz, err;
+    int kind = c.kind;
+    // E_u: uncertainty of the contact's position along the edge
+    float Eu;
+    if (kind == OCL_CUTTER_CYL) {
+        // cc at +-s, pick the higher
+        float z1 = az + (s - u1) * m, z2 = az + (-s - u1) * m;
+        if (z1 > z2) { ccu = s; clz = z1; } else { ccu = -s; clz = z2; }
+        // ds/dd = d/s: position error grows near tangency
+        float dsdd = (s > 1e-6f * c.R) ? dm / s : 1e6f;
+        Eu = E * (2.0f + dsdd);
+        err = E * (2.0f + fabsf(m) * (1.0f + dsdd));
+    } else if (kind == OCL_CUTTER_BALL) {
+        float n0 = bz - az, n1 = -(u2 - u1);
+        float nl = sqrtf(n0 * n0 + n1 * n1);
+        n0 /= nl;
+        n1 /= nl;
+        if (n1 < 0) { n0 = -n0; n1 = -n1; }
+        ccu = -s * n0;
+        clz = az + (ccu - u1) * m + s * n1 - c.R;
+        float dsdd = (s > 1e-6f * c.R) ? dm / s : 1e6f;
+        Eu = E * (2.0f + dsdd);
+        err = E * (3.0f + fabsf(m) + dsdd);
+    } else if (kind == OCL_CUTTER_CONE) {
+        float xu = s;
+        float mu = (c.center_height / c.R) * xu / sqrtf(fmaxf(xu * xu + dm * dm, 1e-30f));
+        float am = fabsf(m), amu = fabsf(mu);
+        float sg = m < 0 ? -1.0f : 1.0f;
+        // reference formula: hyperbola case uses length^2 (conecutter.cpp:122)
+        float den = c.length * c.length - c.R * c.R * m * m;
+        float cu_h = sg * sqrtf(fmaxf(c.R * c.R * m * m * dm * dm / den, 0.0f));
+        float z_h = az + (cu_h - u1) * m - c.center_height + (c.R - sqrtf(cu_h * cu_h + dm * dm)) * c.inv_tan;
+        float cu_r = sg * xu;
+        float z_r = az + (cu_r - u1) * m - c.center_height;
+        float dsdd = (s > 1e-6f * c.R) ? dm / s : 1e6f;
+        float e0 = E * (3.0f + (am + c.inv_tan) * (2.0f + dsdd));
+        float band = 1e-4f * (1.0f + amu);
+        Iv r;
+        if (am < amu - band) { ccu = cu_h; clz = z_h; }
+        else if (am > amu + band) { ccu = cu_r; clz = z_r; }
+        else {
+            // marginal case split: cover both outcomes, CC test on both
+            float lo = fminf(z_h, z_r) - e0, hi = fmaxf(z_h, z_r) + e0;
+            float t1 = (cu_h - u1) / (u2 - u1), t2 = (cu_r - u1) / (u2 - u1);
+            float et = (E * (2.0f + dsdd) + 1e-6f) / L;
+            bool in1 = t1 > et && t1 < 1 - et, in2 = t2 > et && t2 < 1 - et;
+            bool out1 = t1 < -et || t1 > 1 + et, out2 = t2 < -et || t2 > 1 + et;
+            r.lo = (in1 && in2) ? lo : NEG_INF32;
+            r.hi = (out1 && out2) ? NEG_INF32 : hi;
+            if (d + E > c.R && r.lo > NEG_INF32) r.lo = NEG_INF32;
+            return r;
+        }
+        Eu = E * (2.0f + dsdd) + 1e-5f * c.R;
+        err = e0;
+    } else {  // bull
+        if (horiz) {
+            ccu = 0.0f;
+            clz = az - h32(c, dm);
+            Eu = E;
+            err = E * 2.0f;
+            // height is monotone: bracket by d +- E
+            float hlo = h32(c, fminf(dm + E, c.R)), hhi = h32(c, fmaxf(dm - E, 0.0f));
+            float tcc = (ccu - u1) / (u2 - u1);
+            float et = (Eu + 1e-6f) / L;
+            int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
+            if (d + E > c.R && st > 0) st = 0;
+            return gate(st, az - hlo - 2.0f * E, az - hhi + 2.0f * E);
+        }
+        // maximise f(u) = az + (u - u1) m - h(sqrt(u^2 + d^2)) on |u| < s
+        float lo_u = -s, hi_u = s;
+        for (int it = 0; it < 20; ++it) {
+            float mid = 0.5f * (lo_u + hi_u);
+            float rho = sqrtf(mid * mid + dm * dm);
+            float fp = m - dh32(c, rho) * (rho > 0 ? mid / rho : 0.0f);
+            if (fp > 0) lo_u = mid; else hi_u = mid;
+        }
+        ccu = 0.5f * (lo_u + hi_u);
+        float rho = sqrtf(ccu * ccu + dm * dm);
+        clz = az + (ccu - u1) * m - h32(c, rho);
+        // concave: f(max) <= f(lo_u) + f'(lo_u) (hi_u - lo_u)
+        float rl = sqrtf(lo_u * lo_u + dm * dm);
+        float fpl = fabsf(m - dh32(c, rl) * (rl > 0 ? lo_u / rl : 0.0f));
+        float slack = fminf(fpl * (hi_u - lo_u), 1.0f);
+        // sensitivity of the maximum to the line offset d
+        float rd = rho > 1e-20f ? dm / rho : 0.0f;
+        err = E * (3.0f + fabsf(m) + dh32(c, fminf(rho + E, c.R)) * (1.0f + rd)) + slack;
+        float curv = 1.0f + dh32(c, fminf(rho + 4.0f * E, c.R));
+        Eu = E * (2.0f + curv) + 1e-4f * c.r2;
+    }
+    // CC inside the segment (Point::isInside(p1,p2), param in [0,1])
+    float tcc = (ccu - u1) / (u2 - u1);
+    float et = (Eu + 1e-6f) / L;
+    int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
+    if (d + E > c.R && st > 0) st = 0;  // d <= radius is marginal
+    return gate(st, clz - err, clz + err);
+}
+
+// Whole-triangle screen for the basic cutters, local frame (relative to v0).
+// Returns the interval of the triangle's effect on the running z
+// (dropCutter applied to a CL point already at some height Z >= z0).
+// qthr receives the lowest running height at which the reference's branch
+// choice for this triangle could change (cone tip/rim short-circuits), or
+// +inf when the triangle's effect is a plain max (order-independent).
+__device__ inline Iv screen_triangle(const Prof32& c, const Tri32& t, float wx, float wy, float E, float z0_rel,
+                                     float& qthr) {
+    const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
+    qthr = 3.0e38f;
+    // vertices
+    Iv best = vertex32(c, -wx, -wy, 0.0f, E);
+    iv_max(best, vertex32(c, t.e1[0] - wx, t.e1[1] - wy, t.e1[2], E));
+    iv_max(best, vertex32(c, t.e2[0] - wx, t.e2[1] - wy, t.e2[2], E));
+    // edges
+    const float px[3] = {0.0f, t.e1[0], t.e2[0]};
+    const float py[3] = {0.0f, t.e1[1], t.e2[1]};
+    const float pz[3] = {0.0f, t.e1[2], t.e2[2]};
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        if (t.flags & (TF_EDGE0_SKIP << n)) continue;
+        const int k = (n + 1) % 3;
+        const bool horiz = (t.flags & (TF_EDGE0_HORIZ << n)) != 0;
+        iv_max(best, edge32(c, px[n], py[n], pz[n], px[k], py[k], pz[k], wx, wy, E, horiz));
+    }
+    if (c.kind == OCL_CUTTER_CONE) {
+        // ConeCutter::facetDrop (conecutter.cpp:70-105): the tip contact, when
+        // it lifts, ends the triangle; otherwise the rim, otherwise vertices
+        // and edges.  With a running height Z: tip if Z < tip, rim if
+        // tip <= Z < rim, else max(Z, vertex/edge).
+        uint32_t mode = t.flags & TF_FACET_MASK;
+        if (mode == TF_FACET_NONE) return best;
+        Iv tip, rim;
+        int st_tip, st_rim;
+        if (mode == TF_FACET_HORIZ) {
+            st_tip = inside32(t, wx, wy, eps_b);
+            tip = Iv{-E, E};
+            st_rim = -1;
+            rim = iv_none();
+        } else {
+            float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
+            float slope = (fabsf(nx) + fabsf(ny)) / nz;
+            float xyl = sqrtf(nx * nx + ny * ny);
+            float zt = -(nx * wx + ny * wy) / nz;
+            float et = E * (2.0f + slope);
+            tip = Iv{zt - et, zt + et};
+            st_tip = inside32(t, wx, wy, eps_b);
+            float rx = wx - c.R * nx / xyl, ry = wy - c.R * ny / xyl;
+            float zr = -(nx * rx + ny * ry) / nz - c.length;
+            float er = E * (2.0f + slope * 2.0f);
+            rim = Iv{zr - er, zr + er};
+            st_rim = inside32(t, rx, ry, eps_b);
+        }
+        // a contact at or below the start height never lifts
+        if (st_tip >= 0 && tip.hi <= z0_rel) st_tip = -1;
+        if (st_tip > 0 && !(tip.lo > z0_rel)) st_tip = 0;
+        if (st_rim >= 0 && rim.hi <= z0_rel) st_rim = -1;
+        if (st_rim > 0 && !(rim.lo > z0_rel)) st_rim = 0;
+        float lo_after_tip =
+            st_rim > 0 ? rim.lo : (st_rim < 0 ? best.lo : fminf(rim.lo, best.lo));
+        Iv r;
+        r.lo = st_tip > 0 ? tip.lo : (st_tip < 0 ? lo_after_tip : fminf(tip.lo, lo_after_tip));
+        r.hi = best.hi;
+        if (st_tip >= 0) r.hi = fmaxf(r.hi, tip.hi);
+        if (st_rim >= 0) r.hi = fmaxf(r.hi, rim.hi);
+        if (st_tip >= 0 && fmaxf(best.hi, st_rim >= 0 ? rim.hi : NEG_INF32) > tip.lo) qthr = fminf(qthr, tip.lo);
+        if (st_rim >= 0 && best.hi > rim.lo) qthr = fminf(qthr, rim.lo);
+        return r;
+    }
+    // cyl/ball/bull: a lifting facet contact is the highest contact of the
+    // plane, so the effect is the maximum of all certain contacts.
+    iv_max(best, facet32(c, t, wx, wy, E, eps_b));
+    return best;
+}
+
+}  // namespace oclg

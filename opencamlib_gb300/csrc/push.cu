@@ -1,0 +1,341 @@
+// push.cu -- BatchPushCutter on the GPU (BatchPushCutter::pushCutter3,
+// algo/batchpushcutter.cpp:136-188).
+//
+// Lanes are fibers: a warp takes 32 consecutive fibers (a Waterline level's
+// fibers are adjacent), walks the KD tree of the fiber direction (YZ for
+// X-fibers, XZ for Y-fibers) with one visit mask per node, so every lane gets
+// exactly the reference's candidate triangles in the reference's order; each
+// candidate is pushed in FP64 (MillingCutter::pushCutter) and its interval is
+// merged into the lane's fiber with Fiber::addInterval's rules (fiber.cpp:58-93),
+// keeping the reference's interval order and CC points.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "drop.cuh"
+#include "push64.cuh"
+#include "util.cuh"
+
+namespace oclg {
+
+constexpr int PUSH_CAP = 48;        // intervals a fiber may hold while merging (first pass, local memory)
+constexpr int PUSH_CAP_BIG = 4096;  // second pass for the fibers that overflowed (global scratch)
+
+struct PushRec {
+    double lower, upper;
+    double lcc[3], ucc[3];
+    int32_t ltype, utype;
+};
+static_assert(sizeof(PushRec) == 72, "PushRec layout");
+
+struct PushCtx {
+    CutterP cp;
+    int dir;
+    const Tri64* t64;
+    const KDNodeD* nodes;
+    const int32_t* order;
+    const double* fib;
+    int F;
+    PushRec* recs;
+    uint64_t cap;
+    unsigned long long* cursor;
+    uint32_t* counts;
+    uint64_t* offs;
+    unsigned long long* counters;  // [0] calls, [1] capped, [2] merge overflow
+};
+
+__device__ __forceinline__ bool iv_outside(const Ival64& a, const Ival64& b) {
+    if (a.lower > b.upper) return true;
+    if (a.upper < b.lower) return true;
+    return false;
+}
+
+// Fiber::addInterval on a per-lane array; returns false on capacity overflow.
+__device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap) {
+    if (i.lower == 0.0 && i.upper == 0.0) return true;  // Interval::empty (interval.cpp:113-118)
+    if (n == 0) {
+        ints[n++] = i;
+        return true;
+    }
+    for (int k = 0; k < n; ++k)
+        if ((i.lower > ints[k].lower) && (i.upper < ints[k].upper)) return true;  // contains
+    bool missing = true;
+    for (int k = 0; k < n; ++k)
+        if (!iv_outside(i, ints[k])) missing = false;
+    if (missing) {
+        if (n == cap) return false;
+        ints[n++] = i;
+        return true;
+    }
+    // merge all overlapping intervals (in vector order) with i into one sum
+    Ival64 sum;
+    iv_init(sum);
+    int w = 0;
+    for (int k = 0; k < n; ++k) {
+        if (!iv_outside(ints[k], i)) {
+            iv_lower(sum, ints[k].lower, ints[k].lcc);
+            iv_upper(sum, ints[k].upper, ints[k].ucc);
+        } else {
+            ints[w++] = ints[k];
+        }
+    }
+    iv_lower(sum, i.lower, i.lcc);
+    iv_upper(sum, i.upper, i.ucc);
+    n = w;
+    ints[n++] = sum;
+    return true;
+}
+
+// list == nullptr: fibers 0..F-1 with the intervals in local memory;
+// otherwise the listed fibers with PUSH_CAP_BIG intervals each in scratch.
+__global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, const uint32_t* __restrict__ list,
+                                              int nlist, Ival64* __restrict__ scratch) {
+    const PushCtx& ctx = *ctxp;
+    __shared__ uint2 s_stack[4][KD_STACK];
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const int count = list ? nlist : ctx.F;
+    if (base >= count) return;
+    const bool active = base + lane < count;
+    const int slot = active ? base + lane : base;
+    const int f = list ? (int)list[slot] : slot;
+    Fib64 fb;
+    fb.p1 = d3(ctx.fib[6 * f], ctx.fib[6 * f + 1], ctx.fib[6 * f + 2]);
+    fb.p2 = d3(ctx.fib[6 * f + 3], ctx.fib[6 * f + 4], ctx.fib[6 * f + 5]);
+    fb.dir = normalize3(fb.p2 - fb.p1);  // Fiber::calcDir (fiber.cpp:35-39)
+    const double r = ctx.cp.radius;
+    // pushCutter3's search point and KDTree::search_cutter_overlap box
+    double clx, cly;
+    if (ctx.dir == OCL_GB300_XFIBER) { clx = 0; cly = fb.p1.y; }
+    else { clx = fb.p1.x; cly = 0; }
+    const double bb[6] = {clx - r, clx + r, cly - r, cly + r, fb.p1.z, fb.p1.z + ctx.cp.length};
+    Ival64 local_ints[PUSH_CAP];
+    Ival64* ints = list ? scratch + (size_t)slot * PUSH_CAP_BIG : local_ints;
+    const int cap = list ? PUSH_CAP_BIG : PUSH_CAP;
+    int n = 0;
+    bool overflow = false;
+    unsigned long long calls = 0;
+    int capped = 0;
+    uint2* st = s_stack[wl];
+    const unsigned amask = __ballot_sync(0xffffffffu, active);
+    int sp = 0;
+    if (ctx.nodes && amask) {
+        if (lane == 0) st[0] = make_uint2(0u, amask);
+        sp = 1;
+    }
+    __syncwarp();
+    while (sp > 0) {
+        --sp;
+        const uint2 e = st[sp];
+        __syncwarp();
+        const KDNodeD nd = ctx.nodes[e.x];
+        const bool in = (e.y >> lane) & 1u;
+        if (nd.leaf_begin >= 0) {
+            for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
+                if (!in) continue;
+                const Tri64& t = ctx.t64[ctx.order[k]];
+                Ival64 iv;
+                iv_init(iv);
+                push_triangle64(ctx.cp, fb, iv, t, &capped);
+                if (!overflow && !fiber_add(ints, n, iv, cap)) overflow = true;
+                ++calls;
+            }
+            continue;
+        }
+        bool vh, vl;
+        if ((nd.dim & 1) == 0) {
+            const bool only_lo = nd.cut > bb[nd.dim + 1];
+            vh = in && !only_lo && nd.hi >= 0;
+            vl = in && nd.lo >= 0;
+        } else {
+            const bool only_hi = nd.cut < bb[nd.dim - 1];
+            vh = in && nd.hi >= 0;
+            vl = in && !only_hi && nd.lo >= 0;
+        }
+        const unsigned mh = __ballot_sync(0xffffffffu, vh), ml = __ballot_sync(0xffffffffu, vl);
+        if (lane == 0) {
+            if (ml) st[sp] = make_uint2((unsigned)nd.lo, ml);
+            if (mh) st[sp + (ml ? 1 : 0)] = make_uint2((unsigned)nd.hi, mh);
+        }
+        sp += (ml ? 1 : 0) + (mh ? 1 : 0);
+        __syncwarp();
+    }
+    // reserve output slots for the warp
+    int cnt = active ? n : 0;
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    unsigned long long wbase = 0;
+    if (lane == 31) wbase = atomicAdd(ctx.cursor, (unsigned long long)incl);
+    wbase = __shfl_sync(0xffffffffu, wbase, 31);
+    const unsigned long long mine = wbase + (unsigned long long)(incl - cnt);
+    if (active) {
+        ctx.counts[f] = overflow ? 0xFFFFFFFFu : (uint32_t)n;
+        ctx.offs[f] = mine;
+        for (int k = 0; k < n; ++k) {
+            if (mine + k < ctx.cap) {
+                PushRec rec;
+                rec.lower = ints[k].lower;
+                rec.upper = ints[k].upper;
+                rec.lcc[0] = ints[k].lcc.p.x; rec.lcc[1] = ints[k].lcc.p.y; rec.lcc[2] = ints[k].lcc.p.z;
+                rec.ucc[0] = ints[k].ucc.p.x; rec.ucc[1] = ints[k].ucc.p.y; rec.ucc[2] = ints[k].ucc.p.z;
+                rec.ltype = ints[k].lcc.type;
+                rec.utype = ints[k].ucc.type;
+                ctx.recs[mine + k] = rec;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) calls += __shfl_xor_sync(0xffffffffu, calls, o);
+    for (int o = 16; o > 0; o >>= 1) capped += __shfl_xor_sync(0xffffffffu, capped, o);
+    int ov = overflow ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) ov += __shfl_xor_sync(0xffffffffu, ov, o);
+    if (lane == 0) {
+        atomicAdd(&ctx.counters[0], calls);
+        if (capped) atomicAdd(&ctx.counters[1], (unsigned long long)capped);
+        if (ov) atomicAdd(&ctx.counters[2], (unsigned long long)ov);
+    }
+}
+
+static int ensure_push_index(Mesh& m, int dir) {
+    PushIndex& pi = m.push[dir];
+    if (pi.built) return OCL_GB300_OK;
+    KDTreeD kd;
+    kd_build_host(m.host_bb, m.n, m.bucket, dir == OCL_GB300_XFIBER ? 1 : 2, kd);
+    return upload_kd(m, kd, pi);
+}
+
+int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t F, uint64_t* offsets, double* ival,
+             double* cc, int32_t* cctype, uint64_t cap, ocl_gb300_stats* stats) {
+    for (uint64_t k = 0; k < F; ++k) {
+        const double* f = fibers + 6 * k;
+        bool ok = std::isfinite(f[0]) && std::isfinite(f[1]) && std::isfinite(f[2]) && std::isfinite(f[3]) &&
+                  std::isfinite(f[4]) && std::isfinite(f[5]) && f[2] == f[5];
+        ok = ok && (dir == OCL_GB300_XFIBER ? (f[1] == f[4] && f[0] != f[3]) : (f[0] == f[3] && f[1] != f[4]));
+        if (!ok) {
+            set_error("fiber " + std::to_string(k) + " is not a horizontal fiber of the requested direction");
+            return OCL_GB300_BAD_ARG;
+        }
+    }
+    offsets[0] = 0;
+    if (F == 0) return OCL_GB300_OK;
+    if (m.n > 0) {
+        int st = ensure_push_index(m, dir);
+        if (st) return st;
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    DevBuf<double> dfib(6 * F);
+    DevBuf<uint32_t> dcounts(F);
+    DevBuf<uint64_t> doffs(F);
+    DevBuf<unsigned long long> dcnt(4);
+    DevBuf<PushCtx> dctx(1);
+    if (!dfib.ok() || !dcounts.ok() || !doffs.ok() || !dcnt.ok() || !dctx.ok()) return OCL_GB300_OOM;
+    CK(cudaMemcpy(dfib.p, fibers, 6 * F * sizeof(double), cudaMemcpyHostToDevice));
+    uint64_t rcap = std::max<uint64_t>(4 * F, 1024);
+    std::vector<PushRec> hrec;
+    std::vector<uint32_t> hcounts(F);
+    std::vector<uint64_t> hoffs(F);
+    unsigned long long hc[4] = {0, 0, 0, 0};
+    float ms = 0;
+    unsigned long long second_overflow = 0;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        DevBuf<PushRec> drec(rcap);
+        if (!drec.ok()) return OCL_GB300_OOM;
+        PushCtx h;
+        std::memset(&h, 0, sizeof(h));
+        h.cp = cp;
+        h.dir = dir;
+        h.t64 = m.d_t64;
+        h.nodes = m.n > 0 ? m.push[dir].d_nodes : nullptr;
+        h.order = m.n > 0 ? m.push[dir].d_order : nullptr;
+        h.fib = dfib.p;
+        h.F = (int)F;
+        h.recs = drec.p;
+        h.cap = rcap;
+        h.cursor = dcnt.p + 3;
+        h.counts = dcounts.p;
+        h.offs = doffs.p;
+        h.counters = dcnt.p;
+        CK(cudaMemcpy(dctx.p, &h, sizeof(h), cudaMemcpyHostToDevice));
+        CK(cudaMemset(dcnt.p, 0, 4 * sizeof(unsigned long long)));
+        const unsigned warps = (unsigned)((F + 31) / 32);
+        CK(cudaEventRecord(e0));
+        k_push<<<(warps + 3) / 4, 128>>>(dctx.p, nullptr, 0, nullptr);
+        CK(cudaGetLastError());
+        CK(cudaMemcpy(hc, dcnt.p, sizeof(hc), cudaMemcpyDeviceToHost));
+        second_overflow = 0;
+        if (hc[2] > 0) {
+            // fibers that held more intervals than the local buffer: redo them
+            // with a large buffer each in global scratch
+            CK(cudaMemcpy(hcounts.data(), dcounts.p, F * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            std::vector<uint32_t> lst;
+            for (uint64_t k = 0; k < F; ++k)
+                if (hcounts[k] == 0xFFFFFFFFu) lst.push_back((uint32_t)k);
+            DevBuf<uint32_t> dl(lst.size());
+            DevBuf<Ival64> scratch(lst.size() * (size_t)PUSH_CAP_BIG);
+            if (!dl.ok() || !scratch.ok()) return OCL_GB300_OOM;
+            CK(cudaMemcpy(dl.p, lst.data(), lst.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+            CK(cudaMemset(dcnt.p + 2, 0, sizeof(unsigned long long)));
+            const unsigned w2 = (unsigned)((lst.size() + 31) / 32);
+            k_push<<<(w2 + 3) / 4, 128>>>(dctx.p, dl.p, (int)lst.size(), scratch.p);
+            CK(cudaGetLastError());
+            CK(cudaMemcpy(hc, dcnt.p, sizeof(hc), cudaMemcpyDeviceToHost));
+            second_overflow = hc[2];
+        }
+        CK(cudaEventRecord(e1));
+        CK(cudaEventSynchronize(e1));
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (hc[3] > rcap) {
+            rcap = hc[3];
+            continue;
+        }
+        hrec.resize(hc[3]);
+        if (hc[3]) CK(cudaMemcpy(hrec.data(), drec.p, hc[3] * sizeof(PushRec), cudaMemcpyDeviceToHost));
+        break;
+    }
+    hc[2] = second_overflow;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaMemcpy(hcounts.data(), dcounts.p, F * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hoffs.data(), doffs.p, F * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->pairs = hc[0];
+        stats->iter_limit_hits = hc[1];
+        stats->kernel_ms = ms;
+    }
+    if (hc[2]) {
+        set_error("a fiber collected more than " + std::to_string(PUSH_CAP_BIG) + " disjoint intervals while merging");
+        return OCL_GB300_ITER_LIMIT;
+    }
+    uint64_t total = 0;
+    for (uint64_t k = 0; k < F; ++k) {
+        offsets[k] = total;
+        total += hcounts[k];
+    }
+    offsets[F] = total;
+    if (total > cap) {
+        set_error("interval buffer too small");
+        return OCL_GB300_CAPACITY;
+    }
+    for (uint64_t k = 0; k < F; ++k) {
+        for (uint32_t j = 0; j < hcounts[k]; ++j) {
+            const PushRec& r = hrec[hoffs[k] + j];
+            uint64_t o = offsets[k] + j;
+            ival[2 * o] = r.lower;
+            ival[2 * o + 1] = r.upper;
+            std::memcpy(cc + 6 * o, r.lcc, 3 * sizeof(double));
+            std::memcpy(cc + 6 * o + 3, r.ucc, 3 * sizeof(double));
+            cctype[2 * o] = r.ltype;
+            cctype[2 * o + 1] = r.utype;
+        }
+    }
+    return OCL_GB300_OK;
+}
+
+}  // namespace oclg

@@ -1,0 +1,53 @@
+// util.cuh -- error reporting and small RAII helpers for the host side.
+#pragma once
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ocl_gb300.h"
+
+namespace oclg {
+
+void set_error(const std::string& msg);
+
+// Evaluate a CUDA call; on failure record the message and return DEVICE_ERROR
+// (or OOM for allocation failures) from the enclosing function.
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t err__ = (call);                                                      \
+        if (err__ != cudaSuccess) {                                                      \
+            ::oclg::set_error(std::string(#call) + ": " + cudaGetErrorString(err__));    \
+            return err__ == cudaErrorMemoryAllocation ? OCL_GB300_OOM : OCL_GB300_DEVICE_ERROR; \
+        }                                                                                \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    bool alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return true;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+            p = nullptr;
+            set_error("cudaMalloc failed");
+            return false;
+        }
+        return true;
+    }
+    bool ok() const { return n == 0 || p != nullptr; }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { release(); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+};
+
+}  // namespace oclg
