@@ -115,7 +115,11 @@ typedef struct ocl_gb300_stats {
     uint64_t fallback;       /* CL points redone in plain FP64 (candidate list overflow) */
     uint64_t violations;     /* FP64 results below a certified FP32 bound (always 0) */
     uint64_t screened;       /* FP32 whole-triangle screens */
+    uint64_t launches;       /* kernels of this library launched by the call */
     double   kernel_ms;      /* device time of the call's kernels (CUDA events) */
+    double   screen_ms;      /* of which the FP32 screen kernel */
+    double   refine_ms;      /* of which the FP64 refinement kernel */
+    double   fallback_ms;    /* of which the plain FP64 kernel */
     double   total_ms;       /* wall time of the call incl. copies */
 } ocl_gb300_stats;
 

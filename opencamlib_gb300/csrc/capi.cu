@@ -112,21 +112,37 @@ double height_host(const CutterP& c, double r) {
     return height_basic_host(c.sub[idx], r) + c.zoffset[idx];
 }
 
+static void basic_prof(const BasicP& b, Prof32& prof) {
+    std::memset(&prof, 0, sizeof(prof));
+    prof.kind = b.kind;
+    prof.R = (float)b.radius;
+    prof.r1 = (float)b.radius1;
+    prof.r2 = (float)b.radius2;
+    prof.inv_tan = b.kind == OCL_CUTTER_CONE ? (float)(1.0 / b.tan_angle) : 0.0f;
+    prof.center_height = (float)b.center_height;
+    prof.length = (float)b.length;
+    prof.xynl = (float)b.xy_normal_length;
+    prof.nl = (float)b.normal_length;
+}
+
+void fill_comp(const CutterP& cp, Comp32& comp) {
+    std::memset(&comp, 0, sizeof(comp));
+    if (cp.kind != OCL_CUTTER_COMPOSITE) return;
+    comp.nsub = cp.nsub;
+    comp.R = (float)cp.radius;
+    for (int n = 0; n < cp.nsub; ++n) {
+        basic_prof(cp.sub[n], comp.sub[n]);
+        comp.zoff[n] = (float)cp.zoffset[n];
+        comp.rlim[n] = (float)cp.radiusvec[n];
+    }
+}
+
 void fill_prof(const CutterP& cp, Prof32& prof, float* hlb, bool& composite) {
     std::memset(&prof, 0, sizeof(prof));
     composite = cp.kind == OCL_CUTTER_COMPOSITE;
     const BasicP& b = cp.b;
-    prof.kind = composite ? 0 : b.kind;
+    if (!composite) basic_prof(b, prof);
     prof.R = (float)cp.radius;
-    if (!composite) {
-        prof.r1 = (float)b.radius1;
-        prof.r2 = (float)b.radius2;
-        prof.inv_tan = b.kind == OCL_CUTTER_CONE ? (float)(1.0 / b.tan_angle) : 0.0f;
-        prof.center_height = (float)b.center_height;
-        prof.length = (float)b.length;
-        prof.xynl = (float)b.xy_normal_length;
-        prof.nl = (float)b.normal_length;
-    }
     // hlb[k] <= min over r in [k R / N, R] of height(r), built from the top
     // down with dense samples per bin, minus a small margin.
     const double R = cp.radius;
@@ -239,9 +255,24 @@ int ocl_gb300_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const do
         set_error("null buffer");
         return OCL_GB300_BAD_ARG;
     }
-    DevBuf<double> dcl(3 * M), dz(M), dcc(3 * M);
-    DevBuf<int32_t> dty(M);
-    if (!dcl.ok() || !dz.ok() || !dcc.ok() || !dty.ok()) return OCL_GB300_OOM;
+    // device staging buffers, grown on demand and kept per host thread
+    struct HostIO {
+        DevBuf<double> cl, z, cc;
+        DevBuf<int32_t> ty;
+        size_t cap = 0;
+    };
+    static thread_local HostIO io;
+    if (M > io.cap) {
+        if (!io.cl.alloc(3 * M) || !io.z.alloc(M) || !io.cc.alloc(3 * M) || !io.ty.alloc(M)) {
+            io.cap = 0;
+            return OCL_GB300_OOM;
+        }
+        io.cap = M;
+    }
+    DevBuf<double>& dcl = io.cl;
+    DevBuf<double>& dz = io.z;
+    DevBuf<double>& dcc = io.cc;
+    DevBuf<int32_t>& dty = io.ty;
     cudaStream_t s = 0;
     CK(cudaMemcpyAsync(dcl.p, cl_xyz, 3 * M * sizeof(double), cudaMemcpyHostToDevice, s));
     int st = ocl_gb300_drop_device(mesh, cutter, dcl.p, M, precision, dz.p, dcc.p, dty.p, s, stats);

@@ -142,15 +142,10 @@ __device__ __forceinline__ void merge_best(Best64& b, const CL64& c, uint32_t ra
 // dropcutter/batchdropcutter.cpp:187-231).  Used for OCL_GB300_PREC_FP64 and
 // for the points the mixed path hands back.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_drop_kd(const DropCtx* __restrict__ ctxp, const uint32_t* __restrict__ list,
-                                                 int nlist) {
-    const DropCtx& ctx = *ctxp;
-    __shared__ uint2 s_stack[4][KD_STACK];
-    const int lane = threadIdx.x & 31;
-    const int wl = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One warp's 32 points (slot `warp` of the list).
+__device__ __forceinline__ void drop_kd_warp(const DropCtx& ctx, const uint32_t* __restrict__ list, int nlist,
+                                             int warp, uint2* st, int lane) {
     const int base = warp * 32;
-    if (base >= nlist) return;
     const bool active = base + lane < nlist;
     const uint32_t i = list ? list[active ? base + lane : base] : (uint32_t)(active ? base + lane : base);
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
@@ -160,7 +155,6 @@ __global__ void __launch_bounds__(128) k_drop_kd(const DropCtx* __restrict__ ctx
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     unsigned long long pairs = 0;
     int capped = 0;
-    uint2* st = s_stack[wl];
     const unsigned amask = __ballot_sync(0xffffffffu, active);
     int sp = 0;
     if (ctx.kd_nodes && amask) {
@@ -220,6 +214,19 @@ __global__ void __launch_bounds__(128) k_drop_kd(const DropCtx* __restrict__ ctx
     }
 }
 
+// list == nullptr: points 0..M-1; else the *nlist_dev listed points.  The
+// grid strides over warps, so the fallback launch needs no host-side count.
+__global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx ctx, const uint32_t* __restrict__ list,
+                                                 const unsigned long long* __restrict__ nlist_dev) {
+    __shared__ uint2 s_stack[4][KD_STACK];
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int nlist = list ? (int)*nlist_dev : ctx.M;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp * 32 < nlist; warp += nwarps)
+        drop_kd_warp(ctx, list, nlist, warp, s_stack[wl], lane);
+}
+
 // ---------------------------------------------------------------------------
 // FP32 screen
 // ---------------------------------------------------------------------------
@@ -245,6 +252,8 @@ struct ScanShared {
 };
 
 // One pass over the cells under the warp's footprint (centre rows first).
+// KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
+template <int KIND>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
                                            float cx, float cy, float z0l, int c0, int c1, int r0, int r1, int rc,
                                            int cc) {
@@ -286,9 +295,11 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     if (!__any_sync(0xffffffffu, p1)) continue;
                     if (!p1) continue;
                     float lo = NEG_INF32, hi = ub + gd, qt = 3.0e38f;
-                    if (!ctx.composite_screen) {
+                    {
                         const Tri32 t = ctx.t32[e.tri];
-                        Iv v = screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt);
+                        Iv v = (KIND == 2)
+                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, qt)
+                                   : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt);
                         ++ls.screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
                         hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, hi) : NEG_INF32;
@@ -331,12 +342,11 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     }
 }
 
-// quirky: the cutter's per-triangle effect depends on the running height
-// (cone tip/rim short-circuits), so the collection threshold is closed over
-// the branch thresholds of the relevant triangles (three passes).
-template <bool QUIRKY>
-__global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const DropCtx* __restrict__ ctxp) {
-    const DropCtx& ctx = *ctxp;
+// KIND 1/2 (cone, composite): the per-triangle effect depends on the running
+// height (tip/rim short-circuits), so the collection threshold is closed
+// over the branch thresholds of the relevant triangles (three passes).
+template <int KIND>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_constant__ DropCtx ctx) {
     __shared__ ScanShared sh;
     for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
     __syncthreads();
@@ -365,14 +375,14 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const DropCtx
     if (warp_rect(g, xmin, xmax, ymin, ymax, ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius), c0, c1, r0, r1)) {
         const int rc = clampi((int)floor((0.5 * (ymin + ymax) - g.y0) * g.inv_cs), r0, r1);
         const int cc = clampi((int)floor((0.5 * (xmin + xmax) - g.x0) * g.inv_cs), c0, c1);
-        if (!QUIRKY) {
-            scan_cells(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+        if (KIND == 0) {
+            scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
             ls.thr = ls.blo;
         } else {
-            scan_cells(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
-            scan_cells(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells<KIND>(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
             ls.thr = fminf(ls.blo, ls.qthr);
-            scan_cells(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
         }
     } else {
         ls.thr = ls.blo;
@@ -402,8 +412,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const DropCtx
 // dropCutter5 does over its KD candidates.  Triangles left out can neither
 // reach the final height nor change a branch choice of a collected triangle.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_drop_refine(const DropCtx* __restrict__ ctxp) {
-    const DropCtx& ctx = *ctxp;
+__global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ DropCtx ctx) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint32_t)ctx.M) return;
     const int n = ctx.ncand[i];
@@ -429,9 +438,30 @@ __global__ void __launch_bounds__(128) k_drop_refine(const DropCtx* __restrict__
     }
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     int capped = 0;
+    const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
     for (int q = 0; q < n; ++q) {
         const Tri64& t = ctx.t64[tri[q]];
-        if (overlaps64(R, x, y, t) && cl.z < t.bb[5]) drop_triangle64(ctx.cp, cl, t, ctx.t32[tri[q]].flags, &capped);
+        if (!(overlaps64(R, x, y, t) && cl.z < t.bb[5])) continue;
+        uint32_t fl = ctx.t32[tri[q]].flags;
+        if (!ctx.composite_screen) {
+            // an edge whose FP32 upper bound is below the running height cannot
+            // lift it; skipping its FP64 evaluation (for the bull: two Brent
+            // solves) leaves the fold unchanged
+            const Tri32 t3 = ctx.t32[tri[q]];
+            const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
+            const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
+            const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
+            const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
+            const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
+            for (int e = 0; e < 3; ++e) {
+                if (fl & (TF_EDGE0_SKIP << e)) continue;
+                const int k = (e + 1) % 3;
+                Iv v = edge32(ctx.prof, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E,
+                              (fl & (TF_EDGE0_HORIZ << e)) != 0);
+                if (v.hi + ctx.E < zr - ctx.guard) fl |= (TF_EDGE0_SKIP << e);
+            }
+        }
+        drop_triangle64(ctx.cp, cl, t, fl, &capped);
     }
     const uint32_t o = ctx.perm[i];
     ctx.out_z[o] = cl.z;
@@ -458,14 +488,6 @@ __global__ void k_collect_overflow(const uint8_t* ncand, int M, uint32_t* list, 
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-// Cutters whose per-triangle drop depends on the running height: the cone
-// (tip/rim short-circuit) and composites.
-static bool quirky_cutter(const CutterP& cp) {
-    if (cp.kind == OCL_CUTTER_CONE) return true;
-    if (cp.kind == OCL_CUTTER_COMPOSITE) return true;
-    return false;
-}
-
 struct DropWork {
     DevBuf<uint32_t> keys, keys2, perm0, perm;
     DevBuf<double> cls;
@@ -475,15 +497,15 @@ struct DropWork {
     DevBuf<uint32_t> list;
     DevBuf<unsigned long long> counters;
     DevBuf<uint8_t> sort_tmp;
-    DevBuf<DropCtx> ctx;
-    DropCtx* host_ctx = nullptr;  // pinned staging copy of the launch context
+    DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
+    cudaEvent_t events[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     size_t cap = 0;
     bool ensure(size_t M, size_t sort_bytes) {
         if (M > cap || !counters.p) {
             size_t c = std::max<size_t>(M, 1024);
             if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
                 !cand.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) ||
-                !counters.alloc(C_NCOUNTERS + 1) || !ctx.alloc(1))
+                !counters.alloc(C_NCOUNTERS + 1))
                 return false;
             cap = c;
         }
@@ -508,12 +530,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
                                        32, stream));
     if (!w.ensure(M, sort_bytes)) return OCL_GB300_OOM;
 
-    if (!w.host_ctx) {
-        if (cudaMallocHost(&w.host_ctx, sizeof(DropCtx)) != cudaSuccess) return OCL_GB300_OOM;
-    }
-    // the previous call's copy of the context must have left the staging buffer
-    CK(cudaStreamSynchronize(stream));
-    DropCtx* h = w.host_ctx;
+    if (!w.host_ctx) w.host_ctx = new DropCtx();
+    DropCtx* h = w.host_ctx;  // passed by value as the kernels' __grid_constant__ parameter
     std::memset(h, 0, sizeof(DropCtx));
     h->cp = cp;
     h->g = m.grid;
@@ -536,16 +554,18 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     bool composite = false;
     fill_prof(cp, h->prof, h->hlb, composite);
     h->composite_screen = composite;
+    fill_comp(cp, h->comp);
     double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
     double maxabs = half + cp.radius + 1.0;
     h->E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
     h->guard = 4.0f * h->E + 1e-5f * (float)cp.radius;
 
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, stream));
-    CK(cudaMemcpyAsync(w.ctx.p, h, sizeof(DropCtx), cudaMemcpyHostToDevice, stream));
+    if (!w.events[0]) {
+        for (int k = 0; k < 5; ++k) CK(cudaEventCreate(&w.events[k]));
+    }
+    cudaEvent_t* ev = w.events;
+    uint64_t launches = 0;
+    CK(cudaEventRecord(ev[0], stream));
     CK(cudaMemsetAsync(w.counters.p, 0, (C_NCOUNTERS + 1) * sizeof(unsigned long long), stream));
     const int TB = 256;
     const unsigned nb = (unsigned)((M + TB - 1) / TB);
@@ -555,49 +575,62 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     CK(cub::DeviceRadixSort::SortPairs(w.sort_tmp.p, sort_bytes, w.keys.p, w.keys2.p, w.perm0.p, w.perm.p,
                                        (int64_t)M, 0, 32, stream));
     k_gather_cl<<<nb, TB, 0, stream>>>(d_cl, w.perm.p, M, w.cls.p);
+    launches += 2;
+    const unsigned warps = (unsigned)((M + 31) / 32);
+    CK(cudaEventRecord(ev[1], stream));
     if (m.n == 0) {
         // empty surface: every point keeps its z, CC stays NONE
         CK(cudaMemsetAsync(w.ncand.p, 0, M, stream));
         CK(cudaMemsetAsync(w.blo.p, 0xFF, M * sizeof(float), stream));
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(w.ctx.p);
+        CK(cudaEventRecord(ev[2], stream));
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
+        CK(cudaEventRecord(ev[3], stream));
+        launches += 1;
     } else if (precision == OCL_GB300_PREC_FP64) {
-        const unsigned warps = (unsigned)((M + 31) / 32);
-        k_drop_kd<<<(warps + 3) / 4, 128, 0, stream>>>(w.ctx.p, nullptr, (int)M);
+        CK(cudaEventRecord(ev[2], stream));
+        CK(cudaEventRecord(ev[3], stream));
+        k_drop_kd<<<(warps + 3) / 4, 128, 0, stream>>>(*h, nullptr, nullptr);
+        launches += 1;
     } else {
-        const unsigned warps = (unsigned)((M + 31) / 32);
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
-        if (quirky_cutter(cp))
-            k_drop_screen<true><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(w.ctx.p);
+        if (cp.kind == OCL_CUTTER_COMPOSITE)
+            k_drop_screen<2><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
+        else if (cp.kind == OCL_CUTTER_CONE)
+            k_drop_screen<1><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
         else
-            k_drop_screen<false><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(w.ctx.p);
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(w.ctx.p);
+            k_drop_screen<0><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
+        CK(cudaEventRecord(ev[2], stream));
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
+        CK(cudaEventRecord(ev[3], stream));
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
-        unsigned long long nover = 0;
-        CK(cudaMemcpyAsync(&nover, w.counters.p + C_FALLBACK, sizeof(nover), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
-        if (nover > 0) {
-            const unsigned warps2 = (unsigned)((nover + 31) / 32);
-            k_drop_kd<<<(warps2 + 3) / 4, 128, 0, stream>>>(w.ctx.p, w.list.p, (int)nover);
-        }
+        // the fallback grid strides over however many points overflowed
+        const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
+        k_drop_kd<<<fb_blocks, 128, 0, stream>>>(*h, w.list.p, w.counters.p + C_FALLBACK);
+        launches += 4;
     }
     CK(cudaGetLastError());
-    CK(cudaEventRecord(e1, stream));
+    CK(cudaEventRecord(ev[4], stream));
     if (stats) {
         unsigned long long c[C_NCOUNTERS];
         CK(cudaMemcpyAsync(c, w.counters.p, sizeof(c), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
+        float t_all = 0, t_scr = 0, t_ref = 0, t_fb = 0;
+        cudaEventElapsedTime(&t_all, ev[0], ev[4]);
+        cudaEventElapsedTime(&t_scr, ev[1], ev[2]);
+        cudaEventElapsedTime(&t_ref, ev[2], ev[3]);
+        cudaEventElapsedTime(&t_fb, ev[3], ev[4]);
         stats->pairs = c[C_PAIRS];
         stats->refined = c[C_REFINED];
         stats->iter_limit_hits = c[C_CAPPED];
-        stats->kernel_ms = ms;
         stats->fallback = c[C_FALLBACK];
         stats->violations = c[C_VIOLATION];
         stats->screened = c[C_SCREENED];
+        stats->launches = launches;
+        stats->kernel_ms = t_all;
+        stats->screen_ms = t_scr;
+        stats->refine_ms = t_ref;
+        stats->fallback_ms = t_fb;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return OCL_GB300_OK;
 }
 

@@ -6,7 +6,7 @@
 namespace oclg {
 
 constexpr int HLB_N = 256;   // entries of the height lower-bound table
-constexpr int CAND_K = 24;   // refinement candidates kept per CL point
+constexpr int CAND_K = 64;   // refinement candidates kept per CL point
 
 enum Counter {
     C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)
@@ -40,7 +40,8 @@ struct DropCtx {
     unsigned long long* counters;
     float E;                // FP32 position error budget
     float guard;            // margin for the bound tests
-    bool composite_screen;  // composite cutter: no FP32 whole-triangle screen
+    bool composite_screen;  // composite cutter: screen_composite with comp
+    Comp32 comp;
     float hlb[HLB_N];       // lower bound of height(r) on [k R / HLB_N, R]
 };
 
@@ -53,6 +54,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
 int make_cutter_params(const ocl_gb300_cutter& in, CutterP& cp);
 // FP32 profile and the height lower-bound table for the screen.
 void fill_prof(const CutterP& cp, Prof32& prof, float* hlb, bool& composite);
+void fill_comp(const CutterP& cp, Comp32& comp);
 // Host FP64 cutter height(r) (same arithmetic as the device).
 double height_host(const CutterP& cp, double r);
 

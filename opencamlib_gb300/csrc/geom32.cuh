@@ -325,4 +325,85 @@ __device__ inline Iv screen_triangle(const Prof32& c, const Tri32& t, float wx, 
     return best;
 }
 
+
+// Composite cutters (CompositeCutter, compositecutter.cpp:58-193).
+struct Comp32 {
+    int nsub;
+    Prof32 sub[OCL_GB300_MAX_SUB];
+    float zoff[OCL_GB300_MAX_SUB];
+    float rlim[OCL_GB300_MAX_SUB];  // radiusvec
+    float R;
+};
+
+// composite height(r): the first sub-cutter whose radius window holds r
+__device__ __forceinline__ float hcomp32(const Comp32& c, float r) {
+    r = fmaxf(r, 0.0f);
+    int idx = 0;
+    for (int n = 0; n < c.nsub; ++n)
+        if (r <= c.rlim[n] + 1e-6f) { idx = n; break; }
+    return h32(c.sub[idx], fminf(r, c.sub[idx].R)) + c.zoff[idx];
+}
+
+// Screen of one triangle for a composite cutter.  lo: vertex contacts with
+// the composite profile (a facet contact that lifts is the cutter's contact
+// with the plane and lies above them; otherwise the vertices are evaluated).
+// hi: every contact any sub-cutter can make (facet, rim, tip, edges), with
+// the radius windows ignored, which can only raise it.  qthr: the tip of a
+// cone sub-cutter outside the centre window; while the running height is
+// below it, the tip lifts, fails the radius window and hides the rim.
+__device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx, float wy, float E, float& qthr) {
+    const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
+    qthr = 3.0e38f;
+    const float px[3] = {0.0f, t.e1[0], t.e2[0]};
+    const float py[3] = {0.0f, t.e1[1], t.e2[1]};
+    const float pz[3] = {0.0f, t.e1[2], t.e2[2]};
+    Iv r = iv_none();
+    // vertices, composite profile (monotone in r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float dx = px[k] - wx, dy = py[k] - wy;
+        float q = sqrtf(dx * dx + dy * dy);
+        float qlo = q - E, qhi = q + E;
+        if (qlo > c.R) continue;
+        r.hi = fmaxf(r.hi, pz[k] - hcomp32(c, fmaxf(qlo, 0.0f)) + E);
+        if (qhi <= c.R) r.lo = fmaxf(r.lo, pz[k] - hcomp32(c, qhi) - E);
+    }
+    const uint32_t mode = t.flags & TF_FACET_MASK;
+    for (int n = 0; n < c.nsub; ++n) {
+        const Prof32& s = c.sub[n];
+        const float zo = c.zoff[n];
+        // edges of this sub-cutter
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            if (t.flags & (TF_EDGE0_SKIP << e)) continue;
+            const int k = (e + 1) % 3;
+            const bool horiz = (t.flags & (TF_EDGE0_HORIZ << e)) != 0;
+            Iv v = edge32(s, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, E, horiz);
+            if (v.hi > NEG_INF32) r.hi = fmaxf(r.hi, v.hi - zo + E);
+        }
+        if (mode == TF_FACET_NONE) continue;
+        if (s.kind == OCL_CUTTER_CONE) {
+            float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
+            float slope = (fabsf(nx) + fabsf(ny)) / nz;
+            float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
+            float et = E * (2.0f + slope);
+            int st_tip = inside32(t, wx, wy, eps_b);
+            if (st_tip >= 0) {
+                r.hi = fmaxf(r.hi, zt - zo + et);
+                if (n > 0) qthr = fminf(qthr, zt - zo - et);
+            }
+            if (mode == TF_FACET_GENERAL) {
+                float xyl = sqrtf(nx * nx + ny * ny);
+                float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
+                float zr = -(nx * rx + ny * ry) / nz - s.length;
+                if (inside32(t, rx, ry, eps_b) >= 0) r.hi = fmaxf(r.hi, zr - zo + E * (2.0f + 2.0f * slope));
+            }
+        } else {
+            Iv v = facet32(s, t, wx, wy, E, eps_b);
+            if (v.hi > NEG_INF32) r.hi = fmaxf(r.hi, v.hi - zo + E);
+        }
+    }
+    return r;
+}
+
 }  // namespace oclg

@@ -71,6 +71,7 @@ def _lib(which: str):
         L.oracle_overlap_pairs.restype = C.c_long
         L.oracle_cutter_fields.argtypes = [cd, _dp]
         L.oracle_cutter_fields.restype = C.c_int
+        L.oracle_last_loop_seconds.restype = C.c_double
     else:
         L.ref_preset_fields.argtypes = [C.c_int, _dp, _dp]
         L.ref_preset_fields.restype = C.c_int
@@ -215,3 +216,8 @@ def ref_preset_fields(preset: int, args):
     if L.ref_preset_fields(preset, _ptr(a), _ptr(out)) != 0:
         raise RuntimeError("bad preset")
     return out
+
+
+def last_loop_seconds() -> float:
+    """Wall time of the last port drop's CL loop (KD build excluded)."""
+    return float(_lib("port").oracle_last_loop_seconds())

@@ -897,6 +897,11 @@ static long point_drop(const Scene* S, CL* cl, LVec* buf, Ctx* ctx) {
     return calls;
 }
 
+static double g_last_loop_seconds = 0.0;
+
+/* Wall time of the last oracle_drop's CL loop (KD build excluded). */
+double oracle_last_loop_seconds(void) { return g_last_loop_seconds; }
+
 int oracle_drop(const double* tris, long ntri, const ocl_gb300_cutter* cd, const double* clin,
                 long M, int nthreads, unsigned bucket, double* z, double* cc, int32_t* type,
                 long* ncalls) {
@@ -904,6 +909,9 @@ int oracle_drop(const double* tris, long ntri, const ocl_gb300_cutter* cd, const
     int st = scene_init(&S, tris, ntri, cd, bucket, 0);
     if (st) return st;
     long calls = 0;
+#ifdef _OPENMP
+    double t0 = omp_get_wtime();
+#endif
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -928,6 +936,9 @@ int oracle_drop(const double* tris, long ntri, const ocl_gb300_cutter* cd, const
         }
         free(buf.v);
     }
+#ifdef _OPENMP
+    g_last_loop_seconds = omp_get_wtime() - t0;
+#endif
     if (ncalls) *ncalls = calls;
     scene_free(&S);
     return 0;

@@ -56,6 +56,7 @@ long oracle_overlap_pairs(const double* tris, long ntri, double radius,
                           const double* cl, long M, int nthreads);
 
 int oracle_cutter_fields(const ocl_gb300_cutter* c, double* out);
+double oracle_last_loop_seconds(void);
 int ref_preset_fields(int preset, const double* args, double* out);
 
 #ifdef __cplusplus
