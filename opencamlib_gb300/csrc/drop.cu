@@ -241,6 +241,7 @@ struct LaneState {
     int nc;
     bool overflow;
     bool chain;      // a collected triangle's branch depends on uncollected ones
+    float chain_thr; // lowest branch threshold among chained triangles
     unsigned long long screened;
 };
 
@@ -298,7 +299,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     {
                         const Tri32 t = ctx.t32[e.tri];
                         Iv v = (KIND == 2)
-                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, qt)
+                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt)
                                    : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt);
                         ++ls.screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
@@ -316,7 +317,10 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     // collect (PH_SINGLE: lazily pruned against the rising bound)
                     const float keep = (phase == PH_COLLECT) ? ls.thr : ls.blo;
                     if (!(hi >= keep - gd && hi > z0l - gd) || ls.overflow) continue;
-                    if (phase == PH_COLLECT && qt < ls.thr - gd) ls.chain = true;
+                    if (phase == PH_COLLECT && qt < ls.thr - gd) {
+                        ls.chain = true;
+                        ls.chain_thr = fminf(ls.chain_thr, qt);
+                    }
                     if (ls.nc == CAND_K) {
                         int w = 0;
                         for (int q = 0; q < CAND_K; ++q) {
@@ -368,6 +372,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_
     ls.nc = 0;
     ls.overflow = false;
     ls.chain = false;
+    ls.chain_thr = 3.0e38f;
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
@@ -382,7 +387,25 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_
             scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
             scan_cells<KIND>(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
             ls.thr = fminf(ls.blo, ls.qthr);
-            scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            // collect; if a collected triangle's branch threshold lies below
+            // the collection threshold, lower it and collect again
+            bool done = false;
+            for (int round = 0; round < 4; ++round) {
+                const float keep_thr = ls.thr;
+                if (!done) {
+                    ls.nc = 0;
+                    ls.chain = false;
+                    ls.chain_thr = 3.0e38f;
+                } else {
+                    ls.thr = 3.0e38f;  // finished lanes collect nothing more
+                }
+                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+                ls.thr = keep_thr;
+                const bool again = !done && ls.chain && !ls.overflow && round < 3;
+                if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
+                else done = true;
+                if (!__any_sync(0xffffffffu, again)) break;
+            }
         }
     } else {
         ls.thr = ls.blo;

@@ -6,7 +6,7 @@
 namespace oclg {
 
 constexpr int HLB_N = 256;   // entries of the height lower-bound table
-constexpr int CAND_K = 64;   // refinement candidates kept per CL point
+constexpr int CAND_K = 40;   // refinement candidates kept per CL point
 
 enum Counter {
     C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)

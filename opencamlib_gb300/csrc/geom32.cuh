@@ -344,20 +344,29 @@ __device__ __forceinline__ float hcomp32(const Comp32& c, float r) {
     return h32(c.sub[idx], fminf(r, c.sub[idx].R)) + c.zoff[idx];
 }
 
-// Screen of one triangle for a composite cutter.  lo: vertex contacts with
-// the composite profile (a facet contact that lifts is the cutter's contact
-// with the plane and lies above them; otherwise the vertices are evaluated).
-// hi: every contact any sub-cutter can make (facet, rim, tip, edges), with
-// the radius windows ignored, which can only raise it.  qthr: the tip of a
-// cone sub-cutter outside the centre window; while the running height is
-// below it, the tip lifts, fails the radius window and hides the rim.
-__device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx, float wy, float E, float& qthr) {
+// Screen of one triangle for a composite cutter.
+// The composite facet drop (compositecutter.cpp:152-172) ends the triangle
+// as soon as a sub-cutter's facet contact lies in that sub-cutter's radius
+// window and lifts; that contact need not be the cutter's highest contact with
+// the plane (e.g. the shaft on a facet steeper than the cone), so:
+//   lo: the facet outcome if one facet contact certainly lifts, else the
+//       lower of (vertex contacts with the composite profile) and every facet
+//       contact that may end the triangle;
+//   hi: every contact any sub-cutter can make (facet, rim, tip, edges), with
+//       the radius windows ignored;
+//   qthr: the lowest facet contact that may end the triangle while another
+//       contact could be higher (its branch depends on the running height),
+//       and the tip of a cone sub-cutter outside the centre window (while the
+//       running height is below it the tip lifts, fails the window and hides
+//       that sub-cutter's rim).
+__device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx, float wy, float E, float z0_rel,
+                                      float& qthr) {
     const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
     qthr = 3.0e38f;
     const float px[3] = {0.0f, t.e1[0], t.e2[0]};
     const float py[3] = {0.0f, t.e1[1], t.e2[1]};
     const float pz[3] = {0.0f, t.e1[2], t.e2[2]};
-    Iv r = iv_none();
+    float vlo = NEG_INF32, ohi = NEG_INF32;  // vertex-path lower bound; highest non-facet contact
     // vertices, composite profile (monotone in r)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -365,44 +374,94 @@ __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx,
         float q = sqrtf(dx * dx + dy * dy);
         float qlo = q - E, qhi = q + E;
         if (qlo > c.R) continue;
-        r.hi = fmaxf(r.hi, pz[k] - hcomp32(c, fmaxf(qlo, 0.0f)) + E);
-        if (qhi <= c.R) r.lo = fmaxf(r.lo, pz[k] - hcomp32(c, qhi) - E);
+        ohi = fmaxf(ohi, pz[k] - hcomp32(c, fmaxf(qlo, 0.0f)) + E);
+        if (qhi <= c.R) vlo = fmaxf(vlo, pz[k] - hcomp32(c, qhi) - E);
     }
-    const uint32_t mode = t.flags & TF_FACET_MASK;
     for (int n = 0; n < c.nsub; ++n) {
         const Prof32& s = c.sub[n];
         const float zo = c.zoff[n];
-        // edges of this sub-cutter
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             if (t.flags & (TF_EDGE0_SKIP << e)) continue;
             const int k = (e + 1) % 3;
             const bool horiz = (t.flags & (TF_EDGE0_HORIZ << e)) != 0;
             Iv v = edge32(s, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, E, horiz);
-            if (v.hi > NEG_INF32) r.hi = fmaxf(r.hi, v.hi - zo + E);
-        }
-        if (mode == TF_FACET_NONE) continue;
-        if (s.kind == OCL_CUTTER_CONE) {
-            float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
-            float slope = (fabsf(nx) + fabsf(ny)) / nz;
-            float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
-            float et = E * (2.0f + slope);
-            int st_tip = inside32(t, wx, wy, eps_b);
-            if (st_tip >= 0) {
-                r.hi = fmaxf(r.hi, zt - zo + et);
-                if (n > 0) qthr = fminf(qthr, zt - zo - et);
-            }
-            if (mode == TF_FACET_GENERAL) {
-                float xyl = sqrtf(nx * nx + ny * ny);
-                float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
-                float zr = -(nx * rx + ny * ry) / nz - s.length;
-                if (inside32(t, rx, ry, eps_b) >= 0) r.hi = fmaxf(r.hi, zr - zo + E * (2.0f + 2.0f * slope));
-            }
-        } else {
-            Iv v = facet32(s, t, wx, wy, E, eps_b);
-            if (v.hi > NEG_INF32) r.hi = fmaxf(r.hi, v.hi - zo + E);
+            if (v.hi > NEG_INF32) ohi = fmaxf(ohi, v.hi - zo + E);
         }
     }
+    // facet contacts of the sub-cutters, with their window/inside states
+    const uint32_t mode = t.flags & TF_FACET_MASK;
+    float f_certain = NEG_INF32;  // best facet contact that certainly ends the triangle
+    float f_minlo = 3.0e38f;      // lowest facet contact that may end it
+    float f_hi = NEG_INF32;
+    bool f_possible = false;
+    float tip_thr = 3.0e38f;
+    if (mode != TF_FACET_NONE) {
+        const float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
+        const float xyl = sqrtf(nx * nx + ny * ny);
+        const float slope = (mode == TF_FACET_HORIZ) ? 0.0f : (fabsf(nx) + fabsf(ny)) / nz;
+        for (int n = 0; n < c.nsub; ++n) {
+            const Prof32& s = c.sub[n];
+            const float zo = c.zoff[n];
+            const float wlo = (n == 0 ? 0.0f : c.rlim[n - 1]) - 1e-6f, whi = c.rlim[n] + 1e-6f;
+            // up to two candidate contacts per sub-cutter: (value, cc distance, inside state)
+            float val[2], dist[2];
+            int ins[2], m = 0;
+            bool cone_tip_blocks = false;
+            if (s.kind == OCL_CUTTER_CONE) {
+                float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
+                int st_tip = inside32(t, wx, wy, eps_b);
+                if (st_tip >= 0) {
+                    val[m] = zt - zo; dist[m] = 0.0f; ins[m] = st_tip; ++m;
+                    cone_tip_blocks = !(0.0f >= wlo);  // tip outside this sub-cutter's window
+                }
+                if (mode == TF_FACET_GENERAL) {
+                    float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
+                    int st_rim = inside32(t, rx, ry, eps_b);
+                    if (st_rim >= 0) {
+                        val[m] = -(nx * rx + ny * ry) / nz - s.length - zo;
+                        dist[m] = s.R; ins[m] = st_rim; ++m;
+                    }
+                }
+                if (cone_tip_blocks) tip_thr = fminf(tip_thr, val[0] - E * (2.0f + slope));
+            } else {
+                float ccx, ccy, tip;
+                if (mode == TF_FACET_HORIZ) {
+                    ccx = wx; ccy = wy; tip = 0.0f;
+                } else {
+                    float xnx = nx / xyl, xny = ny / xyl;
+                    float rvx = s.xynl * xnx + s.nl * nx, rvy = s.xynl * xny + s.nl * ny, rvz = s.nl * nz;
+                    ccx = wx - rvx; ccy = wy - rvy;
+                    tip = -(nx * ccx + ny * ccy) / nz + rvz - s.center_height;
+                }
+                int st = inside32(t, ccx, ccy, eps_b);
+                if (st >= 0) {
+                    float dx = ccx - wx, dy = ccy - wy;
+                    val[m] = tip - zo; dist[m] = sqrtf(dx * dx + dy * dy); ins[m] = st; ++m;
+                }
+            }
+            const float ev = E * (3.0f + 2.0f * slope);
+            for (int k = 0; k < m; ++k) {
+                // radius window (CompositeCutter::ccValidRadius, compositecutter.cpp:86-102)
+                int win = (dist[k] - E >= wlo && dist[k] + E <= whi) ? 1
+                          : ((dist[k] + E < wlo || dist[k] - E > whi) ? -1 : 0);
+                f_hi = fmaxf(f_hi, val[k] + ev);
+                if (win < 0) continue;
+                int state = (win > 0 && ins[k] > 0) ? 1 : 0;
+                if (val[k] + ev <= z0_rel) continue;  // never lifts
+                f_possible = true;
+                f_minlo = fminf(f_minlo, val[k] - ev);
+                if (state > 0 && val[k] - ev > z0_rel) f_certain = fmaxf(f_certain, val[k] - ev);
+            }
+        }
+    }
+    Iv r;
+    r.hi = fmaxf(ohi, f_hi);
+    if (f_certain > NEG_INF32) r.lo = f_certain;
+    else if (f_possible) r.lo = fminf(vlo, f_minlo);
+    else r.lo = vlo;
+    if (f_possible && ohi > f_minlo) qthr = f_minlo;
+    qthr = fminf(qthr, tip_thr);
     return r;
 }
 
