@@ -137,6 +137,26 @@ int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
                           double* d_z_out, double* d_cc_out, int32_t* d_type_out,
                           void* stream, ocl_gb300_stats* stats);
 
+/* Drop-cutter that allocates no device memory.  No counterpart in the
+ * reference library.  For callers that cannot allocate while they run -- a
+ * machine controller or real-time loop whose device memory is budgeted up
+ * front (an allocation can synchronise the device and stall the loop), or a
+ * host process whose own pool allocator owns the device's memory.  Device
+ * buffers in and out as in ocl_gb300_drop_device (mixed precision, same
+ * results); at most OCL_GB300_NOALLOC_MAX_POINTS points per call, larger
+ * calls return OCL_GB300_BAD_ARG.  Scratch is one fixed array inside the
+ * library (about 3 MB), held by every device that loads the library until
+ * the process exits; the first call on a device looks its address up, so make
+ * that first call before capturing any stream.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  Points are processed in the order given
+ * (spatially ordered inputs run fastest). */
+#define OCL_GB300_NOALLOC_MAX_POINTS 16384
+int ocl_gb300_drop_device_noalloc(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
+                                  const double* d_cl_xyz, uint64_t M,
+                                  double* d_z_out, double* d_cc_out, int32_t* d_type_out,
+                                  void* stream);
+
 /* ---- push-cutter ------------------------------------------------------- */
 #define OCL_GB300_XFIBER 0
 #define OCL_GB300_YFIBER 1

@@ -23,7 +23,7 @@ _u64p = C.POINTER(C.c_uint64)
 # every entry point declared in include/ocl_gb300.h
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
-    "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_push", "ocl_gb300_path_drop",
+    "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_last_error", "ocl_gb300_version", "ocl_gb300_device_available",
 ]
 
@@ -53,6 +53,8 @@ def lib():
     L.ocl_gb300_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_int, _dp, _dp, _ip, st]
     L.ocl_gb300_drop_device.argtypes = [C.c_void_p, cd, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, st]
+    L.ocl_gb300_drop_device_noalloc.argtypes = [C.c_void_p, cd, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]
     L.ocl_gb300_push.argtypes = [C.c_void_p, cd, C.c_int, _dp, C.c_uint64, _u64p, _dp, _dp, _ip, C.c_uint64, st]
     L.ocl_gb300_path_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, C.c_double, _dp, _dp, _ip,
                                       C.c_uint64, _u64p, st]

@@ -244,6 +244,26 @@ int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, c
     return drop_run(*mesh->m, cp, d_cl_xyz, M, precision, d_z_out, d_cc_out, d_type_out, (cudaStream_t)stream, stats);
 }
 
+int ocl_gb300_drop_device_noalloc(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* d_cl_xyz,
+                                  uint64_t M, double* d_z_out, double* d_cc_out, int32_t* d_type_out, void* stream) {
+    if (!mesh || !cutter) {
+        set_error("null mesh or cutter");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (M > 0 && (!d_cl_xyz || !d_z_out || !d_cc_out || !d_type_out)) {
+        set_error("null buffer");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = make_cutter_params(*cutter, cp);
+    if (st) {
+        set_error(st == OCL_GB300_UNSUPPORTED_CUTTER ? "unsupported cutter kind" : "invalid cutter parameters");
+        return st;
+    }
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    return drop_run_noalloc(*mesh->m, cp, d_cl_xyz, M, d_z_out, d_cc_out, d_type_out, (cudaStream_t)stream);
+}
+
 int ocl_gb300_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* cl_xyz, uint64_t M,
                    int precision, double* z_out, double* cc_out, int32_t* type_out, ocl_gb300_stats* stats) {
     auto t0 = std::chrono::steady_clock::now();

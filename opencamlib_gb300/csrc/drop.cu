@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include <cub/cub.cuh>
 
@@ -654,6 +656,126 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         stats->refine_ms = t_ref;
         stats->fallback_ms = t_fb;
     }
+    return OCL_GB300_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Drop without any device allocation (ocl_gb300_drop_device_noalloc).
+//
+// For callers that cannot allocate device memory while they run: a machine
+// controller or real-time loop whose device memory is budgeted up front (a
+// cudaMalloc can synchronise the device and stall the loop), or a host process
+// whose own pool allocator owns the device's memory and forbids other
+// allocations.  All scratch lives in one file-scope __device__ array sized for
+// OCL_GB300_NOALLOC_MAX_POINTS points, loaded with the library and held by
+// every device that loads it until the process exits.  Points are processed
+// in the caller's order (no sort), so spatially ordered inputs (rasters,
+// paths) run best; results equal ocl_gb300_drop's.
+// ---------------------------------------------------------------------------
+struct NoAllocScratch {
+    uint32_t perm[OCL_GB300_NOALLOC_MAX_POINTS];
+    uint32_t cand[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K];
+    uint32_t list[OCL_GB300_NOALLOC_MAX_POINTS];
+    float blo[OCL_GB300_NOALLOC_MAX_POINTS];
+    uint8_t ncand[OCL_GB300_NOALLOC_MAX_POINTS];
+    unsigned long long counters[C_NCOUNTERS + 1];
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+__global__ void k_noalloc_identity(uint32_t* perm, int M) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < M) perm[i] = (uint32_t)i;
+}
+
+// Device address of the scratch array, looked up once per device with that
+// device current (the host-side name is only a stand-in for the symbol).
+static int noalloc_scratch(NoAllocScratch** out) {
+    static std::mutex mu;
+    static NoAllocScratch* addr[256] = {};
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) {
+        set_error("device ordinal out of range");
+        return OCL_GB300_DEVICE_ERROR;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            set_error(std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
+            return OCL_GB300_DEVICE_ERROR;
+        }
+        addr[dev] = static_cast<NoAllocScratch*>(p);
+    }
+    *out = addr[dev];
+    return OCL_GB300_OK;
+}
+
+int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, double* d_z, double* d_cc,
+                     int32_t* d_type, cudaStream_t stream) {
+    if (M > (uint64_t)OCL_GB300_NOALLOC_MAX_POINTS) {
+        set_error("ocl_gb300_drop_device_noalloc: " + std::to_string(M) + " points exceed the maximum of " +
+                  std::to_string(OCL_GB300_NOALLOC_MAX_POINTS));
+        return OCL_GB300_BAD_ARG;
+    }
+    if (M == 0) return OCL_GB300_OK;
+    NoAllocScratch* sc = nullptr;
+    int st = noalloc_scratch(&sc);
+    if (st) return st;
+    DropCtx h;
+    std::memset(&h, 0, sizeof(h));
+    h.cp = cp;
+    h.g = m.grid;
+    h.cells = m.d_cells;
+    h.entries = m.d_entries;
+    h.t64 = m.d_t64;
+    h.t32 = m.d_t32;
+    h.kd_nodes = m.drop_kd.d_nodes;
+    h.kd_order = m.drop_kd.d_order;
+    h.cl = d_cl;  // caller's order
+    h.perm = sc->perm;
+    h.M = (int)M;
+    h.out_z = d_z;
+    h.out_cc = d_cc;
+    h.out_type = d_type;
+    h.cand = sc->cand;
+    h.ncand = sc->ncand;
+    h.blo = sc->blo;
+    h.counters = sc->counters;
+    bool composite = false;
+    fill_prof(cp, h.prof, h.hlb, composite);
+    h.composite_screen = composite;
+    fill_comp(cp, h.comp);
+    double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
+    double maxabs = half + cp.radius + 1.0;
+    h.E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
+    h.guard = 4.0f * h.E + 1e-5f * (float)cp.radius;
+    // the array keeps the previous call's contents: clear what must start at zero
+    CK(cudaMemsetAsync(sc->counters, 0, sizeof(sc->counters), stream));
+    const int TB = 256;
+    const unsigned nb = (unsigned)((M + TB - 1) / TB);
+    k_noalloc_identity<<<nb, TB, 0, stream>>>(sc->perm, (int)M);
+    const unsigned warps = (unsigned)((M + 31) / 32);
+    if (m.n == 0) {
+        CK(cudaMemsetAsync(sc->ncand, 0, M, stream));
+        CK(cudaMemsetAsync(sc->blo, 0xFF, M * sizeof(float), stream));
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+    } else {
+        const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
+        if (cp.kind == OCL_CUTTER_COMPOSITE)
+            k_drop_screen<2><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
+        else if (cp.kind == OCL_CUTTER_CONE)
+            k_drop_screen<1><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
+        else
+            k_drop_screen<0><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
+        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+        k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
+        const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
+        k_drop_kd<<<fb_blocks, 128, 0, stream>>>(h, sc->list, sc->counters + C_FALLBACK);
+    }
+    CK(cudaGetLastError());
     return OCL_GB300_OK;
 }
 

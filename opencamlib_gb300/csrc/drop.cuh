@@ -49,6 +49,9 @@ struct DropWork;
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats);
 
+int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, double* d_z, double* d_cc,
+                     int32_t* d_type, cudaStream_t stream);
+
 // Cutter parameters from the ABI description (the reference constructors'
 // arithmetic); returns an OCL_GB300_* status.
 int make_cutter_params(const ocl_gb300_cutter& in, CutterP& cp);
