@@ -332,6 +332,11 @@ def main():
                    "mesh_build_s": mesh_s},
         "latency": {"p50_step_ms": float(np.percentile(step_ms, 50)), "p99_step_ms": float(np.percentile(step_ms, 99)),
                     "per_cutter_ms": {n: st.kernel_ms for n, st in breakdown}},
+        "per_cutter": {n: {"kernel_ms": st.kernel_ms, "screen_ms": st.screen_ms, "refine_ms": st.refine_ms,
+                           "fallback_ms": st.fallback_ms, "fallback_points": int(st.fallback),
+                           "overflow_points": int(st.overflow_points), "chain_points": int(st.chain_points),
+                           "refined_per_point": st.refined / M, "screened_per_point": st.screened / M}
+                       for n, st in breakdown},
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": "CL-points/s", "h2d_bytes_per_step": len(cuts) * M * 24,
                 "d2h_bytes_per_step": len(cuts) * M * (8 + 24 + 4)},

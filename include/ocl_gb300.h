@@ -115,6 +115,8 @@ typedef struct ocl_gb300_stats {
     uint64_t fallback;       /* CL points redone in plain FP64 (candidate list overflow) */
     uint64_t violations;     /* FP64 results below a certified FP32 bound (always 0) */
     uint64_t screened;       /* FP32 whole-triangle screens */
+    uint64_t overflow_points;/* of the fallback points: candidate list overflow */
+    uint64_t chain_points;   /* of the fallback points: branch thresholds kept chaining */
     uint64_t launches;       /* kernels of this library launched by the call */
     double   kernel_ms;      /* device time of the call's kernels (CUDA events) */
     double   screen_ms;      /* of which the FP32 screen kernel */
@@ -145,13 +147,13 @@ int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
  * buffers in and out as in ocl_gb300_drop_device (mixed precision, same
  * results); at most OCL_GB300_NOALLOC_MAX_POINTS points per call, larger
  * calls return OCL_GB300_BAD_ARG.  Scratch is one fixed array inside the
- * library (about 3 MB), held by every device that loads the library until
+ * library (about 4.3 MB), held by every device that loads the library until
  * the process exits; the first call on a device looks its address up, so make
  * that first call before capturing any stream.  All calls share the array:
  * calls that overlap on the GPU (other streams, other host threads) race and
  * must be serialised by the caller.  Points are processed in the order given
  * (spatially ordered inputs run fastest). */
-#define OCL_GB300_NOALLOC_MAX_POINTS 16384
+#define OCL_GB300_NOALLOC_MAX_POINTS 8192
 int ocl_gb300_drop_device_noalloc(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
                                   const double* d_cl_xyz, uint64_t M,
                                   double* d_z_out, double* d_cc_out, int32_t* d_type_out,

@@ -76,24 +76,27 @@ struct Tri32 {
 };
 static_assert(sizeof(Tri32) == 64, "Tri32 layout");
 
-// Grid entry: one (cell, triangle) incidence with the triangle's FP32 bbox
-// rounded outward, 32 B.  Entries are sorted by cell, cells row-major, so a
-// row of cells is one contiguous run of entries.
+// Grid entry: one triangle in its home cell, with its FP32 bbox rounded
+// outward, 32 B.  Entries are sorted by (level, home cell), cells row-major.
 struct Entry {
     float minx, maxx, miny, maxy;  // local to origin, rounded outward
     float maxz;                    // rounded up
     int32_t tri;                   // triangle index in device order
-    uint16_t col;                  // this entry's cell column
-    uint16_t tcol0;                // cell column of the triangle's min corner
-    uint16_t trow0;                // cell row of the triangle's min corner
-    uint16_t pad;
+    float pad[2];
 };
 static_assert(sizeof(Entry) == 32, "Entry layout");
 
+// Multi-level uniform grid: level L has square cells of cs[L] = cs[0] * 4^L;
+// a triangle lives in the finest level whose cell size covers its xy extent,
+// in the cell holding its bbox min corner, so a query rectangle widened by
+// one cell to the left and below finds every triangle that overlaps it.
+constexpr int GRID_MAX_LEVELS = 8;
 struct GridP {
-    double x0, y0;      // grid origin (FP64)
-    double cs, inv_cs;  // cell size
-    int ncol, nrow;
+    double x0, y0;  // grid origin (FP64)
+    int nlev;
+    double cs[GRID_MAX_LEVELS], inv_cs[GRID_MAX_LEVELS];
+    int ncol[GRID_MAX_LEVELS], nrow[GRID_MAX_LEVELS];
+    uint32_t cell_off[GRID_MAX_LEVELS + 1];  // first cell index of each level
     double ox, oy, oz;  // origin of the FP32 local frame
 };
 

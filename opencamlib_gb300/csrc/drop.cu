@@ -98,16 +98,19 @@ __device__ __forceinline__ int centre_out(int k, int c, int lo, int hi) {
     return (up > dn) ? c + m + rest : c - m - rest;
 }
 
-// Query rectangle of a warp in cell coordinates; returns false if empty.
-__device__ __forceinline__ bool warp_rect(const GridP& g, double xmin, double xmax, double ymin, double ymax,
+// Query rectangle of a warp at grid level L in cell coordinates, widened by
+// one cell to the left and below (a triangle's home cell is its min corner's
+// and its extent is at most one cell); returns false if empty.
+__device__ __forceinline__ bool warp_rect(const GridP& g, int L, double xmin, double xmax, double ymin, double ymax,
                                           double reach, int& c0, int& c1, int& r0, int& r1) {
-    double a0 = floor((xmin - reach - g.x0) * g.inv_cs), a1 = floor((xmax + reach - g.x0) * g.inv_cs);
-    double b0 = floor((ymin - reach - g.y0) * g.inv_cs), b1 = floor((ymax + reach - g.y0) * g.inv_cs);
-    if (a1 < 0 || b1 < 0 || a0 > g.ncol - 1 || b0 > g.nrow - 1) return false;
+    const double inv = g.inv_cs[L];
+    double a0 = floor((xmin - reach - g.x0) * inv) - 1.0, a1 = floor((xmax + reach - g.x0) * inv);
+    double b0 = floor((ymin - reach - g.y0) * inv) - 1.0, b1 = floor((ymax + reach - g.y0) * inv);
+    if (a1 < 0 || b1 < 0 || a0 > g.ncol[L] - 1 || b0 > g.nrow[L] - 1) return false;
     c0 = (int)fmax(a0, 0.0);
-    c1 = (int)fmin(a1, (double)(g.ncol - 1));
+    c1 = (int)fmin(a1, (double)(g.ncol[L] - 1));
     r0 = (int)fmax(b0, 0.0);
-    r1 = (int)fmin(b1, (double)(g.nrow - 1));
+    r1 = (int)fmin(b1, (double)(g.nrow[L] - 1));
     return true;
 }
 
@@ -144,9 +147,14 @@ __device__ __forceinline__ void merge_best(Best64& b, const CL64& c, uint32_t ra
 // dropcutter/batchdropcutter.cpp:187-231).  Used for OCL_GB300_PREC_FP64 and
 // for the points the mixed path hands back.
 // ---------------------------------------------------------------------------
-// One warp's 32 points (slot `warp` of the list).
-__device__ __forceinline__ void drop_kd_warp(const DropCtx& ctx, const uint32_t* __restrict__ list, int nlist,
-                                             int warp, uint2* st, int lane) {
+// One warp's 32 points (slot `warp` of the list).  FAST (the fallback of the
+// mixed path): candidates that cannot overlap or cannot lift the running
+// height are skipped after an FP32 test on the outward-rounded bbox, which
+// leaves the fold unchanged; the plain FP64 path (FAST = false) evaluates
+// every overlap pair in FP64 like the reference.
+template <bool FAST>
+__device__ __forceinline__ void drop_kd_warp(const DropCtx& ctx, const float* hlb, const uint32_t* __restrict__ list,
+                                             int nlist, int warp, uint2* st, int lane) {
     const int base = warp * 32;
     const bool active = base + lane < nlist;
     const uint32_t i = list ? list[active ? base + lane : base] : (uint32_t)(active ? base + lane : base);
@@ -174,6 +182,18 @@ __device__ __forceinline__ void drop_kd_warp(const DropCtx& ctx, const uint32_t*
             for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
                 if (!in) continue;
                 const int32_t tri = ctx.kd_order[k];
+                if (FAST) {
+                    const Entry e = ctx.entries[tri];
+                    const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
+                    const float gd = ctx.guard;
+                    const float dx = fmaxf(0.0f, fmaxf(e.minx - cxl, cxl - e.maxx));
+                    const float dy = fmaxf(0.0f, fmaxf(e.miny - cyl, cyl - e.maxy));
+                    if (dx > ctx.prof.R + gd || dy > ctx.prof.R + gd) continue;  // cannot overlap
+                    const float d = sqrtf(dx * dx + dy * dy);
+                    if (d > ctx.prof.R + gd) continue;  // outside the cutter's reach
+                    const float ub = e.maxz - hlb_at(hlb, d - gd, (float)HLB_N / ctx.prof.R);
+                    if (ub + gd < __double2float_rd(cl.z - ctx.g.oz)) continue;  // cannot lift
+                }
                 const Tri64& t = ctx.t64[tri];
                 if (overlaps64(R, x, y, t)) {
                     ++pairs;
@@ -218,15 +238,19 @@ __device__ __forceinline__ void drop_kd_warp(const DropCtx& ctx, const uint32_t*
 
 // list == nullptr: points 0..M-1; else the *nlist_dev listed points.  The
 // grid strides over warps, so the fallback launch needs no host-side count.
+template <bool FAST>
 __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx ctx, const uint32_t* __restrict__ list,
                                                  const unsigned long long* __restrict__ nlist_dev) {
     __shared__ uint2 s_stack[4][KD_STACK];
+    __shared__ float s_hlb[HLB_N];
+    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
     const int nlist = list ? (int)*nlist_dev : ctx.M;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp * 32 < nlist; warp += nwarps)
-        drop_kd_warp(ctx, list, nlist, warp, s_stack[wl], lane);
+        drop_kd_warp<FAST>(ctx, s_hlb, list, nlist, warp, s_stack[wl], lane);
 }
 
 // ---------------------------------------------------------------------------
@@ -244,22 +268,21 @@ struct LaneState {
     bool overflow;
     bool chain;      // a collected triangle's branch depends on uncollected ones
     float chain_thr; // lowest branch threshold among chained triangles
+    uint32_t self;   // this lane's point (its list slot)
     unsigned long long screened;
 };
 
 struct ScanShared {
     float hlb[HLB_N];
     Entry ent[SCREEN_WARPS][32];
-    uint32_t tri[SCREEN_WARPS][CAND_K][32];
-    float hi[SCREEN_WARPS][CAND_K][32];
 };
 
 // One pass over the cells under the warp's footprint (centre rows first).
 // KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
 template <int KIND>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
-                                           float cx, float cy, float z0l, int c0, int c1, int r0, int r1, int rc,
-                                           int cc) {
+                                           float cx, float cy, float z0l, double xmin, double xmax, double ymin,
+                                           double ymax) {
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
     const GridP& g = ctx.g;
@@ -267,12 +290,21 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     const float gd = ctx.guard;
     const float Rg = R + gd;
     const float inv_step = (float)HLB_N / R;
-    const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
+    const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
+    // coarse levels first: they hold the large triangles and are cheap to scan
+    for (int L = g.nlev - 1; L >= 0; --L) {
+        int c0, c1, r0, r1;
+        if (!warp_rect(g, L, xmin, xmax, ymin, ymax, reach, c0, c1, r0, r1)) continue;
+        const int rc = clampi((int)floor((0.5 * (ymin + ymax) - g.y0) * g.inv_cs[L]), r0, r1);
+        const int cc = clampi((int)floor((0.5 * (xmin + xmax) - g.x0) * g.inv_cs[L]), c0, c1);
+        const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
+        const Cell* cells = ctx.cells + g.cell_off[L];
+        const int ncol = g.ncol[L];
     for (int kr = 0; kr < nr; ++kr) {
         const int r = centre_out(kr, rc, r0, r1);
         for (int kc = 0; kc < ncl; ++kc) {
             const int c = centre_out(kc, cc, c0, c1);
-            const Cell cell = ctx.cells[r * g.ncol + c];
+            const Cell cell = cells[r * ncol + c];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
             const float cut = (phase == PH_COLLECT) ? ls.thr : ls.blo;
@@ -288,7 +320,6 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
                 for (int jj = 0; jj < nj; ++jj) {
                     const Entry e = sh.ent[wl][jj];
-                    if (e.col != max((int)e.tcol0, c0) || r != max((int)e.trow0, r0)) continue;
                     const float cut2 = (phase == PH_COLLECT) ? ls.thr : ls.blo;
                     float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
                     float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
@@ -323,21 +354,25 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                         ls.chain = true;
                         ls.chain_thr = fminf(ls.chain_thr, qt);
                     }
-                    if (ls.nc == CAND_K) {
+                    // per-point list in global memory (L1/L2 resident while the warp runs)
+                    const int cap = ctx.cand_cap;
+                    uint32_t* lt = ctx.cand + (size_t)ls.self * cap;
+                    float* lh = ctx.cand_hi + (size_t)ls.self * cap;
+                    if (ls.nc == cap) {
                         int w = 0;
-                        for (int q = 0; q < CAND_K; ++q) {
-                            float hq = sh.hi[wl][q][lane];
+                        for (int q = 0; q < cap; ++q) {
+                            float hq = lh[q];
                             if (hq >= keep - gd) {
-                                sh.tri[wl][w][lane] = sh.tri[wl][q][lane];
-                                sh.hi[wl][w][lane] = hq;
+                                lt[w] = lt[q];
+                                lh[w] = hq;
                                 ++w;
                             }
                         }
                         ls.nc = w;
                     }
-                    if (ls.nc < CAND_K) {
-                        sh.tri[wl][ls.nc][lane] = (uint32_t)e.tri;
-                        sh.hi[wl][ls.nc][lane] = hi;
+                    if (ls.nc < cap) {
+                        lt[ls.nc] = (uint32_t)e.tri;
+                        lh[ls.nc] = hi;
                         ++ls.nc;
                     } else {
                         ls.overflow = true;
@@ -346,13 +381,14 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
             }
         }
     }
+    }
 }
 
 // KIND 1/2 (cone, composite): the per-triangle effect depends on the running
 // height (tip/rim short-circuits), so the collection threshold is closed
 // over the branch thresholds of the relevant triangles (three passes).
 template <int KIND>
-__global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_constant__ DropCtx ctx) {
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __grid_constant__ DropCtx ctx) {
     __shared__ ScanShared sh;
     for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
     __syncthreads();
@@ -375,19 +411,17 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_
     ls.overflow = false;
     ls.chain = false;
     ls.chain_thr = 3.0e38f;
+    ls.self = i;
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    int c0, c1, r0, r1;
-    if (warp_rect(g, xmin, xmax, ymin, ymax, ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius), c0, c1, r0, r1)) {
-        const int rc = clampi((int)floor((0.5 * (ymin + ymax) - g.y0) * g.inv_cs), r0, r1);
-        const int cc = clampi((int)floor((0.5 * (xmin + xmax) - g.x0) * g.inv_cs), c0, c1);
+    {
         if (KIND == 0) {
-            scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
             ls.thr = ls.blo;
         } else {
-            scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
-            scan_cells<KIND>(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+            scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+            scan_cells<KIND>(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
             ls.thr = fminf(ls.blo, ls.qthr);
             // collect; if a collected triangle's branch threshold lies below
             // the collection threshold, lower it and collect again
@@ -401,7 +435,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_
                 } else {
                     ls.thr = 3.0e38f;  // finished lanes collect nothing more
                 }
-                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, c0, c1, r0, r1, rc, cc);
+                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
                 ls.thr = keep_thr;
                 const bool again = !done && ls.chain && !ls.overflow && round < 3;
                 if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
@@ -409,20 +443,30 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32) k_drop_screen(const __grid_
                 if (!__any_sync(0xffffffffu, again)) break;
             }
         }
-    } else {
-        ls.thr = ls.blo;
     }
     __syncwarp();
     if (active) {
         if (ls.overflow || ls.chain) {
-            ctx.ncand[i] = 0xFF;
+            ctx.ncand[i] = 0xFFFF;
+            atomicAdd(&ctx.counters[ls.overflow ? C_OVERFLOW : C_CHAIN], 1ull);
         } else {
+            uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
+            const float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
             int w = 0;
-            for (int q = 0; q < ls.nc; ++q) {
-                float hq = sh.hi[wl][q][lane];
-                if (hq >= ls.thr - gd) ctx.cand[(size_t)i * CAND_K + w++] = sh.tri[wl][q][lane];
+            for (int q = 0; q < ls.nc; ++q)
+                if (lh[q] >= ls.thr - gd) lt[w++] = lt[q];
+            // order the list by the reference's visit order (ascending KD rank)
+            for (int a = 1; a < w; ++a) {
+                const uint32_t t = lt[a];
+                const uint32_t rk = ctx.t32[t].kd_rank;
+                int b = a - 1;
+                while (b >= 0 && ctx.t32[lt[b]].kd_rank > rk) {
+                    lt[b + 1] = lt[b];
+                    --b;
+                }
+                lt[b + 1] = t;
             }
-            ctx.ncand[i] = (uint8_t)w;
+            ctx.ncand[i] = (uint16_t)w;
         }
         ctx.blo[i] = ls.blo;
     }
@@ -441,26 +485,10 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint32_t)ctx.M) return;
     const int n = ctx.ncand[i];
-    if (n == 0xFF) return;  // handed to the plain path
+    if (n == 0xFFFF) return;  // handed to the plain path
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
     const double R = ctx.cp.radius;
-    uint32_t tri[CAND_K], rank[CAND_K];
-    for (int q = 0; q < n; ++q) {
-        tri[q] = ctx.cand[(size_t)i * CAND_K + q];
-        rank[q] = ctx.t32[tri[q]].kd_rank;
-    }
-    // insertion sort by KD rank
-    for (int a = 1; a < n; ++a) {
-        uint32_t t = tri[a], rk = rank[a];
-        int b = a - 1;
-        while (b >= 0 && rank[b] > rk) {
-            tri[b + 1] = tri[b];
-            rank[b + 1] = rank[b];
-            --b;
-        }
-        tri[b + 1] = t;
-        rank[b + 1] = rk;
-    }
+    const uint32_t* tri = ctx.cand + (size_t)i * ctx.cand_cap;  // already in KD order
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     int capped = 0;
     const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
@@ -501,10 +529,10 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
 }
 
-__global__ void k_collect_overflow(const uint8_t* ncand, int M, uint32_t* list, unsigned long long* counter) {
+__global__ void k_collect_overflow(const uint16_t* ncand, int M, uint32_t* list, unsigned long long* counter) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
-    if (ncand[i] == 0xFF) {
+    if (ncand[i] == 0xFFFF) {
         unsigned long long slot = atomicAdd(counter, 1ull);
         list[slot] = (uint32_t)i;
     }
@@ -517,7 +545,8 @@ struct DropWork {
     DevBuf<uint32_t> keys, keys2, perm0, perm;
     DevBuf<double> cls;
     DevBuf<uint32_t> cand;
-    DevBuf<uint8_t> ncand;
+    DevBuf<float> cand_hi;
+    DevBuf<uint16_t> ncand;
     DevBuf<float> blo;
     DevBuf<uint32_t> list;
     DevBuf<unsigned long long> counters;
@@ -529,7 +558,7 @@ struct DropWork {
         if (M > cap || !counters.p) {
             size_t c = std::max<size_t>(M, 1024);
             if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
-                !cand.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) ||
+                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) ||
                 !counters.alloc(C_NCOUNTERS + 1))
                 return false;
             cap = c;
@@ -571,6 +600,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     h->out_cc = d_cc;
     h->out_type = d_type;
     h->cand = w.cand.p;
+    h->cand_hi = w.cand_hi.p;
+    h->cand_cap = CAND_K;
     h->ncand = w.ncand.p;
     h->blo = w.blo.p;
     h->counters = w.counters.p;
@@ -605,7 +636,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     CK(cudaEventRecord(ev[1], stream));
     if (m.n == 0) {
         // empty surface: every point keeps its z, CC stays NONE
-        CK(cudaMemsetAsync(w.ncand.p, 0, M, stream));
+        CK(cudaMemsetAsync(w.ncand.p, 0, M * sizeof(uint16_t), stream));
         CK(cudaMemsetAsync(w.blo.p, 0xFF, M * sizeof(float), stream));
         CK(cudaEventRecord(ev[2], stream));
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
@@ -614,7 +645,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     } else if (precision == OCL_GB300_PREC_FP64) {
         CK(cudaEventRecord(ev[2], stream));
         CK(cudaEventRecord(ev[3], stream));
-        k_drop_kd<<<(warps + 3) / 4, 128, 0, stream>>>(*h, nullptr, nullptr);
+        k_drop_kd<false><<<(warps + 3) / 4, 128, 0, stream>>>(*h, nullptr, nullptr);
         launches += 1;
     } else {
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
@@ -630,7 +661,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
         // the fallback grid strides over however many points overflowed
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
-        k_drop_kd<<<fb_blocks, 128, 0, stream>>>(*h, w.list.p, w.counters.p + C_FALLBACK);
+        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list.p, w.counters.p + C_FALLBACK);
         launches += 4;
     }
     CK(cudaGetLastError());
@@ -650,6 +681,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         stats->fallback = c[C_FALLBACK];
         stats->violations = c[C_VIOLATION];
         stats->screened = c[C_SCREENED];
+        stats->overflow_points = c[C_OVERFLOW];
+        stats->chain_points = c[C_CHAIN];
         stats->launches = launches;
         stats->kernel_ms = t_all;
         stats->screen_ms = t_scr;
@@ -675,10 +708,11 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
 // ---------------------------------------------------------------------------
 struct NoAllocScratch {
     uint32_t perm[OCL_GB300_NOALLOC_MAX_POINTS];
-    uint32_t cand[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K];
+    uint32_t cand[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
+    float cand_hi[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     uint32_t list[OCL_GB300_NOALLOC_MAX_POINTS];
     float blo[OCL_GB300_NOALLOC_MAX_POINTS];
-    uint8_t ncand[OCL_GB300_NOALLOC_MAX_POINTS];
+    uint16_t ncand[OCL_GB300_NOALLOC_MAX_POINTS];
     unsigned long long counters[C_NCOUNTERS + 1];
 };
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
@@ -741,6 +775,8 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     h.out_cc = d_cc;
     h.out_type = d_type;
     h.cand = sc->cand;
+    h.cand_hi = sc->cand_hi;
+    h.cand_cap = CAND_K_NOALLOC;
     h.ncand = sc->ncand;
     h.blo = sc->blo;
     h.counters = sc->counters;
@@ -759,7 +795,7 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     k_noalloc_identity<<<nb, TB, 0, stream>>>(sc->perm, (int)M);
     const unsigned warps = (unsigned)((M + 31) / 32);
     if (m.n == 0) {
-        CK(cudaMemsetAsync(sc->ncand, 0, M, stream));
+        CK(cudaMemsetAsync(sc->ncand, 0, M * sizeof(uint16_t), stream));
         CK(cudaMemsetAsync(sc->blo, 0xFF, M * sizeof(float), stream));
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
     } else {
@@ -773,7 +809,7 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
         k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
-        k_drop_kd<<<fb_blocks, 128, 0, stream>>>(h, sc->list, sc->counters + C_FALLBACK);
+        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(h, sc->list, sc->counters + C_FALLBACK);
     }
     CK(cudaGetLastError());
     return OCL_GB300_OK;

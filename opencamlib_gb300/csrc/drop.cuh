@@ -6,7 +6,8 @@
 namespace oclg {
 
 constexpr int HLB_N = 256;   // entries of the height lower-bound table
-constexpr int CAND_K = 40;   // refinement candidates kept per CL point
+constexpr int CAND_K = 256;  // refinement candidates kept per CL point (drop_run)
+constexpr int CAND_K_NOALLOC = 64;  // the same for the no-allocation entry point
 
 enum Counter {
     C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)
@@ -15,6 +16,8 @@ enum Counter {
     C_VIOLATION = 3,  // FP64 result below a certified FP32 lower bound (must stay 0)
     C_CAPPED = 4,     // Brent solves that hit the iteration cap
     C_SCREENED = 5,   // FP32 whole-triangle screens
+    C_OVERFLOW = 6,   // points handed back because their candidate list overflowed
+    C_CHAIN = 7,      // points handed back because branch thresholds kept chaining
     C_NCOUNTERS = 8
 };
 
@@ -34,8 +37,10 @@ struct DropCtx {
     double* out_z;
     double* out_cc;
     int32_t* out_type;
-    uint32_t* cand;         // M x CAND_K candidate triangles
-    uint8_t* ncand;         // per CL: count, or 0xFF = overflow
+    uint32_t* cand;         // M x cand_cap candidate triangles (sorted by KD rank when final)
+    float* cand_hi;         // M x cand_cap their FP32 upper bounds (screen only)
+    uint16_t* ncand;        // per CL: count, or 0xFFFF = handed to the plain path
+    int cand_cap;           // list capacity per CL point
     float* blo;             // per CL: certified lower bound (local frame)
     unsigned long long* counters;
     float E;                // FP32 position error budget

@@ -158,63 +158,78 @@ void kd_build_host(const std::vector<double>& bb6, uint64_t n, unsigned bucket, 
 }
 
 // ---------------------------------------------------------------------------
-// Device grid build.
+// Multi-level grid.  Host: level and home cell of every triangle (this fixes
+// the device order of the triangles: sorted by (level, home cell)).  Device:
+// entries (FP32 bboxes rounded outward) and per-cell bounds over the cell's
+// own triangles (union bbox, max z), from the sorted cell keys.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cell_range(const GridP& g, const double* bb, int& c0, int& c1, int& r0, int& r1) {
-    c0 = clampi((int)floor((bb[0] - g.x0) * g.inv_cs), 0, g.ncol - 1);
-    c1 = clampi((int)floor((bb[1] - g.x0) * g.inv_cs), 0, g.ncol - 1);
-    r0 = clampi((int)floor((bb[2] - g.y0) * g.inv_cs), 0, g.nrow - 1);
-    r1 = clampi((int)floor((bb[3] - g.y0) * g.inv_cs), 0, g.nrow - 1);
+static void grid_params(Mesh& M, const std::vector<Tri64>& t64, GridP& g) {
+    const uint64_t n = M.n;
+    double ex = std::max(M.bb[1] - M.bb[0], 1e-9), ey = std::max(M.bb[3] - M.bb[2], 1e-9);
+    // finest cell: 1.25 x the 90th percentile of the triangles' xy extent,
+    // at least half the mean spacing, at most 4096 cells per axis
+    std::vector<double> ext(n);
+    for (uint64_t i = 0; i < n; ++i) ext[i] = std::max(t64[i].bb[1] - t64[i].bb[0], t64[i].bb[3] - t64[i].bb[2]);
+    double p90 = 0.0;
+    if (n > 0) {
+        size_t k = (size_t)(0.9 * (double)(n - 1));
+        std::nth_element(ext.begin(), ext.begin() + k, ext.end());
+        p90 = ext[k];
+    }
+    double cs = std::max(1.25 * p90, 0.5 * std::sqrt(ex * ey / (double)std::max<uint64_t>(n, 1)));
+    cs = std::max(cs, std::max(ex, ey) / 4096.0);
+    cs = std::max(cs, 1e-9);
+    g.x0 = M.bb[0];
+    g.y0 = M.bb[2];
+    g.ox = 0.5 * (M.bb[0] + M.bb[1]);
+    g.oy = 0.5 * (M.bb[2] + M.bb[3]);
+    g.oz = 0.5 * (M.bb[4] + M.bb[5]);
+    g.nlev = 0;
+    uint32_t off = 0;
+    for (int L = 0; L < GRID_MAX_LEVELS; ++L) {
+        g.cs[L] = cs;
+        g.inv_cs[L] = 1.0 / cs;
+        g.ncol[L] = (int)std::floor(ex / cs) + 1;
+        g.nrow[L] = (int)std::floor(ey / cs) + 1;
+        g.cell_off[L] = off;
+        off += (uint32_t)g.ncol[L] * (uint32_t)g.nrow[L];
+        g.nlev = L + 1;
+        if (g.ncol[L] == 1 && g.nrow[L] == 1) break;
+        cs *= 4.0;
+    }
+    g.cell_off[g.nlev] = off;
 }
 
-__global__ void k_grid_count(const Tri64* t, uint64_t n, GridP g, uint64_t* cnt) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c0, c1, r0, r1;
-    cell_range(g, t[i].bb, c0, c1, r0, r1);
-    cnt[i] = (uint64_t)(c1 - c0 + 1) * (uint64_t)(r1 - r0 + 1);
-}
-
-__global__ void k_grid_emit(const Tri64* t, uint64_t n, GridP g, const uint64_t* off, uint32_t* keys, uint32_t* vals) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c0, c1, r0, r1;
-    cell_range(g, t[i].bb, c0, c1, r0, r1);
-    uint64_t o = off[i];
-    for (int r = r0; r <= r1; ++r)
-        for (int c = c0; c <= c1; ++c) {
-            keys[o] = (uint32_t)(r * g.ncol + c);
-            vals[o] = (uint32_t)i;
-            ++o;
-        }
+// level and global home-cell index of one triangle
+static uint32_t grid_key(const GridP& g, const double* bb) {
+    const double dx = bb[1] - bb[0], dy = bb[3] - bb[2];
+    int L = 0;
+    while (L < g.nlev - 1 && (dx > g.cs[L] || dy > g.cs[L])) ++L;
+    int c = std::min(std::max((int)std::floor((bb[0] - g.x0) * g.inv_cs[L]), 0), g.ncol[L] - 1);
+    int r = std::min(std::max((int)std::floor((bb[2] - g.y0) * g.inv_cs[L]), 0), g.nrow[L] - 1);
+    return g.cell_off[L] + (uint32_t)r * (uint32_t)g.ncol[L] + (uint32_t)c;
 }
 
 __device__ __forceinline__ float f_rd(double x) { return __double2float_rd(x); }
 __device__ __forceinline__ float f_ru(double x) { return __double2float_ru(x); }
 
-__global__ void k_grid_entries(const Tri64* t, GridP g, const uint32_t* keys, const uint32_t* vals, uint64_t total,
-                               Entry* ent, uint32_t* cstart, uint32_t* cend) {
+__global__ void k_grid_entries(const Tri64* t, GridP g, const uint32_t* keys, uint64_t n, Entry* ent,
+                               uint32_t* cstart, uint32_t* cend) {
     uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (k >= total) return;
-    uint32_t key = keys[k];
-    uint32_t tri = vals[k];
-    const double* bb = t[tri].bb;
+    if (k >= n) return;
+    const double* bb = t[k].bb;
     Entry e;
     e.minx = f_rd(bb[0] - g.ox);
     e.maxx = f_ru(bb[1] - g.ox);
     e.miny = f_rd(bb[2] - g.oy);
     e.maxy = f_ru(bb[3] - g.oy);
     e.maxz = f_ru(bb[5] - g.oz);
-    e.tri = (int32_t)tri;
-    int c0, c1, r0, r1;
-    cell_range(g, bb, c0, c1, r0, r1);
-    e.col = (uint16_t)(key % (uint32_t)g.ncol);
-    e.tcol0 = (uint16_t)c0;
-    e.trow0 = (uint16_t)r0;
-    e.pad = 0;
+    e.tri = (int32_t)k;
+    e.pad[0] = e.pad[1] = 0.0f;
     ent[k] = e;
+    const uint32_t key = keys[k];
     if (k == 0 || keys[k - 1] != key) cstart[key] = (uint32_t)k;
-    if (k == total - 1 || keys[k + 1] != key) cend[key] = (uint32_t)(k + 1);
+    if (k == n - 1 || keys[k + 1] != key) cend[key] = (uint32_t)(k + 1);
 }
 
 __global__ void k_grid_cells(const Entry* ent, const uint32_t* cstart, const uint32_t* cend, uint32_t ncells,
@@ -238,70 +253,27 @@ __global__ void k_grid_cells(const Entry* ent, const uint32_t* cstart, const uin
     cells[c] = cl;
 }
 
-static int build_grid(Mesh& m, const std::vector<Tri64>& t64dev) {
+static int build_grid(Mesh& m, const std::vector<uint32_t>& keys_dev) {
     const uint64_t n = m.n;
-    GridP& g = m.grid;
-    double ex = std::max(m.bb[1] - m.bb[0], 1e-9), ey = std::max(m.bb[3] - m.bb[2], 1e-9);
-    double cs = 2.5 * std::sqrt(ex * ey / (double)std::max<uint64_t>(n, 1));
-    cs = std::max(cs, std::max(ex, ey) / 4096.0);
-    cs = std::max(cs, 1e-9);
-    g.x0 = m.bb[0];
-    g.y0 = m.bb[2];
-    g.cs = cs;
-    g.inv_cs = 1.0 / cs;
-    g.ncol = (int)std::floor(ex / cs) + 1;
-    g.nrow = (int)std::floor(ey / cs) + 1;
-    g.ox = 0.5 * (m.bb[0] + m.bb[1]);
-    g.oy = 0.5 * (m.bb[2] + m.bb[3]);
-    g.oz = 0.5 * (m.bb[4] + m.bb[5]);
-    const uint32_t ncells = (uint32_t)g.ncol * (uint32_t)g.nrow;
-
-    DevBuf<uint32_t> keys, vals, keys2, vals2, cstart(ncells), cend(ncells);
-    DevBuf<uint64_t> cnt(n), off(n);
-    if (!cnt.ok() || !off.ok() || !cstart.ok() || !cend.ok()) return OCL_GB300_OOM;
-    const int TB = 256;
-    unsigned nb = (unsigned)((n + TB - 1) / TB);
-    k_grid_count<<<nb, TB>>>(m.d_t64, n, g, cnt.p);
-    size_t sb = 0;
-    CK(cub::DeviceScan::ExclusiveSum(nullptr, sb, cnt.p, off.p, (int64_t)n));
-    {
-        DevBuf<uint8_t> st(sb);
-        if (!st.ok()) return OCL_GB300_OOM;
-        CK(cub::DeviceScan::ExclusiveSum(st.p, sb, cnt.p, off.p, (int64_t)n));
-    }
-    uint64_t last_off = 0, last_cnt = 0;
-    CK(cudaMemcpy(&last_off, off.p + (n - 1), sizeof(uint64_t), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&last_cnt, cnt.p + (n - 1), sizeof(uint64_t), cudaMemcpyDeviceToHost));
-    uint64_t total = last_off + last_cnt;
-    if (total >= (1ull << 32)) {
-        set_error("grid too large");
-        return OCL_GB300_OOM;
-    }
-    if (!keys.alloc(total) || !vals.alloc(total) || !keys2.alloc(total) || !vals2.alloc(total)) return OCL_GB300_OOM;
-    k_grid_emit<<<nb, TB>>>(m.d_t64, n, g, off.p, keys.p, vals.p);
-    int endbit = 1;
-    while ((1ull << endbit) < ncells) ++endbit;
-    size_t tmpb = 0;
-    CK(cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys.p, keys2.p, vals.p, vals2.p, (int64_t)total, 0, endbit));
-    DevBuf<uint8_t> tmp(tmpb);
-    if (!tmp.ok()) return OCL_GB300_OOM;
-    CK(cub::DeviceRadixSort::SortPairs(tmp.p, tmpb, keys.p, keys2.p, vals.p, vals2.p, (int64_t)total, 0, endbit));
+    const GridP& g = m.grid;
+    const uint32_t ncells = g.cell_off[g.nlev];
+    DevBuf<uint32_t> keys(n), cstart(ncells), cend(ncells);
+    if (!keys.ok() || !cstart.ok() || !cend.ok()) return OCL_GB300_OOM;
+    CK(cudaMemcpy(keys.p, keys_dev.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemset(cstart.p, 0, ncells * sizeof(uint32_t)));
     CK(cudaMemset(cend.p, 0, ncells * sizeof(uint32_t)));
     if (m.d_entries) cudaFree(m.d_entries);
     if (m.d_cells) cudaFree(m.d_cells);
     m.d_entries = nullptr;
     m.d_cells = nullptr;
-    CK(cudaMalloc(&m.d_entries, std::max<uint64_t>(total, 1) * sizeof(Entry)));
+    CK(cudaMalloc(&m.d_entries, std::max<uint64_t>(n, 1) * sizeof(Entry)));
     CK(cudaMalloc(&m.d_cells, (size_t)ncells * sizeof(Cell)));
-    if (total > 0)
-        k_grid_entries<<<(unsigned)((total + TB - 1) / TB), TB>>>(m.d_t64, g, keys2.p, vals2.p, total, m.d_entries,
-                                                                   cstart.p, cend.p);
+    const int TB = 256;
+    k_grid_entries<<<(unsigned)((n + TB - 1) / TB), TB>>>(m.d_t64, g, keys.p, n, m.d_entries, cstart.p, cend.p);
     k_grid_cells<<<(ncells + TB - 1) / TB, TB>>>(m.d_entries, cstart.p, cend.p, ncells, m.d_cells);
     CK(cudaGetLastError());
     CK(cudaDeviceSynchronize());
-    m.nentries = total;
-    (void)t64dev;
+    m.nentries = n;
     return OCL_GB300_OK;
 }
 
@@ -364,25 +336,19 @@ int mesh_create(const double* tris, uint64_t n, unsigned bucket, Mesh** out) {
     std::vector<uint32_t> kd_rank(n);
     for (uint64_t r = 0; r < kd.order.size(); ++r) kd_rank[kd.order[r]] = (uint32_t)r;
 
-    // grid parameters decide the device order: row-major by min-corner cell
+    // grid parameters decide the device order: sorted by (level, home cell)
     Mesh& M = *m;
-    double ex = std::max(M.bb[1] - M.bb[0], 1e-9), ey = std::max(M.bb[3] - M.bb[2], 1e-9);
-    double cs = 2.5 * std::sqrt(ex * ey / (double)std::max<uint64_t>(n, 1));
-    cs = std::max(cs, std::max(ex, ey) / 4096.0);
-    cs = std::max(cs, 1e-9);
-    int ncol = (int)std::floor(ex / cs) + 1;
-    std::vector<uint64_t> key(n);
-    for (uint64_t i = 0; i < n; ++i) {
-        int c = std::min(std::max((int)std::floor((t64[i].bb[0] - M.bb[0]) * (1.0 / cs)), 0), ncol - 1);
-        int r = std::max((int)std::floor((t64[i].bb[2] - M.bb[2]) * (1.0 / cs)), 0);
-        key[i] = (uint64_t)r * (uint64_t)ncol + (uint64_t)c;
-    }
+    grid_params(M, t64, M.grid);
+    std::vector<uint32_t> key(n);
+    for (uint64_t i = 0; i < n; ++i) key[i] = grid_key(M.grid, t64[i].bb);
     M.dev_to_ins.resize(n);
     std::iota(M.dev_to_ins.begin(), M.dev_to_ins.end(), 0);
     std::stable_sort(M.dev_to_ins.begin(), M.dev_to_ins.end(),
                      [&](int32_t a, int32_t b) { return key[a] < key[b]; });
     M.ins_to_dev.resize(n);
     for (uint64_t d = 0; d < n; ++d) M.ins_to_dev[M.dev_to_ins[d]] = (int32_t)d;
+    std::vector<uint32_t> key_dev(n);
+    for (uint64_t d = 0; d < n; ++d) key_dev[d] = key[M.dev_to_ins[d]];
 
     double ox = 0.5 * (M.bb[0] + M.bb[1]), oy = 0.5 * (M.bb[2] + M.bb[3]), oz = 0.5 * (M.bb[4] + M.bb[5]);
     std::vector<Tri64> t64d(n);
@@ -423,7 +389,7 @@ int mesh_create(const double* tris, uint64_t n, unsigned bucket, Mesh** out) {
             delete m;
             return OCL_GB300_DEVICE_ERROR;
         }
-        st = build_grid(M, t64d);
+        st = build_grid(M, key_dev);
         if (st != OCL_GB300_OK) {
             delete m;
             return st;

@@ -121,6 +121,8 @@ static int drop_host(Mesh& m, const CutterP& cp, const std::vector<double>& cl, 
         acc->fallback += st.fallback;
         acc->violations += st.violations;
         acc->screened += st.screened;
+        acc->overflow_points += st.overflow_points;
+        acc->chain_points += st.chain_points;
         acc->kernel_ms += st.kernel_ms;
     }
     return OCL_GB300_OK;

@@ -61,7 +61,7 @@ def test_noalloc_matches_drop_two_calls_in_a_row(env):
     mesh = ocl.DeviceMesh(tris)
     # first call: many points, bull cutter; second: fewer points, ball cutter,
     # so stale scratch contents from the first call would show
-    cl1 = w.raster(120, 120, 100.0 / 119.0, z0=-50.0)
+    cl1 = w.raster(90, 90, 100.0 / 89.0, z0=-50.0)
     cl2 = w.raster(50, 40, 2.0, z0=-20.0, x0=1.3, y0=2.1)
     for cutter, cl in ((ocl.BullCutter(6.0, 1.0, 20.0), cl1), (ocl.BallCutter(6.0, 20.0), cl2)):
         ref = mesh.drop(cutter, cl, precision="mixed")[:3]
@@ -82,7 +82,7 @@ def test_noalloc_rejects_too_many_points(env):
     ocl, torch = env
     mesh = ocl.DeviceMesh(w.heightfield(8, 8, seed=1))
     L = ocl.lib()
-    M = 16384 + 1
+    M = 8192 + 1
     desc = ocl.BallCutter(6.0, 20.0).desc()
     st = L.ocl_gb300_drop_device_noalloc(mesh.handle, C.byref(desc), C.c_void_p(1), M, C.c_void_p(1),
                                          C.c_void_p(1), C.c_void_p(1), None)
