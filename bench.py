@@ -335,6 +335,9 @@ def main():
         "per_cutter": {n: {"kernel_ms": st.kernel_ms, "screen_ms": st.screen_ms, "refine_ms": st.refine_ms,
                            "fallback_ms": st.fallback_ms, "fallback_points": int(st.fallback),
                            "overflow_points": int(st.overflow_points), "chain_points": int(st.chain_points),
+                           "open_branch_points": int(st.open_branch_points),
+                           "untracked_branch_points": int(st.untracked_branch_points),
+                           "plain_points": int(st.plain_points),
                            "refined_per_point": st.refined / M, "screened_per_point": st.screened / M}
                        for n, st in breakdown},
         "clocks": clocks,

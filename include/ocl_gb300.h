@@ -117,6 +117,12 @@ typedef struct ocl_gb300_stats {
     uint64_t screened;       /* FP32 whole-triangle screens */
     uint64_t overflow_points;/* of the fallback points: candidate list overflow */
     uint64_t chain_points;   /* of the fallback points: branch thresholds kept chaining */
+    uint64_t open_branch_points; /* points collected below their lower bound: a
+                                    triangle's branch (cone tip/rim, composite
+                                    facet short-circuit) stayed undecided */
+    uint64_t untracked_branch_points; /* of those: more branching triangles than tracked */
+    uint64_t plain_points;   /* of the fallback points: more candidates than the exact
+                                per-point kernel holds, done by the plain FP64 kernel */
     uint64_t launches;       /* kernels of this library launched by the call */
     double   kernel_ms;      /* device time of the call's kernels (CUDA events) */
     double   screen_ms;      /* of which the FP32 screen kernel */

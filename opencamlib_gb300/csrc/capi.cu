@@ -134,6 +134,15 @@ void fill_comp(const CutterP& cp, Comp32& comp) {
         basic_prof(cp.sub[n], comp.sub[n]);
         comp.zoff[n] = (float)cp.zoffset[n];
         comp.rlim[n] = (float)cp.radiusvec[n];
+        // CompositeCutter::ccValidRadius (compositecutter.cpp:86-102) bounds
+        const double lo = (n == 0) ? -1E-6 : cp.radiusvec[n - 1] - 1E-6;
+        const double hi = cp.radiusvec[n] + 1e-6;
+        float f = (float)lo;
+        comp.wlo_in[n] = ((double)f >= lo) ? f : std::nextafter(f, 3.0e38f);
+        comp.wlo_out[n] = ((double)f <= lo) ? f : std::nextafter(f, -3.0e38f);
+        f = (float)hi;
+        comp.whi_in[n] = ((double)f <= hi) ? f : std::nextafter(f, -3.0e38f);
+        comp.whi_out[n] = ((double)f >= hi) ? f : std::nextafter(f, 3.0e38f);
     }
 }
 

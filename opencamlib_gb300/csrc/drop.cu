@@ -257,14 +257,18 @@ __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx
 // FP32 screen
 // ---------------------------------------------------------------------------
 constexpr int SCREEN_WARPS = 4;
+constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 
-enum ScanPhase { PH_SINGLE = 0, PH_LOWER = 1, PH_THRESH = 2, PH_COLLECT = 3 };
+enum ScanPhase { PH_SINGLE = 0, PH_LOWER = 1, PH_RESOLVE = 2, PH_COLLECT = 3 };
 
 struct LaneState {
     float blo;       // certified lower bound of the final height
-    float qthr;      // lowest branch threshold of a relevant cone triangle
-    float thr;       // collection threshold (PH_COLLECT)
+    float qx;        // lowest branch threshold of relevant triangles not tracked
+    float thr;       // collection threshold (PH_RESOLVE cut, PH_COLLECT keep)
+    float zu;        // start height rounded up (local frame)
     int nc;
+    int nb;          // tracked branching triangles
+    unsigned resolved;  // bit j: branch of tracked triangle j is decided
     bool overflow;
     bool chain;      // a collected triangle's branch depends on uncollected ones
     float chain_thr; // lowest branch threshold among chained triangles
@@ -272,10 +276,36 @@ struct LaneState {
     unsigned long long screened;
 };
 
+// Branching triangles of one warp's lanes ([slot][lane]): triangles whose
+// effect on the running height Z has a branch point in [qlo, qhi] (cone tip
+// and rim, composite facet short-circuits).  W/wtri: the highest certified
+// lower bound among triangles visited before it (lower KD rank) and that
+// triangle; H: the highest upper bound among them (or the start height).
+//   W > qhi: every fold reaches the triangle with Z above all branch points;
+//   H < qlo: every fold reaches it with Z below all branch points;
+// either way its branch is decided without the triangles below the bound.
+struct BranchTab {
+    uint32_t tri[NBRANCH][32];
+    uint32_t rank[NBRANCH][32];
+    float qlo[NBRANCH][32];
+    float qhi[NBRANCH][32];
+    float hi[NBRANCH][32];
+    float W[NBRANCH][32];
+    float H[NBRANCH][32];
+    uint32_t wtri[NBRANCH][32];
+};
+
 struct ScanShared {
     float hlb[HLB_N];
     Entry ent[SCREEN_WARPS][32];
+    BranchTab br[SCREEN_WARPS];
 };
+
+__device__ __forceinline__ bool is_resolved(const BranchTab& b, const LaneState& ls, int lane, uint32_t tri) {
+    for (int j = 0; j < ls.nb; ++j)
+        if (((ls.resolved >> j) & 1u) && b.tri[j][lane] == tri) return true;
+    return false;
+}
 
 // One pass over the cells under the warp's footprint (centre rows first).
 // KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
@@ -285,6 +315,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                                            double ymax) {
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
+    BranchTab& br = sh.br[wl];
     const GridP& g = ctx.g;
     const float R = ctx.prof.R;
     const float gd = ctx.guard;
@@ -307,7 +338,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
             const Cell cell = cells[r * ncol + c];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
-            const float cut = (phase == PH_COLLECT) ? ls.thr : ls.blo;
+            const float cut = (phase == PH_COLLECT || phase == PH_RESOLVE) ? ls.thr : ls.blo;
             float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
             float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
             float d = sqrtf(dx * dx + dy * dy);
@@ -320,7 +351,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
                 for (int jj = 0; jj < nj; ++jj) {
                     const Entry e = sh.ent[wl][jj];
-                    const float cut2 = (phase == PH_COLLECT) ? ls.thr : ls.blo;
+                    const float cut2 = (phase == PH_COLLECT || phase == PH_RESOLVE) ? ls.thr : ls.blo;
                     float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
                     float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
                     float de = sqrtf(ex * ex + ey * ey);
@@ -328,29 +359,62 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     bool p1 = active && de <= Rg && ub >= cut2 - gd && ub > z0l - gd;
                     if (!__any_sync(0xffffffffu, p1)) continue;
                     if (!p1) continue;
-                    float lo = NEG_INF32, hi = ub + gd, qt = 3.0e38f;
+                    float lo = NEG_INF32, hi = ub + gd, qt = 3.0e38f, qth = NEG_INF32;
+                    uint32_t rank = 0;
                     {
                         const Tri32 t = ctx.t32[e.tri];
                         Iv v = (KIND == 2)
-                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt)
-                                   : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt);
+                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2],
+                                                      qt, qth)
+                                   : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2],
+                                                     qt, qth);
                         ++ls.screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
                         hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, hi) : NEG_INF32;
-                        if (qt < 3.0e38f) qt = qt + t.v0[2] - ctx.E;
+                        if (qt < 3.0e38f) {
+                            qt = qt + t.v0[2] - ctx.E;
+                            qth = qth + t.v0[2] + ctx.E;
+                        }
+                        rank = t.kd_rank;
                     }
                     if (phase == PH_SINGLE || phase == PH_LOWER) {
                         if (lo > ls.blo) ls.blo = lo;
                     }
-                    if (phase == PH_THRESH) {
-                        if (hi >= ls.blo - gd && qt < ls.qthr) ls.qthr = qt;
+                    if (phase == PH_LOWER) {
+                        // track triangles that branch and may still matter
+                        if (qt < 3.0e38f && hi >= ls.blo - gd) {
+                            int slot = ls.nb < NBRANCH ? ls.nb : -1;
+                            for (int j = 0; slot < 0 && j < NBRANCH; ++j)
+                                if (br.hi[j][lane] < ls.blo - gd) slot = j;  // no longer relevant
+                            if (slot < 0) {
+                                ls.qx = fminf(ls.qx, qt);
+                            } else {
+                                br.tri[slot][lane] = e.tri;
+                                br.rank[slot][lane] = rank;
+                                br.qlo[slot][lane] = qt;
+                                br.qhi[slot][lane] = qth;
+                                br.hi[slot][lane] = hi;
+                                if (slot == ls.nb) ++ls.nb;
+                            }
+                        }
                         continue;
                     }
-                    if (phase == PH_LOWER) continue;
-                    // collect (PH_SINGLE: lazily pruned against the rising bound)
+                    if (phase == PH_RESOLVE) {
+                        for (int j = 0; j < ls.nb; ++j) {
+                            if (rank < br.rank[j][lane]) {
+                                if (lo > br.W[j][lane]) {
+                                    br.W[j][lane] = lo;
+                                    br.wtri[j][lane] = e.tri;
+                                }
+                                br.H[j][lane] = fmaxf(br.H[j][lane], hi);
+                            }
+                        }
+                    }
+                    // collect (PH_SINGLE: lazily pruned against the rising bound;
+                    // PH_RESOLVE: optimistically against blo)
                     const float keep = (phase == PH_COLLECT) ? ls.thr : ls.blo;
                     if (!(hi >= keep - gd && hi > z0l - gd) || ls.overflow) continue;
-                    if (phase == PH_COLLECT && qt < ls.thr - gd) {
+                    if (phase == PH_COLLECT && qt < ls.thr - gd && !is_resolved(br, ls, lane, e.tri)) {
                         ls.chain = true;
                         ls.chain_thr = fminf(ls.chain_thr, qt);
                     }
@@ -384,9 +448,13 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     }
 }
 
-// KIND 1/2 (cone, composite): the per-triangle effect depends on the running
-// height (tip/rim short-circuits), so the collection threshold is closed
-// over the branch thresholds of the relevant triangles (three passes).
+// KIND 1/2 (cone, composite): the effect of a triangle on the running height
+// can depend on the height reached before it (tip/rim short-circuits).
+//   pass 1  certified lower bound blo; branching triangles that may matter;
+//   pass 2  decide each branching triangle from the triangles visited before
+//           it (BranchTab), collecting optimistically at blo;
+//   then    if a branch stays open, collect again at the lowest open branch
+//           threshold, closing over the thresholds of what is collected.
 template <int KIND>
 __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __grid_constant__ DropCtx ctx) {
     __shared__ ScanShared sh;
@@ -403,11 +471,15 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
     const float z0l = __double2float_rd(z0 - g.oz);
     const float gd = ctx.guard;
+    BranchTab& br = sh.br[wl];
     LaneState ls;
     ls.blo = z0l;
-    ls.qthr = 3.0e38f;
+    ls.qx = 3.0e38f;
     ls.thr = 0.0f;
+    ls.zu = __double2float_ru(z0 - g.oz);
     ls.nc = 0;
+    ls.nb = 0;
+    ls.resolved = 0;
     ls.overflow = false;
     ls.chain = false;
     ls.chain_thr = 3.0e38f;
@@ -415,32 +487,86 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    {
-        if (KIND == 0) {
-            scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-            ls.thr = ls.blo;
-        } else {
-            scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-            scan_cells<KIND>(ctx, sh, PH_THRESH, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-            ls.thr = fminf(ls.blo, ls.qthr);
-            // collect; if a collected triangle's branch threshold lies below
-            // the collection threshold, lower it and collect again
-            bool done = false;
+    if (KIND == 0) {
+        scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+        ls.thr = ls.blo;
+    } else {
+        scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+        // keep the branching triangles that can still reach blo
+        {
+            int w = 0;
+            float cut = ls.blo;
+            for (int j = 0; j < ls.nb; ++j) {
+                if (br.hi[j][lane] < ls.blo - gd) continue;
+                br.tri[w][lane] = br.tri[j][lane];
+                br.rank[w][lane] = br.rank[j][lane];
+                br.qlo[w][lane] = br.qlo[j][lane];
+                br.qhi[w][lane] = br.qhi[j][lane];
+                br.hi[w][lane] = br.hi[j][lane];
+                br.W[w][lane] = NEG_INF32;
+                br.H[w][lane] = ls.zu;
+                br.wtri[w][lane] = 0xFFFFFFFFu;
+                cut = fminf(cut, br.qlo[w][lane]);
+                ++w;
+            }
+            ls.nb = w;
+            ls.thr = cut;
+        }
+        scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+        float open = ls.qx;
+        for (int j = 0; j < ls.nb; ++j) {
+            const bool above = br.W[j][lane] > br.qhi[j][lane] + gd;
+            const bool below = br.H[j][lane] < br.qlo[j][lane] - gd;
+            if (above || below) ls.resolved |= 1u << j;
+            else open = fminf(open, br.qlo[j][lane]);
+        }
+        ls.thr = ls.blo;
+        bool need = open < ls.blo && !ls.overflow;
+        if (active && need) {
+            atomicAdd(&ctx.counters[C_OPEN], 1ull);
+            if (ls.qx < ls.blo) atomicAdd(&ctx.counters[C_UNTRACKED], 1ull);
+        }
+        if (__any_sync(0xffffffffu, need)) {
+            // collect at the lowest open threshold; if a collected triangle's
+            // branch threshold lies below it, lower it and collect again
+            const float first = need ? open : 3.0e38f;  // other lanes keep their lists
+            ls.thr = first;
+            bool done = !need;
             for (int round = 0; round < 4; ++round) {
                 const float keep_thr = ls.thr;
                 if (!done) {
                     ls.nc = 0;
                     ls.chain = false;
                     ls.chain_thr = 3.0e38f;
-                } else {
-                    ls.thr = 3.0e38f;  // finished lanes collect nothing more
                 }
-                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active && !done, cx, cy, z0l, xmin, xmax, ymin, ymax);
                 ls.thr = keep_thr;
                 const bool again = !done && ls.chain && !ls.overflow && round < 3;
                 if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
                 else done = true;
                 if (!__any_sync(0xffffffffu, again)) break;
+            }
+            if (!need) ls.thr = ls.blo;
+        }
+        // the witnesses of branches decided from above must be folded before
+        // their triangles: add them to the list (pinned against pruning)
+        if (active && !ls.overflow && !ls.chain) {
+            for (int j = 0; j < ls.nb; ++j) {
+                if (!((ls.resolved >> j) & 1u)) continue;
+                if (!(br.W[j][lane] > br.qhi[j][lane] + gd)) continue;
+                const uint32_t wt = br.wtri[j][lane];
+                uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
+                float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
+                bool have = false;
+                for (int q = 0; q < ls.nc && !have; ++q) have = (lt[q] == wt);
+                if (have) continue;
+                if (ls.nc == ctx.cand_cap) {
+                    ls.overflow = true;
+                    break;
+                }
+                lt[ls.nc] = wt;
+                lh[ls.nc] = 3.0e38f;
+                ++ls.nc;
             }
         }
     }
@@ -475,6 +601,34 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     if (lane == 0 && scr) atomicAdd(&ctx.counters[C_SCREENED], scr);
 }
 
+// One step of dropCutter5's fold (batchdropcutter.cpp:187-231): the overlap
+// and below tests, then MillingCutter::dropCutter on the triangle.
+__device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t tri, float cxl, float cyl,
+                                         int& capped) {
+    const Tri64& t = ctx.t64[tri];
+    if (!(overlaps64(ctx.cp.radius, cl.x, cl.y, t) && cl.z < t.bb[5])) return;
+    uint32_t fl = ctx.t32[tri].flags;
+    if (!ctx.composite_screen) {
+        // an edge whose FP32 upper bound is below the running height cannot
+        // lift it; skipping its FP64 evaluation (for the bull: two Brent
+        // solves) leaves the fold unchanged
+        const Tri32 t3 = ctx.t32[tri];
+        const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
+        const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
+        const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
+        const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
+        const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
+        for (int e = 0; e < 3; ++e) {
+            if (fl & (TF_EDGE0_SKIP << e)) continue;
+            const int k = (e + 1) % 3;
+            Iv v = edge32(ctx.prof, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E,
+                          (fl & (TF_EDGE0_HORIZ << e)) != 0);
+            if (v.hi + ctx.E < zr - ctx.guard) fl |= (TF_EDGE0_SKIP << e);
+        }
+    }
+    drop_triangle64(ctx.cp, cl, t, fl, &capped);
+}
+
 // ---------------------------------------------------------------------------
 // FP64 refinement: one thread per CL point folds its candidates in the
 // reference's visit order (ascending KD rank) against a running height, as
@@ -487,35 +641,11 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     const int n = ctx.ncand[i];
     if (n == 0xFFFF) return;  // handed to the plain path
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
-    const double R = ctx.cp.radius;
     const uint32_t* tri = ctx.cand + (size_t)i * ctx.cand_cap;  // already in KD order
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     int capped = 0;
     const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
-    for (int q = 0; q < n; ++q) {
-        const Tri64& t = ctx.t64[tri[q]];
-        if (!(overlaps64(R, x, y, t) && cl.z < t.bb[5])) continue;
-        uint32_t fl = ctx.t32[tri[q]].flags;
-        if (!ctx.composite_screen) {
-            // an edge whose FP32 upper bound is below the running height cannot
-            // lift it; skipping its FP64 evaluation (for the bull: two Brent
-            // solves) leaves the fold unchanged
-            const Tri32 t3 = ctx.t32[tri[q]];
-            const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
-            const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
-            const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
-            const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
-            const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
-            for (int e = 0; e < 3; ++e) {
-                if (fl & (TF_EDGE0_SKIP << e)) continue;
-                const int k = (e + 1) % 3;
-                Iv v = edge32(ctx.prof, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E,
-                              (fl & (TF_EDGE0_HORIZ << e)) != 0);
-                if (v.hi + ctx.E < zr - ctx.guard) fl |= (TF_EDGE0_SKIP << e);
-            }
-        }
-        drop_triangle64(ctx.cp, cl, t, fl, &capped);
-    }
+    for (int q = 0; q < n; ++q) fold_one(ctx, cl, tri[q], cxl, cyl, capped);
     const uint32_t o = ctx.perm[i];
     ctx.out_z[o] = cl.z;
     ctx.out_cc[3 * o] = cl.cc.x;
@@ -527,6 +657,142 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     if (cl.z < lb - 1e-9 * (1.0 + fabs(lb))) atomicAdd(&ctx.counters[C_VIOLATION], 1ull);
     if (n) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)n);
     if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+}
+
+// ---------------------------------------------------------------------------
+// Exact fold of one handed-back CL point per block.
+// The block gathers every triangle whose certified FP32 upper bound lies above
+// the start height (no branch threshold needed), sorts them by KD rank and
+// folds them in that order; a triangle whose upper bound is below the running
+// height cannot lift it and is passed over, so only a few reach FP64.  Points
+// with more than EXACT_CAP such triangles go on to the plain FP64 kernel.
+// ---------------------------------------------------------------------------
+constexpr int EXACT_CAP = 4096;
+constexpr int EXACT_THREADS = 256;
+constexpr size_t EXACT_SMEM = (size_t)EXACT_CAP * (8 + 4 + 4);
+
+template <bool COMP>
+__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_constant__ DropCtx ctx,
+                                                              const uint32_t* __restrict__ list,
+                                                              const unsigned long long* __restrict__ nlist_dev,
+                                                              uint32_t* __restrict__ list2,
+                                                              unsigned long long* __restrict__ nlist2) {
+    extern __shared__ unsigned long long s_key[];  // EXACT_CAP keys (KD rank << 32 | slot)
+    uint32_t* s_tri = reinterpret_cast<uint32_t*>(s_key + EXACT_CAP);
+    float* s_hi = reinterpret_cast<float*>(s_tri + EXACT_CAP);
+    __shared__ float s_hlb[HLB_N];
+    __shared__ int s_n;
+    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nlist = (int)*nlist_dev;
+    const GridP& g = ctx.g;
+    const float R = ctx.prof.R, gd = ctx.guard, Rg = R + gd, inv_step = (float)HLB_N / R;
+    const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
+    for (int p = blockIdx.x; p < nlist; p += gridDim.x) {
+        const uint32_t i = list[p];
+        const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+        const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
+        const float z0l = __double2float_rd(z0 - g.oz);
+        if (tid == 0) s_n = 0;
+        __syncthreads();
+        // gather: one thread per grid cell under the cutter, all levels
+        for (int L = g.nlev - 1; L >= 0; --L) {
+            int c0, c1, r0, r1;
+            if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
+            const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
+            const Cell* cells = ctx.cells + g.cell_off[L];
+            for (int k = tid; k < ncells; k += blockDim.x) {
+                const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
+                if (cell.count == 0) continue;
+                float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
+                float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
+                float d = sqrtf(dx * dx + dy * dy);
+                if (!(d <= Rg && cell.maxz - hlb_at(s_hlb, d - gd, inv_step) > z0l - gd)) continue;
+                for (uint32_t j = 0; j < cell.count; ++j) {
+                    const Entry e = ctx.entries[cell.start + j];
+                    float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                    float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                    float de = sqrtf(ex * ex + ey * ey);
+                    float ub = e.maxz - hlb_at(s_hlb, de - gd, inv_step);
+                    if (!(de <= Rg && ub > z0l - gd)) continue;
+                    const Tri32 t = ctx.t32[e.tri];
+                    float qt, qth;
+                    Iv v = COMP ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth)
+                                : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
+                    if (!(v.hi > NEG_INF32)) continue;
+                    const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
+                    if (!(hi > z0l - gd)) continue;
+                    const int slot = atomicAdd(&s_n, 1);
+                    if (slot < EXACT_CAP) {
+                        s_key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
+                        s_tri[slot] = (uint32_t)e.tri;
+                        s_hi[slot] = hi;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int n = s_n;
+        if (n > EXACT_CAP) {
+            if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
+            __syncthreads();
+            continue;
+        }
+        // bitonic sort of the keys (padded to a power of two)
+        int np = 1;
+        while (np < n) np <<= 1;
+        for (int k = n + tid; k < np; k += blockDim.x) s_key[k] = ~0ull;
+        __syncthreads();
+        for (int k = 2; k <= np; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int a = tid; a < np; a += blockDim.x) {
+                    const int b = a ^ j;
+                    if (b > a) {
+                        const unsigned long long ka = s_key[a], kb = s_key[b];
+                        if ((ka > kb) == ((a & k) == 0)) {
+                            s_key[a] = kb;
+                            s_key[b] = ka;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // fold in KD order (warp 0; every lane computes the same fold)
+        if (tid < 32) {
+            CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
+            int capped = 0;
+            unsigned evals = 0;
+            const float cxl = cx, cyl = cy;
+            for (int q0 = 0; q0 < n; q0 += 32) {
+                const int q = q0 + lane;
+                const uint32_t slot = q < n ? (uint32_t)s_key[q] : 0u;
+                const float h = q < n ? s_hi[slot] : NEG_INF32;
+                const uint32_t tr = q < n ? s_tri[slot] : 0u;
+                unsigned m = __ballot_sync(0xffffffffu, h + gd >= __double2float_rd(cl.z - g.oz));
+                while (m) {
+                    const int b = __ffs(m) - 1;
+                    m &= m - 1;
+                    const float hb = __shfl_sync(0xffffffffu, h, b);
+                    const uint32_t tb = __shfl_sync(0xffffffffu, tr, b);
+                    if (hb + gd < __double2float_rd(cl.z - g.oz)) continue;  // passed by the rising height
+                    fold_one(ctx, cl, tb, cxl, cyl, capped);
+                    ++evals;
+                }
+            }
+            if (lane == 0) {
+                const uint32_t o = ctx.perm[i];
+                ctx.out_z[o] = cl.z;
+                ctx.out_cc[3 * o] = cl.cc.x;
+                ctx.out_cc[3 * o + 1] = cl.cc.y;
+                ctx.out_cc[3 * o + 2] = cl.cc.z;
+                ctx.out_type[o] = cl.type;
+                if (evals) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)evals);
+                if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void k_collect_overflow(const uint16_t* ncand, int M, uint32_t* list, unsigned long long* counter) {
@@ -548,7 +814,7 @@ struct DropWork {
     DevBuf<float> cand_hi;
     DevBuf<uint16_t> ncand;
     DevBuf<float> blo;
-    DevBuf<uint32_t> list;
+    DevBuf<uint32_t> list, list2;
     DevBuf<unsigned long long> counters;
     DevBuf<uint8_t> sort_tmp;
     DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
@@ -558,7 +824,7 @@ struct DropWork {
         if (M > cap || !counters.p) {
             size_t c = std::max<size_t>(M, 1024);
             if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
-                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) ||
+                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) || !list2.alloc(c) ||
                 !counters.alloc(C_NCOUNTERS + 1))
                 return false;
             cap = c;
@@ -569,6 +835,30 @@ struct DropWork {
 };
 
 static thread_local DropWork* tl_work = nullptr;
+
+// k_drop_exact over the handed-back points (count on the device).
+static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
+                        uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(k_drop_exact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)EXACT_SMEM);
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(k_drop_exact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)EXACT_SMEM);
+    });
+    if (attr_err != cudaSuccess) {
+        set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(attr_err));
+        return OCL_GB300_DEVICE_ERROR;
+    }
+    if (blocks == 0) blocks = 1;
+    if (composite)
+        k_drop_exact<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2);
+    else
+        k_drop_exact<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2);
+    return OCL_GB300_OK;
+}
 
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats) {
@@ -583,6 +873,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     CK(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, w.keys.p, w.keys2.p, w.perm0.p, w.perm.p, (int64_t)M, 0,
                                        32, stream));
     if (!w.ensure(M, sort_bytes)) return OCL_GB300_OOM;
+    int st = OCL_GB300_OK;
 
     if (!w.host_ctx) w.host_ctx = new DropCtx();
     DropCtx* h = w.host_ctx;  // passed by value as the kernels' __grid_constant__ parameter
@@ -659,10 +950,13 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
         CK(cudaEventRecord(ev[3], stream));
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
-        // the fallback grid strides over however many points overflowed
+        // the fallback grids stride over however many points were handed back
+        st = launch_exact(*h, composite, w.list.p, w.counters.p + C_FALLBACK, w.list2.p, w.counters.p + C_PLAIN,
+                          (unsigned)std::min<uint64_t>(M, 152u * 3u), stream);
+        if (st) return st;
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
-        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list.p, w.counters.p + C_FALLBACK);
-        launches += 4;
+        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list2.p, w.counters.p + C_PLAIN);
+        launches += 5;
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[4], stream));
@@ -683,6 +977,9 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         stats->screened = c[C_SCREENED];
         stats->overflow_points = c[C_OVERFLOW];
         stats->chain_points = c[C_CHAIN];
+        stats->open_branch_points = c[C_OPEN];
+        stats->untracked_branch_points = c[C_UNTRACKED];
+        stats->plain_points = c[C_PLAIN];
         stats->launches = launches;
         stats->kernel_ms = t_all;
         stats->screen_ms = t_scr;
@@ -711,6 +1008,7 @@ struct NoAllocScratch {
     uint32_t cand[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     float cand_hi[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     uint32_t list[OCL_GB300_NOALLOC_MAX_POINTS];
+    uint32_t list2[OCL_GB300_NOALLOC_MAX_POINTS];
     float blo[OCL_GB300_NOALLOC_MAX_POINTS];
     uint16_t ncand[OCL_GB300_NOALLOC_MAX_POINTS];
     unsigned long long counters[C_NCOUNTERS + 1];
@@ -808,8 +1106,11 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
             k_drop_screen<0><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
         k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
+        st = launch_exact(h, composite, sc->list, sc->counters + C_FALLBACK, sc->list2, sc->counters + C_PLAIN,
+                          (unsigned)std::min<uint64_t>(M, 152u * 3u), stream);
+        if (st) return st;
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
-        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(h, sc->list, sc->counters + C_FALLBACK);
+        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(h, sc->list2, sc->counters + C_PLAIN);
     }
     CK(cudaGetLastError());
     return OCL_GB300_OK;

@@ -18,7 +18,10 @@ enum Counter {
     C_SCREENED = 5,   // FP32 whole-triangle screens
     C_OVERFLOW = 6,   // points handed back because their candidate list overflowed
     C_CHAIN = 7,      // points handed back because branch thresholds kept chaining
-    C_NCOUNTERS = 8
+    C_OPEN = 8,       // points collected below blo: a branch stayed undecided
+    C_UNTRACKED = 9,  // of those: more branching triangles than tracked
+    C_PLAIN = 10,     // handed-back points whose candidates exceed the exact kernel's buffer
+    C_NCOUNTERS = 11
 };
 
 struct DropCtx {

@@ -137,8 +137,19 @@ __device__ __forceinline__ Iv facet32(const Prof32& c, const Tri32& t, float wx,
 // the maximum of the concave function f(u) = z(u) - height(rho(u)) along the
 // edge line, which is what the offset-ellipse solve of bullcutter.cpp:82-105
 // finds; it is bracketed by bisection on f'.
+// State of a CC point at xy distance ~r (error er) against a radius window
+// [wlo, whi] (CompositeCutter::ccValidRadius): 1 inside, -1 outside, 0 unsure.
+__device__ __forceinline__ int window_state(float r, float er, float wlo, float whi) {
+    if (r - er >= wlo && r + er <= whi) return 1;
+    if (r + er < wlo || r - er > whi) return -1;
+    return 0;
+}
+
+// Edge contact of one cutter profile; with a window [wlo, whi] only a CC
+// point whose xy distance from the CL may lie in it counts (a composite's
+// sub-cutter: compositecutter.cpp:174-193).
 __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float bx, float by, float bz, float wx, float wy,
-                     float E, bool horiz) {
+                     float E, bool horiz, float wlo = -1.0f, float whi = 3.0e38f) {
     float dx = bx - ax, dy = by - ay;
     float L = sqrtf(dx * dx + dy * dy);
     float ux = dx / L, uy = dy / L;
@@ -200,6 +211,15 @@ __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float
             float et = (E * (2.0f + dsdd) + 1e-6f) / L;
             bool in1 = t1 > et && t1 < 1 - et, in2 = t2 > et && t2 < 1 - et;
             bool out1 = t1 < -et || t1 > 1 + et, out2 = t2 < -et || t2 > 1 + et;
+            {
+                const float ew = E * (3.0f + dsdd) + 1e-5f * c.R + 1e-6f;
+                const int w1 = window_state(sqrtf(cu_h * cu_h + dm * dm), ew, wlo, whi);
+                const int w2 = window_state(sqrtf(cu_r * cu_r + dm * dm), ew, wlo, whi);
+                in1 = in1 && w1 > 0;
+                in2 = in2 && w2 > 0;
+                out1 = out1 || w1 < 0;
+                out2 = out2 || w2 < 0;
+            }
             r.lo = (in1 && in2) ? lo : NEG_INF32;
             r.hi = (out1 && out2) ? NEG_INF32 : hi;
             if (d + E > c.R && r.lo > NEG_INF32) r.lo = NEG_INF32;
@@ -219,6 +239,7 @@ __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float
             float et = (Eu + 1e-6f) / L;
             int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
             if (d + E > c.R && st > 0) st = 0;
+            st = min(st, window_state(dm, 2.0f * E + 1e-6f, wlo, whi));
             return gate(st, az - hlo - 2.0f * E, az - hhi + 2.0f * E);
         }
         // maximise f(u) = az + (u - u1) m - h(sqrt(u^2 + d^2)) on |u| < s
@@ -247,6 +268,7 @@ __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float
     float et = (Eu + 1e-6f) / L;
     int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
     if (d + E > c.R && st > 0) st = 0;  // d <= radius is marginal
+    st = min(st, window_state(sqrtf(ccu * ccu + dm * dm), Eu + E + 1e-6f, wlo, whi));
     return gate(st, clz - err, clz + err);
 }
 
@@ -255,11 +277,14 @@ __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float
 // (dropCutter applied to a CL point already at some height Z >= z0).
 // qthr receives the lowest running height at which the reference's branch
 // choice for this triangle could change (cone tip/rim short-circuits), or
-// +inf when the triangle's effect is a plain max (order-independent).
+// +inf when the triangle's effect is a plain max (order-independent); qthr_hi
+// the highest one.  Below qthr the effect does not depend on the running
+// height Z beyond max(Z, c); above qthr_hi it is max(Z, vertex/edge contacts).
 __device__ inline Iv screen_triangle(const Prof32& c, const Tri32& t, float wx, float wy, float E, float z0_rel,
-                                     float& qthr) {
+                                     float& qthr, float& qthr_hi) {
     const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
     qthr = 3.0e38f;
+    qthr_hi = NEG_INF32;
     // vertices
     Iv best = vertex32(c, -wx, -wy, 0.0f, E);
     iv_max(best, vertex32(c, t.e1[0] - wx, t.e1[1] - wy, t.e1[2], E));
@@ -315,8 +340,14 @@ __device__ inline Iv screen_triangle(const Prof32& c, const Tri32& t, float wx, 
         r.hi = best.hi;
         if (st_tip >= 0) r.hi = fmaxf(r.hi, tip.hi);
         if (st_rim >= 0) r.hi = fmaxf(r.hi, rim.hi);
-        if (st_tip >= 0 && fmaxf(best.hi, st_rim >= 0 ? rim.hi : NEG_INF32) > tip.lo) qthr = fminf(qthr, tip.lo);
-        if (st_rim >= 0 && best.hi > rim.lo) qthr = fminf(qthr, rim.lo);
+        if (st_tip >= 0 && fmaxf(best.hi, st_rim >= 0 ? rim.hi : NEG_INF32) > tip.lo) {
+            qthr = fminf(qthr, tip.lo);
+            qthr_hi = fmaxf(qthr_hi, tip.hi);
+        }
+        if (st_rim >= 0 && best.hi > rim.lo) {
+            qthr = fminf(qthr, rim.lo);
+            qthr_hi = fmaxf(qthr_hi, rim.hi);
+        }
         return r;
     }
     // cyl/ball/bull: a lifting facet contact is the highest contact of the
@@ -333,7 +364,20 @@ struct Comp32 {
     float zoff[OCL_GB300_MAX_SUB];
     float rlim[OCL_GB300_MAX_SUB];  // radiusvec
     float R;
+    // radius window of sub-cutter n, [radiusvec[n-1] - 1e-6, radiusvec[n] + 1e-6]
+    // (the reference's doubles), rounded inward (in) and outward (out) to float
+    float wlo_in[OCL_GB300_MAX_SUB], whi_in[OCL_GB300_MAX_SUB];
+    float wlo_out[OCL_GB300_MAX_SUB], whi_out[OCL_GB300_MAX_SUB];
 };
+
+// Window state of a CC at xy distance dist (error ed) for sub-cutter n:
+// 1 certainly inside, -1 certainly outside, 0 unsure.
+__device__ __forceinline__ int comp_window(const Comp32& c, int n, float dist, float ed) {
+    const float e = ed + dist * 1.2e-7f;  // rounding of dist +- ed
+    if (dist - e >= c.wlo_in[n] && dist + e <= c.whi_in[n]) return 1;
+    if (dist + e < c.wlo_out[n] || dist - e > c.whi_out[n]) return -1;
+    return 0;
+}
 
 // composite height(r): the first sub-cutter whose radius window holds r
 __device__ __forceinline__ float hcomp32(const Comp32& c, float r) {
@@ -352,17 +396,21 @@ __device__ __forceinline__ float hcomp32(const Comp32& c, float r) {
 //   lo: the facet outcome if one facet contact certainly lifts, else the
 //       lower of (vertex contacts with the composite profile) and every facet
 //       contact that may end the triangle;
-//   hi: every contact any sub-cutter can make (facet, rim, tip, edges), with
-//       the radius windows ignored;
+//   hi: every contact of the composite profile with a vertex, and every facet
+//       or edge contact of a sub-cutter whose CC may lie in that sub-cutter's
+//       radius window (contacts outside it never lift the composite);
 //   qthr: the lowest facet contact that may end the triangle while another
 //       contact could be higher (its branch depends on the running height),
 //       and the tip of a cone sub-cutter outside the centre window (while the
 //       running height is below it the tip lifts, fails the window and hides
-//       that sub-cutter's rim).
+//       that sub-cutter's rim);
+//   qthr_hi: the highest of those contacts (above it no facet contact lifts
+//       and the effect is max(Z, vertex/edge contacts)).
 __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx, float wy, float E, float z0_rel,
-                                      float& qthr) {
+                                      float& qthr, float& qthr_hi) {
     const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
     qthr = 3.0e38f;
+    qthr_hi = NEG_INF32;
     const float px[3] = {0.0f, t.e1[0], t.e2[0]};
     const float py[3] = {0.0f, t.e1[1], t.e2[1]};
     const float pz[3] = {0.0f, t.e1[2], t.e2[2]};
@@ -377,82 +425,139 @@ __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx,
         ohi = fmaxf(ohi, pz[k] - hcomp32(c, fmaxf(qlo, 0.0f)) + E);
         if (qhi <= c.R) vlo = fmaxf(vlo, pz[k] - hcomp32(c, qhi) - E);
     }
+    // edges: a sub-cutter's edge contact counts only when its CC lies in the
+    // sub-cutter's radius window (its highest edge contact's CC is tested, so
+    // the in-window contacts bound what it can add)
     for (int n = 0; n < c.nsub; ++n) {
         const Prof32& s = c.sub[n];
         const float zo = c.zoff[n];
+        const float wlo = (n == 0 ? 0.0f : c.rlim[n - 1]) - 1e-6f, whi = c.rlim[n] + 1e-6f;
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
             if (t.flags & (TF_EDGE0_SKIP << e)) continue;
             const int k = (e + 1) % 3;
             const bool horiz = (t.flags & (TF_EDGE0_HORIZ << e)) != 0;
-            Iv v = edge32(s, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, E, horiz);
+            Iv v = edge32(s, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, E, horiz, wlo, whi);
             if (v.hi > NEG_INF32) ohi = fmaxf(ohi, v.hi - zo + E);
         }
     }
     // facet contacts of the sub-cutters, with their window/inside states
     const uint32_t mode = t.flags & TF_FACET_MASK;
-    float f_certain = NEG_INF32;  // best facet contact that certainly ends the triangle
-    float f_minlo = 3.0e38f;      // lowest facet contact that may end it
+    // Facet contacts of the sub-cutters (CompositeCutter::facetDrop,
+    // compositecutter.cpp:152-172), one slot per (sub-cutter, tip/rim):
+    //   pv    value of a contact that may lift the composite (else +inf);
+    //   f_certain: the best contact that lifts whenever it is above Z.
+    // For Z below f_certain the facet ends the triangle with the highest
+    // valid contact, whatever Z is: contacts below f_certain branch nothing.
+    constexpr int NS = 2 * OCL_GB300_MAX_SUB;
+    float pv[NS];
+    float rimv[OCL_GB300_MAX_SUB], tlo[OCL_GB300_MAX_SUB], thi[OCL_GB300_MAX_SUB];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) pv[k] = 3.0e38f;
+#pragma unroll
+    for (int k = 0; k < OCL_GB300_MAX_SUB; ++k) {
+        rimv[k] = NEG_INF32;
+        tlo[k] = 3.0e38f;
+        thi[k] = NEG_INF32;
+    }
+    float f_certain = NEG_INF32;
     float f_hi = NEG_INF32;
-    bool f_possible = false;
-    float tip_thr = 3.0e38f;
+    float ev = E * 3.0f;
     if (mode != TF_FACET_NONE) {
         const float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
         const float xyl = sqrtf(nx * nx + ny * ny);
         const float slope = (mode == TF_FACET_HORIZ) ? 0.0f : (fabsf(nx) + fabsf(ny)) / nz;
-        for (int n = 0; n < c.nsub; ++n) {
+        ev = E * (3.0f + 2.0f * slope);
+#pragma unroll
+        for (int n = 0; n < OCL_GB300_MAX_SUB; ++n) {
+            if (n >= c.nsub) break;
             const Prof32& s = c.sub[n];
             const float zo = c.zoff[n];
-            const float wlo = (n == 0 ? 0.0f : c.rlim[n - 1]) - 1e-6f, whi = c.rlim[n] + 1e-6f;
-            // up to two candidate contacts per sub-cutter: (value, cc distance, inside state)
-            float val[2], dist[2];
-            int ins[2], m = 0;
-            bool cone_tip_blocks = false;
+            // up to two candidate contacts per sub-cutter: value, window state,
+            // inside state, and whether it certainly lifts whenever it is above Z
+            float val[2] = {0.0f, 0.0f};
+            int win[2] = {-1, -1}, ins[2] = {-1, -1};
+            bool sure[2] = {true, true};
             if (s.kind == OCL_CUTTER_CONE) {
-                float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
-                int st_tip = inside32(t, wx, wy, eps_b);
+                // ConeCutter::facetDrop (conecutter.cpp:70-105): the tip, when it
+                // lifts, ends the sub-cutter's drop and hides its rim
+                const float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
+                const int st_tip = inside32(t, wx, wy, eps_b);
+                const float vt = zt - zo;
+                const bool tip_may_lift = st_tip >= 0 && vt + ev > z0_rel;
                 if (st_tip >= 0) {
-                    val[m] = zt - zo; dist[m] = 0.0f; ins[m] = st_tip; ++m;
-                    cone_tip_blocks = !(0.0f >= wlo);  // tip outside this sub-cutter's window
+                    val[0] = vt; win[0] = comp_window(c, n, 0.0f, 0.0f); ins[0] = st_tip;
                 }
                 if (mode == TF_FACET_GENERAL) {
-                    float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
-                    int st_rim = inside32(t, rx, ry, eps_b);
+                    const float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
+                    const int st_rim = inside32(t, rx, ry, eps_b);
                     if (st_rim >= 0) {
-                        val[m] = -(nx * rx + ny * ry) / nz - s.length - zo;
-                        dist[m] = s.R; ins[m] = st_rim; ++m;
+                        // the rim CC lies at xy distance R (the reference's
+                        // FP64 arithmetic, exact to ~1e-14)
+                        val[1] = -(nx * rx + ny * ry) / nz - s.length - zo;
+                        win[1] = comp_window(c, n, s.R, 1e-9f + s.R * 1e-9f);
+                        ins[1] = st_rim;
+                        sure[1] = !tip_may_lift;  // hidden while Z is below the tip
+                        // below the tip the rim is not tried: a branch at the tip
+                        if (tip_may_lift && win[1] >= 0 && val[1] + ev > z0_rel) {
+                            rimv[n] = val[1];
+                            tlo[n] = vt - ev;
+                            thi[n] = vt + ev;
+                        }
                     }
                 }
-                if (cone_tip_blocks) tip_thr = fminf(tip_thr, val[0] - E * (2.0f + slope));
             } else {
-                float ccx, ccy, tip;
+                // MillingCutter::facetDrop (millingcutter.cpp:51-75): CC at
+                // cl - (xy_normal_length * xyn + normal_length * n), whose xy
+                // distance from the CL is xy_normal_length + normal_length |n_xy|
+                float ccx, ccy, tip, dist, ed;
                 if (mode == TF_FACET_HORIZ) {
                     ccx = wx; ccy = wy; tip = 0.0f;
+                    dist = 0.0f;
+                    ed = 0.0f;
                 } else {
                     float xnx = nx / xyl, xny = ny / xyl;
                     float rvx = s.xynl * xnx + s.nl * nx, rvy = s.xynl * xny + s.nl * ny, rvz = s.nl * nz;
                     ccx = wx - rvx; ccy = wy - rvy;
                     tip = -(nx * ccx + ny * ccy) / nz + rvz - s.center_height;
+                    dist = s.xynl + s.nl * xyl;
+                    ed = s.nl * xyl * 3e-7f + 1e-9f;
                 }
                 int st = inside32(t, ccx, ccy, eps_b);
                 if (st >= 0) {
-                    float dx = ccx - wx, dy = ccy - wy;
-                    val[m] = tip - zo; dist[m] = sqrtf(dx * dx + dy * dy); ins[m] = st; ++m;
+                    val[0] = tip - zo; win[0] = comp_window(c, n, dist, ed); ins[0] = st;
                 }
             }
-            const float ev = E * (3.0f + 2.0f * slope);
-            for (int k = 0; k < m; ++k) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
                 // radius window (CompositeCutter::ccValidRadius, compositecutter.cpp:86-102)
-                int win = (dist[k] - E >= wlo && dist[k] + E <= whi) ? 1
-                          : ((dist[k] + E < wlo || dist[k] - E > whi) ? -1 : 0);
+                if (ins[k] < 0 || win[k] < 0) continue;  // never lifts the composite
                 f_hi = fmaxf(f_hi, val[k] + ev);
-                if (win < 0) continue;
-                int state = (win > 0 && ins[k] > 0) ? 1 : 0;
-                if (val[k] + ev <= z0_rel) continue;  // never lifts
-                f_possible = true;
-                f_minlo = fminf(f_minlo, val[k] - ev);
-                if (state > 0 && val[k] - ev > z0_rel) f_certain = fmaxf(f_certain, val[k] - ev);
+                if (val[k] + ev <= z0_rel) continue;  // never above the start height
+                pv[2 * n + k] = val[k];
+                if (win[k] > 0 && ins[k] > 0 && sure[k] && val[k] - ev > z0_rel)
+                    f_certain = fmaxf(f_certain, val[k] - ev);
             }
+        }
+    }
+    // branch points: the contacts that may lie above f_certain, and the tips
+    // that hide a rim which may lie above it
+    bool f_possible = false;
+    float f_minlo = 3.0e38f, f_maxhi = NEG_INF32;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        if (pv[k] < 3.0e38f && pv[k] + ev > f_certain) {
+            f_possible = true;
+            f_minlo = fminf(f_minlo, pv[k] - ev);
+            f_maxhi = fmaxf(f_maxhi, pv[k] + ev);
+        }
+    }
+    float tip_thr = 3.0e38f, tip_thr_hi = NEG_INF32;
+#pragma unroll
+    for (int k = 0; k < OCL_GB300_MAX_SUB; ++k) {
+        if (rimv[k] + ev > f_certain && tlo[k] < 3.0e38f) {
+            tip_thr = fminf(tip_thr, tlo[k]);
+            tip_thr_hi = fmaxf(tip_thr_hi, thi[k]);
         }
     }
     Iv r;
@@ -460,8 +565,14 @@ __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx,
     if (f_certain > NEG_INF32) r.lo = f_certain;
     else if (f_possible) r.lo = fminf(vlo, f_minlo);
     else r.lo = vlo;
-    if (f_possible && ohi > f_minlo) qthr = f_minlo;
-    qthr = fminf(qthr, tip_thr);
+    if (f_possible && ohi > f_minlo) {
+        qthr = f_minlo;
+        qthr_hi = f_maxhi;
+    }
+    if (tip_thr < 3.0e38f) {
+        qthr = fminf(qthr, tip_thr);
+        qthr_hi = fmaxf(qthr_hi, tip_thr_hi);
+    }
     return r;
 }
 

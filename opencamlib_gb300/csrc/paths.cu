@@ -123,6 +123,9 @@ static int drop_host(Mesh& m, const CutterP& cp, const std::vector<double>& cl, 
         acc->screened += st.screened;
         acc->overflow_points += st.overflow_points;
         acc->chain_points += st.chain_points;
+        acc->open_branch_points += st.open_branch_points;
+        acc->untracked_branch_points += st.untracked_branch_points;
+        acc->plain_points += st.plain_points;
         acc->kernel_ms += st.kernel_ms;
     }
     return OCL_GB300_OK;

@@ -1,0 +1,99 @@
+"""Handed-back CL points on the GPU.
+
+Points whose FP32 candidate list overflows are finished by the exact
+per-point kernel (every triangle that may lift the point, sorted by the
+reference's KD visit order, folded with the running-height skip), or, with
+more candidates than that kernel holds, by the plain FP64 kernel.  A flat,
+finely triangulated plate under a flat-bottomed cutter puts hundreds of
+triangles at exactly the cutter's height, so every list overflows and the CC
+point chosen among equal contacts must follow the reference's KD visit order
+(CLPoint::liftZ lifts only on a strictly higher contact).  Results must equal
+the oracle's bit for bit."""
+import math
+
+import numpy as np
+import pytest
+
+from opencamlib_gb300 import cutters as cu
+from opencamlib_gb300 import workloads as w
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ocl():
+    import opencamlib_gb300 as ocl
+    if not ocl.device_available():
+        pytest.fail("no CUDA device")
+    return ocl
+
+
+def flat_plate(n: int, size: float = 12.0) -> np.ndarray:
+    xs = np.linspace(0.0, size, n)
+    X, Y = np.meshgrid(xs, xs)
+    return w.grid_triangles(X, Y, np.zeros_like(X))
+
+
+def points(count: int, seed: int, lo: float = 1.0, hi: float = 11.0) -> np.ndarray:
+    u = w.uniform(seed, 2 * count).reshape(-1, 2)
+    return np.stack([lo + (hi - lo) * u[:, 0], lo + (hi - lo) * u[:, 1], np.full(count, -5.0)], axis=1)
+
+
+def _same(got, ref):
+    z, cc, ty = got[:3]
+    zr, ccr, tyr = ref[:3]
+    np.testing.assert_array_equal(z, zr)
+    np.testing.assert_array_equal(ty, tyr)
+    np.testing.assert_array_equal(cc, ccr)
+
+
+CASES = {
+    # 85 x 85 cells over 12 mm: ~2,800 triangles under a 6 mm cutter, ~300
+    # of them at the height of a 2 mm flat centre
+    "cyl": (86, lambda: cu.CylCutter(6.0, 20.0)),
+    "cylcone": (86, lambda: cu.CylConeCutter(2.0, 6.0, math.pi / 4)),
+    "bull": (86, lambda: cu.BullCutter(6.0, 1.0, 20.0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_exact_kernel_matches_oracle(ocl, oracle_lib, name):
+    n, make = CASES[name]
+    tris = flat_plate(n)
+    cl = points(240, 5)
+    c = make()
+    mesh = ocl.DeviceMesh(tris)
+    z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+    assert st.fallback > 0, "the plate should overflow the candidate lists"
+    assert st.plain_points == 0
+    assert st.violations == 0 and st.iter_limit_hits == 0
+    _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
+    z64, cc64, ty64, _ = mesh.drop(c, cl, precision="fp64")
+    _same((z, cc, ty), (z64, cc64, ty64))
+
+
+def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
+    # 160 x 160 cells over 12 mm: ~10,000 triangles under a 6 mm cutter,
+    # more than the exact kernel holds
+    tris = flat_plate(161)
+    cl = points(64, 6)
+    c = cu.CylCutter(6.0, 20.0)
+    mesh = ocl.DeviceMesh(tris)
+    z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+    assert st.plain_points > 0
+    assert st.violations == 0
+    _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
+
+
+def test_fallback_on_a_tilted_plate(ocl, oracle_lib):
+    # a gently tilted fine plate under a cone: ties broken by tiny height
+    # differences, candidate lists still overflow for the flat cutters
+    tris = flat_plate(86)
+    tris[:, 2::3] = 1e-7 * tris[:, 0::3] + 2e-7 * tris[:, 1::3]
+    cl = points(200, 7)
+    for c in (cu.CylCutter(6.0, 20.0), cu.ConeCutter(6.0, math.pi / 4, 20.0),
+              cu.BallConeCutter(2.0, 6.0, math.pi / 4)):
+        mesh = ocl.DeviceMesh(tris)
+        z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+        assert st.violations == 0
+        _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
