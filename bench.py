@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1024, help="CL points per cutter in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cutters", default="", help="comma list of cutters (default: all five); for profiling")
+    ap.add_argument("--block", type=int, default=0,
+                    help="only an N x N block of the raster (a small case for profiling)")
     return ap.parse_args()
 
 
@@ -110,9 +113,13 @@ def dist_setup(n):
     return 0, 1, 0, None
 
 
-def cutters():
+def cutters(names=""):
     from opencamlib_gb300 import cutters as cu
-    return list(cu.standard_cutters().items())
+    allc = list(cu.standard_cutters().items())
+    if not names:
+        return allc
+    keep = names.split(",")
+    return [(n, c) for n, c in allc if n in keep]
 
 
 def cpu_baseline(tris, cl, sample, nthreads=0):
@@ -190,9 +197,10 @@ def main():
     from opencamlib_gb300 import workloads as w
 
     tris = w.mesh_c2()
-    cl = w.raster_c2()
+    cl_full = w.raster_c2()
+    cl = cl_full[block_indices(args.block)] if args.block else cl_full
     M = cl.shape[0]
-    cuts = cutters()
+    cuts = cutters(args.cutters)
     t0 = time.time()
     mesh = ocl.DeviceMesh(tris)
     torch.cuda.synchronize()
@@ -283,7 +291,7 @@ def main():
     # per cutter, and the plain FP64 kernel's rate on the same block
     prec = {}
     fp64_rate = {}
-    pts = cl[block_indices(200)]
+    pts = cl_full[block_indices(200)]
     for name, c in cuts:
         z64, cc64, ty64, s64 = mesh.drop(c, pts, "fp64")
         zm, ccm, tym, sm = mesh.drop(c, pts, "mixed")
@@ -317,7 +325,7 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(tris, cl, args.cpu_sample)
+            cpu = cpu_baseline(tris, cl_full, args.cpu_sample)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "error": str(e)}
 
@@ -325,7 +333,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "CL-points/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "cl_points": int(M),
+        "config": {"workload": WORKLOAD if not (args.block or args.cutters) else
+                   f"subset of: {WORKLOAD} (block {args.block or 1000}, cutters {[n for n, _ in cuts]})",
+                   "triangles": int(tris.shape[0]), "cl_points": int(M),
                    "cutters": [n for n, _ in cuts], "precision": "mixed (FP32 screen, FP64 refine)",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2: mesh device data ~330 MB (FP64+FP32 records, grid) > 129 MB L2",
@@ -338,6 +348,7 @@ def main():
                            "open_branch_points": int(st.open_branch_points),
                            "untracked_branch_points": int(st.untracked_branch_points),
                            "plain_points": int(st.plain_points),
+                           "verify_failed_points": int(st.verify_failed_points),
                            "refined_per_point": st.refined / M, "screened_per_point": st.screened / M}
                        for n, st in breakdown},
         "clocks": clocks,

@@ -117,12 +117,15 @@ typedef struct ocl_gb300_stats {
     uint64_t screened;       /* FP32 whole-triangle screens */
     uint64_t overflow_points;/* of the fallback points: candidate list overflow */
     uint64_t chain_points;   /* of the fallback points: branch thresholds kept chaining */
-    uint64_t open_branch_points; /* points collected below their lower bound: a
-                                    triangle's branch (cone tip/rim, composite
-                                    facet short-circuit) stayed undecided */
-    uint64_t untracked_branch_points; /* of those: more branching triangles than tracked */
+    uint64_t open_branch_points; /* points where a triangle's branch (cone tip/rim,
+                                    composite facet short-circuit) stayed undecided
+                                    by the FP32 screen */
+    uint64_t untracked_branch_points; /* of those: collected again below their lower
+                                    bound (the branch could not be checked in FP64) */
     uint64_t plain_points;   /* of the fallback points: more candidates than the exact
                                 per-point kernel holds, done by the plain FP64 kernel */
+    uint64_t verify_failed_points; /* of the fallback points: an undecided branch,
+                                checked in FP64, lay below the collection threshold */
     uint64_t launches;       /* kernels of this library launched by the call */
     double   kernel_ms;      /* device time of the call's kernels (CUDA events) */
     double   screen_ms;      /* of which the FP32 screen kernel */
@@ -153,7 +156,7 @@ int ocl_gb300_drop_device(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter,
  * buffers in and out as in ocl_gb300_drop_device (mixed precision, same
  * results); at most OCL_GB300_NOALLOC_MAX_POINTS points per call, larger
  * calls return OCL_GB300_BAD_ARG.  Scratch is one fixed array inside the
- * library (about 4.3 MB), held by every device that loads the library until
+ * library (about 6.5 MB), held by every device that loads the library until
  * the process exits; the first call on a device looks its address up, so make
  * that first call before capturing any stream.  All calls share the array:
  * calls that overlap on the GPU (other streams, other host threads) race and

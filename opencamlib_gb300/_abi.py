@@ -52,5 +52,6 @@ class Stats(C.Structure):
     _fields_ = [("pairs", C.c_uint64), ("refined", C.c_uint64), ("iter_limit_hits", C.c_uint64),
                 ("fallback", C.c_uint64), ("violations", C.c_uint64), ("screened", C.c_uint64),
                 ("overflow_points", C.c_uint64), ("chain_points", C.c_uint64), ("open_branch_points", C.c_uint64),
-                ("untracked_branch_points", C.c_uint64), ("plain_points", C.c_uint64), ("launches", C.c_uint64), ("kernel_ms", C.c_double), ("screen_ms", C.c_double),
+                ("untracked_branch_points", C.c_uint64), ("plain_points", C.c_uint64),
+                ("verify_failed_points", C.c_uint64), ("launches", C.c_uint64), ("kernel_ms", C.c_double), ("screen_ms", C.c_double),
                 ("refine_ms", C.c_double), ("fallback_ms", C.c_double), ("total_ms", C.c_double)]

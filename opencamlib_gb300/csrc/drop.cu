@@ -259,16 +259,17 @@ __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx
 constexpr int SCREEN_WARPS = 4;
 constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 
-enum ScanPhase { PH_SINGLE = 0, PH_LOWER = 1, PH_RESOLVE = 2, PH_COLLECT = 3 };
+enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
 
 struct LaneState {
     float blo;       // certified lower bound of the final height
     float qx;        // lowest branch threshold of relevant triangles not tracked
-    float thr;       // collection threshold (PH_RESOLVE cut, PH_COLLECT keep)
+    float thr;       // PH_RESOLVE: cut; PH_COLLECT: collection threshold
     float zu;        // start height rounded up (local frame)
     int nc;
     int nb;          // tracked branching triangles
     unsigned resolved;  // bit j: branch of tracked triangle j is decided
+    unsigned pending;   // bit j: PH_RESOLVE still looks for a witness of j
     bool overflow;
     bool chain;      // a collected triangle's branch depends on uncollected ones
     float chain_thr; // lowest branch threshold among chained triangles
@@ -309,6 +310,13 @@ __device__ __forceinline__ bool is_resolved(const BranchTab& b, const LaneState&
 
 // One pass over the cells under the warp's footprint (centre rows first).
 // KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
+//   PH_SINGLE   raise blo; collect triangles whose upper bound reaches the
+//               running blo (lazily pruned); KIND 1/2: track branching ones;
+//   PH_RESOLVE  for the pending tracked triangles, the best witness W and the
+//               highest upper bound H among earlier-ranked triangles; a lane
+//               stops once every pending triangle has a witness;
+//   PH_COLLECT  collect everything reaching thr, noting branch thresholds
+//               below it that are not decided (chains).
 template <int KIND>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
                                            float cx, float cy, float z0l, double xmin, double xmax, double ymin,
@@ -333,12 +341,16 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
         const int ncol = g.ncol[L];
     for (int kr = 0; kr < nr; ++kr) {
         const int r = centre_out(kr, rc, r0, r1);
+        if (phase == PH_RESOLVE) {
+            if (ls.pending == 0) active = false;
+            if (!__any_sync(0xffffffffu, active)) return;
+        }
         for (int kc = 0; kc < ncl; ++kc) {
             const int c = centre_out(kc, cc, c0, c1);
             const Cell cell = cells[r * ncol + c];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
-            const float cut = (phase == PH_COLLECT || phase == PH_RESOLVE) ? ls.thr : ls.blo;
+            const float cut = (phase == PH_SINGLE) ? ls.blo : ls.thr;
             float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
             float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
             float d = sqrtf(dx * dx + dy * dy);
@@ -351,7 +363,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
                 for (int jj = 0; jj < nj; ++jj) {
                     const Entry e = sh.ent[wl][jj];
-                    const float cut2 = (phase == PH_COLLECT || phase == PH_RESOLVE) ? ls.thr : ls.blo;
+                    const float cut2 = (phase == PH_SINGLE) ? ls.blo : ls.thr;
                     float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
                     float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
                     float de = sqrtf(ex * ex + ey * ey);
@@ -377,12 +389,23 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                         }
                         rank = t.kd_rank;
                     }
-                    if (phase == PH_SINGLE || phase == PH_LOWER) {
-                        if (lo > ls.blo) ls.blo = lo;
+                    if (phase == PH_RESOLVE) {
+                        for (int j = 0; j < ls.nb; ++j) {
+                            if (((ls.pending >> j) & 1u) && rank < br.rank[j][lane]) {
+                                if (lo > br.W[j][lane]) {
+                                    br.W[j][lane] = lo;
+                                    br.wtri[j][lane] = e.tri;
+                                    if (lo > br.qhi[j][lane] + gd) ls.pending &= ~(1u << j);
+                                }
+                                br.H[j][lane] = fmaxf(br.H[j][lane], hi);
+                            }
+                        }
+                        continue;
                     }
-                    if (phase == PH_LOWER) {
+                    if (phase == PH_SINGLE) {
+                        if (lo > ls.blo) ls.blo = lo;
                         // track triangles that branch and may still matter
-                        if (qt < 3.0e38f && hi >= ls.blo - gd) {
+                        if (KIND != 0 && qt < 3.0e38f && hi >= ls.blo - gd) {
                             int slot = ls.nb < NBRANCH ? ls.nb : -1;
                             for (int j = 0; slot < 0 && j < NBRANCH; ++j)
                                 if (br.hi[j][lane] < ls.blo - gd) slot = j;  // no longer relevant
@@ -397,21 +420,8 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                                 if (slot == ls.nb) ++ls.nb;
                             }
                         }
-                        continue;
                     }
-                    if (phase == PH_RESOLVE) {
-                        for (int j = 0; j < ls.nb; ++j) {
-                            if (rank < br.rank[j][lane]) {
-                                if (lo > br.W[j][lane]) {
-                                    br.W[j][lane] = lo;
-                                    br.wtri[j][lane] = e.tri;
-                                }
-                                br.H[j][lane] = fmaxf(br.H[j][lane], hi);
-                            }
-                        }
-                    }
-                    // collect (PH_SINGLE: lazily pruned against the rising bound;
-                    // PH_RESOLVE: optimistically against blo)
+                    // collect (PH_SINGLE: lazily pruned against the rising bound)
                     const float keep = (phase == PH_COLLECT) ? ls.thr : ls.blo;
                     if (!(hi >= keep - gd && hi > z0l - gd) || ls.overflow) continue;
                     if (phase == PH_COLLECT && qt < ls.thr - gd && !is_resolved(br, ls, lane, e.tri)) {
@@ -422,6 +432,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     const int cap = ctx.cand_cap;
                     uint32_t* lt = ctx.cand + (size_t)ls.self * cap;
                     float* lh = ctx.cand_hi + (size_t)ls.self * cap;
+                    float* ll = ctx.cand_lo + (size_t)ls.self * cap;
                     if (ls.nc == cap) {
                         int w = 0;
                         for (int q = 0; q < cap; ++q) {
@@ -429,6 +440,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                             if (hq >= keep - gd) {
                                 lt[w] = lt[q];
                                 lh[w] = hq;
+                                ll[w] = ll[q];
                                 ++w;
                             }
                         }
@@ -437,6 +449,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     if (ls.nc < cap) {
                         lt[ls.nc] = (uint32_t)e.tri;
                         lh[ls.nc] = hi;
+                        ll[ls.nc] = lo;
                         ++ls.nc;
                     } else {
                         ls.overflow = true;
@@ -448,11 +461,14 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     }
 }
 
-// KIND 1/2 (cone, composite): the effect of a triangle on the running height
-// can depend on the height reached before it (tip/rim short-circuits).
-//   pass 1  certified lower bound blo; branching triangles that may matter;
-//   pass 2  decide each branching triangle from the triangles visited before
-//           it (BranchTab), collecting optimistically at blo;
+// Screen kernel.  KIND 0: one pass.  KIND 1/2 (cone, composite): the effect
+// of a triangle on the running height can depend on the height reached before
+// it (tip/rim short-circuits), so
+//   pass 1  blo, the list at blo, and the branching triangles that matter;
+//           a branch point below blo is decided by a witness in the list (an
+//           earlier-ranked triangle certainly above it);
+//   pass 2  (only lanes with an undecided branch) witnesses among all
+//           triangles, or every earlier-ranked triangle below the branch;
 //   then    if a branch stays open, collect again at the lowest open branch
 //           threshold, closing over the thresholds of what is collected.
 template <int KIND>
@@ -480,6 +496,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     ls.nc = 0;
     ls.nb = 0;
     ls.resolved = 0;
+    ls.pending = 0;
     ls.overflow = false;
     ls.chain = false;
     ls.chain_thr = 3.0e38f;
@@ -487,15 +504,16 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    if (KIND == 0) {
-        scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-        ls.thr = ls.blo;
-    } else {
-        scan_cells<KIND>(ctx, sh, PH_LOWER, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-        // keep the branching triangles that can still reach blo
+    scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+    ls.thr = ls.blo;
+    if (KIND != 0) {
+        uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
+        const float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
+        const float* ll = ctx.cand_lo + (size_t)i * ctx.cand_cap;
+        // keep the branching triangles that can still reach blo; those whose
+        // branch points lie at or above blo need no decision
         {
             int w = 0;
-            float cut = ls.blo;
             for (int j = 0; j < ls.nb; ++j) {
                 if (br.hi[j][lane] < ls.blo - gd) continue;
                 br.tri[w][lane] = br.tri[j][lane];
@@ -506,31 +524,74 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                 br.W[w][lane] = NEG_INF32;
                 br.H[w][lane] = ls.zu;
                 br.wtri[w][lane] = 0xFFFFFFFFu;
-                cut = fminf(cut, br.qlo[w][lane]);
+                if (br.qlo[w][lane] < ls.blo) ls.pending |= 1u << w;
+                else ls.resolved |= 1u << w;
                 ++w;
             }
             ls.nb = w;
-            ls.thr = cut;
         }
-        scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
-        float open = ls.qx;
-        for (int j = 0; j < ls.nb; ++j) {
-            const bool above = br.W[j][lane] > br.qhi[j][lane] + gd;
-            const bool below = br.H[j][lane] < br.qlo[j][lane] - gd;
-            if (above || below) ls.resolved |= 1u << j;
-            else open = fminf(open, br.qlo[j][lane]);
+        // witnesses in the list (they are folded anyway)
+        if (active && ls.pending && !ls.overflow) {
+            for (int q = 0; q < ls.nc; ++q) {
+                if (!(lh[q] >= ls.blo - gd)) continue;
+                const float lq = ll[q];
+                const uint32_t rq = ctx.t32[lt[q]].kd_rank;
+                for (int j = 0; j < ls.nb; ++j)
+                    if (((ls.pending >> j) & 1u) && rq < br.rank[j][lane] && lq > br.qhi[j][lane] + gd) {
+                        ls.pending &= ~(1u << j);
+                        ls.resolved |= 1u << j;
+                    }
+                if (!ls.pending) break;
+            }
+        }
+        if (!active || ls.overflow || ls.qx < ls.blo) ls.pending = 0;
+        if (__any_sync(0xffffffffu, ls.pending != 0)) {
+            float cut = 3.0e38f;
+            for (int j = 0; j < ls.nb; ++j)
+                if ((ls.pending >> j) & 1u) cut = fminf(cut, br.qlo[j][lane]);
+            ls.thr = cut;
+            const unsigned was = ls.pending;
+            scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, cx, cy, z0l, xmin, xmax, ymin, ymax);
+            for (int j = 0; j < ls.nb; ++j) {
+                if (!((was >> j) & 1u)) continue;
+                const bool above = br.W[j][lane] > br.qhi[j][lane] + gd;
+                const bool below = br.H[j][lane] < br.qlo[j][lane] - gd;
+                if (above || below) ls.resolved |= 1u << j;
+            }
+            ls.pending = 0;
+        }
+        // a branch still undecided: the refinement decides it exactly (FP64)
+        // for a tracked triangle, which is in the list (flagged); untracked
+        // ones lower the collection threshold instead
+        float open = 3.0e38f;
+        bool verify = false;
+        if (active && !ls.overflow) {
+            int pos[NBRANCH];
+            bool all_found = ls.qx >= ls.blo;
+            for (int j = 0; j < ls.nb; ++j) {
+                pos[j] = -1;
+                if ((ls.resolved >> j) & 1u) continue;
+                open = fminf(open, br.qlo[j][lane]);
+                for (int q = 0; q < ls.nc && pos[j] < 0; ++q)
+                    if (lt[q] == br.tri[j][lane] && lh[q] >= ls.blo - gd) pos[j] = q;
+                if (pos[j] < 0) all_found = false;
+            }
+            if (all_found && open < ls.blo) {
+                for (int j = 0; j < ls.nb; ++j)
+                    if (pos[j] >= 0) lt[pos[j]] |= CAND_VERIFY;
+                verify = true;
+                open = 3.0e38f;
+            }
+            open = fminf(open, ls.qx);
         }
         ls.thr = ls.blo;
-        bool need = open < ls.blo && !ls.overflow;
-        if (active && need) {
-            atomicAdd(&ctx.counters[C_OPEN], 1ull);
-            if (ls.qx < ls.blo) atomicAdd(&ctx.counters[C_UNTRACKED], 1ull);
-        }
+        const bool need = active && open < ls.blo && !ls.overflow;
+        if (need || (active && verify)) atomicAdd(&ctx.counters[C_OPEN], 1ull);
+        if (need) atomicAdd(&ctx.counters[C_UNTRACKED], 1ull);
         if (__any_sync(0xffffffffu, need)) {
             // collect at the lowest open threshold; if a collected triangle's
             // branch threshold lies below it, lower it and collect again
-            const float first = need ? open : 3.0e38f;  // other lanes keep their lists
-            ls.thr = first;
+            ls.thr = need ? open : 3.0e38f;
             bool done = !need;
             for (int round = 0; round < 4; ++round) {
                 const float keep_thr = ls.thr;
@@ -548,24 +609,24 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
             }
             if (!need) ls.thr = ls.blo;
         }
-        // the witnesses of branches decided from above must be folded before
-        // their triangles: add them to the list (pinned against pruning)
+        // witnesses found outside the list must be folded before their
+        // triangles: add them (pinned against pruning)
         if (active && !ls.overflow && !ls.chain) {
+            float* lhw = ctx.cand_hi + (size_t)i * ctx.cand_cap;
             for (int j = 0; j < ls.nb; ++j) {
                 if (!((ls.resolved >> j) & 1u)) continue;
-                if (!(br.W[j][lane] > br.qhi[j][lane] + gd)) continue;
                 const uint32_t wt = br.wtri[j][lane];
-                uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
-                float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
+                if (wt == 0xFFFFFFFFu || !(br.W[j][lane] > br.qhi[j][lane] + gd)) continue;
                 bool have = false;
-                for (int q = 0; q < ls.nc && !have; ++q) have = (lt[q] == wt);
+                for (int q = 0; q < ls.nc && !have; ++q)
+                    have = ((lt[q] & ~CAND_VERIFY) == wt && lhw[q] >= ls.thr - gd);
                 if (have) continue;
                 if (ls.nc == ctx.cand_cap) {
                     ls.overflow = true;
                     break;
                 }
                 lt[ls.nc] = wt;
-                lh[ls.nc] = 3.0e38f;
+                lhw[ls.nc] = 3.0e38f;
                 ++ls.nc;
             }
         }
@@ -584,9 +645,9 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
             // order the list by the reference's visit order (ascending KD rank)
             for (int a = 1; a < w; ++a) {
                 const uint32_t t = lt[a];
-                const uint32_t rk = ctx.t32[t].kd_rank;
+                const uint32_t rk = ctx.t32[t & ~CAND_VERIFY].kd_rank;
                 int b = a - 1;
-                while (b >= 0 && ctx.t32[lt[b]].kd_rank > rk) {
+                while (b >= 0 && ctx.t32[lt[b] & ~CAND_VERIFY].kd_rank > rk) {
                     lt[b + 1] = lt[b];
                     --b;
                 }
@@ -645,7 +706,23 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     int capped = 0;
     const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
-    for (int q = 0; q < n; ++q) fold_one(ctx, cl, tri[q], cxl, cyl, capped);
+    // collection threshold less the guard: triangles left out lie below it
+    const double tcut = (double)ctx.blo[i] + ctx.g.oz - (double)ctx.guard;
+    for (int q = 0; q < n; ++q) {
+        const uint32_t tq = tri[q] & ~CAND_VERIFY;
+        if ((tri[q] & CAND_VERIFY) && cl.z < tcut) {
+            // a branch the screen could not decide.  From a running height at
+            // or above the cut every fold agrees; below it, the folds agree
+            // only if the triangle's lowest branch point is not below the cut
+            const Tri64& t = ctx.t64[tq];
+            if (overlaps64(ctx.cp.radius, x, y, t) && branch_low64(ctx.cp, x, y, t, ctx.t32[tq].flags) < tcut) {
+                ctx.ncand[i] = 0xFFFF;  // the exact kernel redoes this point
+                atomicAdd(&ctx.counters[C_VFAIL], 1ull);
+                return;
+            }
+        }
+        fold_one(ctx, cl, tq, cxl, cyl, capped);
+    }
     const uint32_t o = ctx.perm[i];
     ctx.out_z[o] = cl.z;
     ctx.out_cc[3 * o] = cl.cc.x;
@@ -811,7 +888,7 @@ struct DropWork {
     DevBuf<uint32_t> keys, keys2, perm0, perm;
     DevBuf<double> cls;
     DevBuf<uint32_t> cand;
-    DevBuf<float> cand_hi;
+    DevBuf<float> cand_hi, cand_lo;
     DevBuf<uint16_t> ncand;
     DevBuf<float> blo;
     DevBuf<uint32_t> list, list2;
@@ -824,7 +901,7 @@ struct DropWork {
         if (M > cap || !counters.p) {
             size_t c = std::max<size_t>(M, 1024);
             if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
-                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) || !list2.alloc(c) ||
+                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !cand_lo.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) || !list2.alloc(c) ||
                 !counters.alloc(C_NCOUNTERS + 1))
                 return false;
             cap = c;
@@ -892,6 +969,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     h->out_type = d_type;
     h->cand = w.cand.p;
     h->cand_hi = w.cand_hi.p;
+    h->cand_lo = w.cand_lo.p;
     h->cand_cap = CAND_K;
     h->ncand = w.ncand.p;
     h->blo = w.blo.p;
@@ -980,6 +1058,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         stats->open_branch_points = c[C_OPEN];
         stats->untracked_branch_points = c[C_UNTRACKED];
         stats->plain_points = c[C_PLAIN];
+        stats->verify_failed_points = c[C_VFAIL];
         stats->launches = launches;
         stats->kernel_ms = t_all;
         stats->screen_ms = t_scr;
@@ -1007,6 +1086,7 @@ struct NoAllocScratch {
     uint32_t perm[OCL_GB300_NOALLOC_MAX_POINTS];
     uint32_t cand[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     float cand_hi[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
+    float cand_lo[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     uint32_t list[OCL_GB300_NOALLOC_MAX_POINTS];
     uint32_t list2[OCL_GB300_NOALLOC_MAX_POINTS];
     float blo[OCL_GB300_NOALLOC_MAX_POINTS];
@@ -1074,6 +1154,7 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     h.out_type = d_type;
     h.cand = sc->cand;
     h.cand_hi = sc->cand_hi;
+    h.cand_lo = sc->cand_lo;
     h.cand_cap = CAND_K_NOALLOC;
     h.ncand = sc->ncand;
     h.blo = sc->blo;

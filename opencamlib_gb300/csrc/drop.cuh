@@ -8,6 +8,7 @@ namespace oclg {
 constexpr int HLB_N = 256;   // entries of the height lower-bound table
 constexpr int CAND_K = 256;  // refinement candidates kept per CL point (drop_run)
 constexpr int CAND_K_NOALLOC = 64;  // the same for the no-allocation entry point
+constexpr uint32_t CAND_VERIFY = 0x80000000u;  // list flag: decide this triangle's branch in FP64
 
 enum Counter {
     C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)
@@ -21,7 +22,8 @@ enum Counter {
     C_OPEN = 8,       // points collected below blo: a branch stayed undecided
     C_UNTRACKED = 9,  // of those: more branching triangles than tracked
     C_PLAIN = 10,     // handed-back points whose candidates exceed the exact kernel's buffer
-    C_NCOUNTERS = 11
+    C_VFAIL = 11,     // points whose undecided branch lay below the collection threshold
+    C_NCOUNTERS = 12
 };
 
 struct DropCtx {
@@ -42,6 +44,7 @@ struct DropCtx {
     int32_t* out_type;
     uint32_t* cand;         // M x cand_cap candidate triangles (sorted by KD rank when final)
     float* cand_hi;         // M x cand_cap their FP32 upper bounds (screen only)
+    float* cand_lo;         // M x cand_cap their certified FP32 lower bounds (screen only)
     uint16_t* ncand;        // per CL: count, or 0xFFFF = handed to the plain path
     int cand_cap;           // list capacity per CL point
     float* blo;             // per CL: certified lower bound (local frame)

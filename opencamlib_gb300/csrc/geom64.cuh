@@ -438,6 +438,62 @@ __device__ inline bool comp_drop(const CutterP& c, CL64& cl, const Tri64& t, uin
     return result;
 }
 
+// Lowest running height at which the effect of triangle t on a CL point at
+// (x, y) changes form, for the cone and the composites (+inf: the effect is
+// max(Z, c) for every running height Z, or there is no facet contact).
+// Below the returned height every fold gets the same value and CC point from
+// the triangle's facet, whatever the running height is.
+//   ConeCutter::facetDrop (conecutter.cpp:70-105): the first of tip, rim that
+//   lies inside the triangle ends the drop when it lifts;
+//   CompositeCutter::facetDrop (compositecutter.cpp:152-172): the facet ends
+//   the triangle at the highest valid contact; a cone sub-cutter's rim is only
+//   tried from at or above its tip.
+__device__ inline double branch_low64(const CutterP& c, double x, double y, const Tri64& t, uint32_t flags) {
+    const double INF = 1.0e300;
+    if ((flags & TF_FACET_MASK) == TF_FACET_NONE) return INF;
+    if (c.kind == OCL_CUTTER_CONE) {
+        CL64 tmp{x, y, -INF, d3(0, 0, 0), OCL_CC_NONE};
+        return facet_drop_cone(c.b, tmp, t, flags) ? tmp.z : INF;
+    }
+    if (c.kind != OCL_CUTTER_COMPOSITE) return INF;
+    double mh = -INF;  // highest valid contact no tip can hide
+    double tipv[OCL_GB300_MAX_SUB], rimv[OCL_GB300_MAX_SUB];
+    for (int n = 0; n < c.nsub; ++n) {
+        tipv[n] = INF;
+        rimv[n] = -INF;
+        const BasicP& s = c.sub[n];
+        const double zo = c.zoffset[n];
+        const double lo = (n == 0) ? -1E-6 : c.radiusvec[n - 1] - 1E-6;
+        const double hi = c.radiusvec[n] + 1e-6;
+        CL64 tmp{x, y, -INF, d3(0, 0, 0), OCL_CC_NONE};
+        if (s.kind == OCL_CUTTER_CONE) {
+            const bool hit = facet_drop_cone(s, tmp, t, flags);
+            if (!hit) continue;
+            const double dd = xynorm(d3(tmp.x, tmp.y, tmp.z) - tmp.cc);
+            const bool valid = !(dd < lo) && !(dd > hi);
+            if (valid) mh = fmax(mh, tmp.z - zo);
+            if (tmp.type == OCL_CC_FACET_TIP) {
+                // the rim, tried only from at or above the tip
+                CL64 t2{x, y, tmp.z, d3(0, 0, 0), OCL_CC_NONE};
+                if (facet_drop_cone(s, t2, t, flags) && t2.type == OCL_CC_FACET_CYL) {
+                    const double d2 = xynorm(d3(t2.x, t2.y, t2.z) - t2.cc);
+                    if (!(d2 < lo) && !(d2 > hi)) {
+                        tipv[n] = tmp.z - zo;
+                        rimv[n] = t2.z - zo;
+                    }
+                }
+            }
+        } else if (facet_drop_base(s, tmp, t, flags)) {
+            const double dd = xynorm(d3(tmp.x, tmp.y, tmp.z) - tmp.cc);
+            if (!(dd < lo) && !(dd > hi)) mh = fmax(mh, tmp.z - zo);
+        }
+    }
+    double b = (mh > -INF) ? mh : INF;
+    for (int n = 0; n < c.nsub; ++n)
+        if (rimv[n] >= mh) b = fmin(b, tipv[n]);
+    return b;
+}
+
 // MillingCutter::dropCutter for one triangle, from cl.z; cl is updated.
 __device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped) {
     if (!(cl.z < t.bb[5])) return;

@@ -126,6 +126,7 @@ static int drop_host(Mesh& m, const CutterP& cp, const std::vector<double>& cl, 
         acc->open_branch_points += st.open_branch_points;
         acc->untracked_branch_points += st.untracked_branch_points;
         acc->plain_points += st.plain_points;
+        acc->verify_failed_points += st.verify_failed_points;
         acc->kernel_ms += st.kernel_ms;
     }
     return OCL_GB300_OK;
