@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--cutters", default="", help="comma list of cutters (default: all five); for profiling")
     ap.add_argument("--block", type=int, default=0,
                     help="only an N x N block of the raster (a small case for profiling)")
+    ap.add_argument("--block-origin", default="400,300", help="raster column,row of the block's corner")
+    ap.add_argument("--stride", type=int, default=0,
+                    help="only every S-th raster point along x and y (a small case spanning the whole mesh)")
     return ap.parse_args()
 
 
@@ -198,7 +201,10 @@ def main():
 
     tris = w.mesh_c2()
     cl_full = w.raster_c2()
-    cl = cl_full[block_indices(args.block)] if args.block else cl_full
+    bi0, bj0 = (int(v) for v in args.block_origin.split(","))
+    cl = cl_full[block_indices(args.block, bi0, bj0)] if args.block else cl_full
+    if args.stride:
+        cl = cl.reshape(1000, 1000, 3)[::args.stride, ::args.stride].reshape(-1, 3) if not args.block else cl[::args.stride]
     M = cl.shape[0]
     cuts = cutters(args.cutters)
     t0 = time.time()
@@ -333,8 +339,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "CL-points/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD if not (args.block or args.cutters) else
-                   f"subset of: {WORKLOAD} (block {args.block or 1000}, cutters {[n for n, _ in cuts]})",
+        "config": {"workload": WORKLOAD if not (args.block or args.cutters or args.stride) else
+                   f"subset of: {WORKLOAD} (block {args.block or 1000} at {args.block_origin}, stride {args.stride or 1}, "
+                   f"cutters {[n for n, _ in cuts]})",
                    "triangles": int(tris.shape[0]), "cl_points": int(M),
                    "cutters": [n for n, _ in cuts], "precision": "mixed (FP32 screen, FP64 refine)",
                    "parallelism": f"replicas x{world}",

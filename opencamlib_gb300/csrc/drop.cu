@@ -261,27 +261,24 @@ constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 
 enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
 
-struct LaneState {
-    float blo;       // certified lower bound of the final height
-    float qx;        // lowest branch threshold of relevant triangles not tracked
-    float thr;       // PH_RESOLVE: cut; PH_COLLECT: collection threshold
-    float zu;        // start height rounded up (local frame)
-    int nc;
-    int nb;          // tracked branching triangles
-    unsigned resolved;  // bit j: branch of tracked triangle j is decided
-    unsigned pending;   // bit j: PH_RESOLVE still looks for a witness of j
-    bool overflow;
-    bool chain;      // a collected triangle's branch depends on uncollected ones
-    float chain_thr; // lowest branch threshold among chained triangles
-    uint32_t self;   // this lane's point (its list slot)
-    unsigned long long screened;
-};
+// Float <-> int keys whose integer order is the float order (for atomicMax /
+// atomicMin on floats held in shared memory).
+__device__ __forceinline__ int f2o(float f) {
+    const int b = __float_as_int(f);
+    return b >= 0 ? b : b ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float o2f(int o) { return __int_as_float(o >= 0 ? o : o ^ 0x7FFFFFFF); }
+__device__ __forceinline__ unsigned f2u(float f) {
+    const unsigned b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float u2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u); }
 
-// Branching triangles of one warp's lanes ([slot][lane]): triangles whose
+// Branching triangles of one warp's points ([slot][point]): triangles whose
 // effect on the running height Z has a branch point in [qlo, qhi] (cone tip
-// and rim, composite facet short-circuits).  W/wtri: the highest certified
-// lower bound among triangles visited before it (lower KD rank) and that
-// triangle; H: the highest upper bound among them (or the start height).
+// and rim, composite facet short-circuits).  Wp: the highest certified lower
+// bound among triangles visited before it (lower KD rank), packed with that
+// triangle's id; H: the highest upper bound among them (or the start height).
 //   W > qhi: every fold reaches the triangle with Z above all branch points;
 //   H < qlo: every fold reaches it with Z below all branch points;
 // either way its branch is decided without the triangles below the bound.
@@ -291,46 +288,114 @@ struct BranchTab {
     float qlo[NBRANCH][32];
     float qhi[NBRANCH][32];
     float hi[NBRANCH][32];
-    float W[NBRANCH][32];
-    float H[NBRANCH][32];
-    uint32_t wtri[NBRANCH][32];
+    unsigned long long Wp[NBRANCH][32];
+    int H[NBRANCH][32];  // ordered key of a float
 };
+
+// Per-warp state of the 32 points, shared by the lanes that screen
+// (point, triangle) pairs on their behalf.
+struct WarpPoints {
+    float cx[32], cy[32], z0l[32], thr[32];
+    int blo[32];       // ordered key of the certified lower bound
+    int qx[32];        // ordered key: lowest threshold of untracked branching triangles
+    int chain_thr[32]; // ordered key: lowest branch threshold among chained triangles
+    int nc[32];        // candidates in the point's list
+    int nb[32];        // tracked branching triangles (may run past NBRANCH)
+    unsigned pending[32];
+    unsigned resolved[32];
+    int flags[32];     // PF_*
+    unsigned msk[32];  // entries of the current chunk the point wants screened
+    int pre[32];       // exclusive prefix of the masks' popcounts
+};
+constexpr int PF_OVERFLOW = 1, PF_CHAIN = 2;
 
 struct ScanShared {
     float hlb[HLB_N];
     Entry ent[SCREEN_WARPS][32];
     BranchTab br[SCREEN_WARPS];
+    WarpPoints pt[SCREEN_WARPS];
 };
 
-__device__ __forceinline__ bool is_resolved(const BranchTab& b, const LaneState& ls, int lane, uint32_t tri) {
-    for (int j = 0; j < ls.nb; ++j)
-        if (((ls.resolved >> j) & 1u) && b.tri[j][lane] == tri) return true;
+struct LaneState {
+    float blo;          // certified lower bound of the final height
+    float qx;           // lowest branch threshold of relevant triangles not tracked
+    float thr;          // PH_RESOLVE: cut; PH_COLLECT: collection threshold
+    float zu;           // start height rounded up (local frame)
+    int nc;
+    int nb;             // tracked branching triangles
+    unsigned resolved;  // bit j: branch of tracked triangle j is decided
+    unsigned pending;   // bit j: PH_RESOLVE still looks for a witness of j
+    bool overflow;
+    bool chain;         // a collected triangle's branch depends on uncollected ones
+    float chain_thr;    // lowest branch threshold among chained triangles
+    unsigned long long screened;
+};
+
+__device__ __forceinline__ bool is_resolved(const BranchTab& b, int nb, unsigned resolved, int p, uint32_t tri) {
+    for (int j = 0; j < nb; ++j)
+        if (((resolved >> j) & 1u) && b.tri[j][p] == tri) return true;
     return false;
 }
 
-// One pass over the cells under the warp's footprint (centre rows first).
-// KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
+// Lazy prune of point p's list against keep (its owner lane, between chunks).
+__device__ __forceinline__ int prune_list(const DropCtx& ctx, uint32_t self, int nc, float keep) {
+    const int cap = ctx.cand_cap;
+    uint32_t* lt = ctx.cand + (size_t)self * cap;
+    float* lh = ctx.cand_hi + (size_t)self * cap;
+    float* ll = ctx.cand_lo + (size_t)self * cap;
+    int w = 0;
+    for (int q = 0; q < min(nc, cap); ++q) {
+        const float hq = lh[q];
+        if (hq >= keep) {
+            lt[w] = lt[q];
+            lh[w] = hq;
+            ll[w] = ll[q];
+            ++w;
+        }
+    }
+    return w;
+}
+
+// One pass over the cells under the warp's footprint (coarse levels first,
+// centre rows first).  Per chunk of 32 grid entries every lane marks the
+// entries its own point wants screened; the marked (point, triangle) pairs are
+// then spread over all 32 lanes, and each lane applies its results to the
+// pair's point through shared memory.
 //   PH_SINGLE   raise blo; collect triangles whose upper bound reaches the
-//               running blo (lazily pruned); KIND 1/2: track branching ones;
-//   PH_RESOLVE  for the pending tracked triangles, the best witness W and the
-//               highest upper bound H among earlier-ranked triangles; a lane
+//               running blo; KIND 1/2: track branching ones;
+//   PH_RESOLVE  for the pending tracked triangles, the best witness and the
+//               highest upper bound among earlier-ranked triangles; a point
 //               stops once every pending triangle has a witness;
 //   PH_COLLECT  collect everything reaching thr, noting branch thresholds
 //               below it that are not decided (chains).
+// KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
 template <int KIND>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
-                                           float cx, float cy, float z0l, double xmin, double xmax, double ymin,
-                                           double ymax) {
+                                           uint32_t base, double xmin, double xmax, double ymin, double ymax) {
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
     BranchTab& br = sh.br[wl];
+    WarpPoints& P = sh.pt[wl];
     const GridP& g = ctx.g;
     const float R = ctx.prof.R;
     const float gd = ctx.guard;
     const float Rg = R + gd;
     const float inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    // coarse levels first: they hold the large triangles and are cheap to scan
+    const int cap = ctx.cand_cap;
+    // publish this lane's point state
+    P.blo[lane] = f2o(ls.blo);
+    P.qx[lane] = f2o(ls.qx);
+    P.chain_thr[lane] = f2o(ls.chain_thr);
+    P.thr[lane] = ls.thr;
+    P.nc[lane] = ls.nc;
+    P.nb[lane] = ls.nb;
+    P.pending[lane] = ls.pending;
+    P.resolved[lane] = ls.resolved;
+    P.flags[lane] = (ls.overflow ? PF_OVERFLOW : 0) | (ls.chain ? PF_CHAIN : 0);
+    const float cx = P.cx[lane], cy = P.cy[lane], z0l = P.z0l[lane];
+    unsigned long long screened = 0;
+    __syncwarp();
     for (int L = g.nlev - 1; L >= 0; --L) {
         int c0, c1, r0, r1;
         if (!warp_rect(g, L, xmin, xmax, ymin, ymax, reach, c0, c1, r0, r1)) continue;
@@ -342,15 +407,15 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     for (int kr = 0; kr < nr; ++kr) {
         const int r = centre_out(kr, rc, r0, r1);
         if (phase == PH_RESOLVE) {
-            if (ls.pending == 0) active = false;
-            if (!__any_sync(0xffffffffu, active)) return;
+            if (P.pending[lane] == 0) active = false;
+            if (!__any_sync(0xffffffffu, active)) goto done;
         }
         for (int kc = 0; kc < ncl; ++kc) {
             const int c = centre_out(kc, cc, c0, c1);
             const Cell cell = cells[r * ncol + c];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
-            const float cut = (phase == PH_SINGLE) ? ls.blo : ls.thr;
+            const float cut = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
             float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
             float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
             float d = sqrtf(dx * dx + dy * dy);
@@ -361,28 +426,72 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
                 if (lane < nj) sh.ent[wl][lane] = ctx.entries[cell.start + j0 + lane];
                 __syncwarp();
-                for (int jj = 0; jj < nj; ++jj) {
-                    const Entry e = sh.ent[wl][jj];
-                    const float cut2 = (phase == PH_SINGLE) ? ls.blo : ls.thr;
-                    float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
-                    float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
-                    float de = sqrtf(ex * ex + ey * ey);
-                    float ub = e.maxz - hlb_at(sh.hlb, de - gd, inv_step);
-                    bool p1 = active && de <= Rg && ub >= cut2 - gd && ub > z0l - gd;
-                    if (!__any_sync(0xffffffffu, p1)) continue;
-                    if (!p1) continue;
-                    float lo = NEG_INF32, hi = ub + gd, qt = 3.0e38f, qth = NEG_INF32;
-                    uint32_t rank = 0;
+                // 1. the entries this lane's point wants screened
+                unsigned m = 0;
+                if (pass) {
+                    const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
+                    for (int jj = 0; jj < nj; ++jj) {
+                        const Entry& e = sh.ent[wl][jj];
+                        float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                        float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                        float de = sqrtf(ex * ex + ey * ey);
+                        float ub = e.maxz - hlb_at(sh.hlb, de - gd, inv_step);
+                        if (de <= Rg && ub >= cut2 - gd && ub > z0l - gd) m |= 1u << jj;
+                    }
+                }
+                const int cnt = __popc(m);
+                // 2. room in the point's list for what this chunk may add
+                if (phase != PH_RESOLVE && cnt && P.nc[lane] + cnt > cap && !(P.flags[lane] & PF_OVERFLOW)) {
+                    const float keep = (phase == PH_COLLECT) ? ls.thr : o2f(P.blo[lane]);
+                    P.nc[lane] = prune_list(ctx, base + lane, P.nc[lane], keep - gd);
+                }
+                if (KIND != 0 && phase == PH_SINGLE && P.nb[lane] >= NBRANCH) {
+                    // drop tracked triangles that can no longer reach blo
+                    const float keep = o2f(P.blo[lane]) - gd;
+                    int w = 0;
+                    for (int j = 0; j < NBRANCH; ++j) {
+                        if (br.hi[j][lane] < keep) continue;
+                        br.tri[w][lane] = br.tri[j][lane];
+                        br.rank[w][lane] = br.rank[j][lane];
+                        br.qlo[w][lane] = br.qlo[j][lane];
+                        br.qhi[w][lane] = br.qhi[j][lane];
+                        br.hi[w][lane] = br.hi[j][lane];
+                        ++w;
+                    }
+                    P.nb[lane] = w;
+                }
+                int incl = cnt;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                if (total == 0) continue;
+                P.msk[lane] = m;
+                P.pre[lane] = incl - cnt;
+                __syncwarp();
+                // 3. screen the marked pairs, 32 at a time
+                for (int k = lane; k < total; k += 32) {
+                    int p = 0;
+#pragma unroll
+                    for (int s = 16; s > 0; s >>= 1)
+                        if (p + s < 32 && P.pre[p + s] <= k) p += s;
+                    const int jj = __fns(P.msk[p], 0, k - P.pre[p] + 1);
+                    const Entry& e = sh.ent[wl][jj];
+                    const float px = P.cx[p], py = P.cy[p], pz0 = P.z0l[p];
+                    const float ub = e.maxz;  // refined below by the screen
+                    float lo, hi, qt = 3.0e38f, qth = NEG_INF32;
+                    uint32_t rank;
                     {
                         const Tri32 t = ctx.t32[e.tri];
                         Iv v = (KIND == 2)
-                                   ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2],
+                                   ? screen_composite(ctx.comp, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
                                                       qt, qth)
-                                   : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2],
+                                   : screen_triangle(ctx.prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
                                                      qt, qth);
-                        ++ls.screened;
+                        ++screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
-                        hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, hi) : NEG_INF32;
+                        hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, ub + gd) : NEG_INF32;
                         if (qt < 3.0e38f) {
                             qt = qt + t.v0[2] - ctx.E;
                             qth = qth + t.v0[2] + ctx.E;
@@ -390,75 +499,69 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                         rank = t.kd_rank;
                     }
                     if (phase == PH_RESOLVE) {
-                        for (int j = 0; j < ls.nb; ++j) {
-                            if (((ls.pending >> j) & 1u) && rank < br.rank[j][lane]) {
-                                if (lo > br.W[j][lane]) {
-                                    br.W[j][lane] = lo;
-                                    br.wtri[j][lane] = e.tri;
-                                    if (lo > br.qhi[j][lane] + gd) ls.pending &= ~(1u << j);
-                                }
-                                br.H[j][lane] = fmaxf(br.H[j][lane], hi);
+                        const int nbp = min(P.nb[p], NBRANCH);
+                        for (int j = 0; j < nbp; ++j) {
+                            if (((P.pending[p] >> j) & 1u) && rank < br.rank[j][p]) {
+                                atomicMax(&br.Wp[j][p], ((unsigned long long)f2u(lo) << 32) | (unsigned)e.tri);
+                                atomicMax(&br.H[j][p], f2o(hi));
+                                if (lo > br.qhi[j][p] + gd) atomicAnd(&P.pending[p], ~(1u << j));
                             }
                         }
                         continue;
                     }
                     if (phase == PH_SINGLE) {
-                        if (lo > ls.blo) ls.blo = lo;
+                        if (lo > o2f(P.blo[p])) atomicMax(&P.blo[p], f2o(lo));
                         // track triangles that branch and may still matter
-                        if (KIND != 0 && qt < 3.0e38f && hi >= ls.blo - gd) {
-                            int slot = ls.nb < NBRANCH ? ls.nb : -1;
-                            for (int j = 0; slot < 0 && j < NBRANCH; ++j)
-                                if (br.hi[j][lane] < ls.blo - gd) slot = j;  // no longer relevant
-                            if (slot < 0) {
-                                ls.qx = fminf(ls.qx, qt);
+                        if (KIND != 0 && qt < 3.0e38f && hi >= o2f(P.blo[p]) - gd) {
+                            const int slot = atomicAdd(&P.nb[p], 1);
+                            if (slot < NBRANCH) {
+                                br.tri[slot][p] = e.tri;
+                                br.rank[slot][p] = rank;
+                                br.qlo[slot][p] = qt;
+                                br.qhi[slot][p] = qth;
+                                br.hi[slot][p] = hi;
                             } else {
-                                br.tri[slot][lane] = e.tri;
-                                br.rank[slot][lane] = rank;
-                                br.qlo[slot][lane] = qt;
-                                br.qhi[slot][lane] = qth;
-                                br.hi[slot][lane] = hi;
-                                if (slot == ls.nb) ++ls.nb;
+                                atomicMin(&P.qx[p], f2o(qt));
                             }
                         }
                     }
                     // collect (PH_SINGLE: lazily pruned against the rising bound)
-                    const float keep = (phase == PH_COLLECT) ? ls.thr : ls.blo;
-                    if (!(hi >= keep - gd && hi > z0l - gd) || ls.overflow) continue;
-                    if (phase == PH_COLLECT && qt < ls.thr - gd && !is_resolved(br, ls, lane, e.tri)) {
-                        ls.chain = true;
-                        ls.chain_thr = fminf(ls.chain_thr, qt);
+                    const float keep = (phase == PH_COLLECT) ? P.thr[p] : o2f(P.blo[p]);
+                    if (!(hi >= keep - gd && hi > pz0 - gd) || (P.flags[p] & PF_OVERFLOW)) continue;
+                    if (phase == PH_COLLECT && qt < P.thr[p] - gd &&
+                        !is_resolved(br, min(P.nb[p], NBRANCH), P.resolved[p], p, e.tri)) {
+                        atomicOr(&P.flags[p], PF_CHAIN);
+                        atomicMin(&P.chain_thr[p], f2o(qt));
                     }
-                    // per-point list in global memory (L1/L2 resident while the warp runs)
-                    const int cap = ctx.cand_cap;
-                    uint32_t* lt = ctx.cand + (size_t)ls.self * cap;
-                    float* lh = ctx.cand_hi + (size_t)ls.self * cap;
-                    float* ll = ctx.cand_lo + (size_t)ls.self * cap;
-                    if (ls.nc == cap) {
-                        int w = 0;
-                        for (int q = 0; q < cap; ++q) {
-                            float hq = lh[q];
-                            if (hq >= keep - gd) {
-                                lt[w] = lt[q];
-                                lh[w] = hq;
-                                ll[w] = ll[q];
-                                ++w;
-                            }
-                        }
-                        ls.nc = w;
-                    }
-                    if (ls.nc < cap) {
-                        lt[ls.nc] = (uint32_t)e.tri;
-                        lh[ls.nc] = hi;
-                        ll[ls.nc] = lo;
-                        ++ls.nc;
+                    const int slot = atomicAdd(&P.nc[p], 1);
+                    if (slot < cap) {
+                        const size_t o = (size_t)(base + p) * cap + slot;
+                        ctx.cand[o] = (uint32_t)e.tri;
+                        ctx.cand_hi[o] = hi;
+                        ctx.cand_lo[o] = lo;
                     } else {
-                        ls.overflow = true;
+                        atomicOr(&P.flags[p], PF_OVERFLOW);
                     }
                 }
+                __syncwarp();
+                if (P.nc[lane] > cap) P.nc[lane] = cap;
+                __syncwarp();
             }
         }
     }
     }
+done:
+    __syncwarp();
+    ls.blo = o2f(P.blo[lane]);
+    ls.qx = o2f(P.qx[lane]);
+    ls.chain_thr = o2f(P.chain_thr[lane]);
+    ls.nc = min(P.nc[lane], cap);
+    ls.nb = min(P.nb[lane], NBRANCH);
+    ls.pending = P.pending[lane];
+    ls.overflow = (P.flags[lane] & PF_OVERFLOW) != 0;
+    ls.chain = (P.flags[lane] & PF_CHAIN) != 0;
+    ls.screened += screened;
+    __syncwarp();
 }
 
 // Screen kernel.  KIND 0: one pass.  KIND 1/2 (cone, composite): the effect
@@ -467,10 +570,11 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
 //   pass 1  blo, the list at blo, and the branching triangles that matter;
 //           a branch point below blo is decided by a witness in the list (an
 //           earlier-ranked triangle certainly above it);
-//   pass 2  (only lanes with an undecided branch) witnesses among all
+//   pass 2  (only points with an undecided branch) witnesses among all
 //           triangles, or every earlier-ranked triangle below the branch;
-//   then    if a branch stays open, collect again at the lowest open branch
-//           threshold, closing over the thresholds of what is collected.
+//   then    a branch still undecided is checked exactly by the refinement
+//           (the triangle is flagged in the list), or, for untracked ones, the
+//           list is collected again at the lowest open branch threshold.
 template <int KIND>
 __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __grid_constant__ DropCtx ctx) {
     __shared__ ScanShared sh;
@@ -484,12 +588,14 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     const uint32_t i = (uint32_t)(active ? base + lane : base);
     const GridP& g = ctx.g;
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
-    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
-    const float z0l = __double2float_rd(z0 - g.oz);
     const float gd = ctx.guard;
     BranchTab& br = sh.br[wl];
+    WarpPoints& P = sh.pt[wl];
+    P.cx[lane] = (float)(x - g.ox);
+    P.cy[lane] = (float)(y - g.oy);
+    P.z0l[lane] = __double2float_rd(z0 - g.oz);
     LaneState ls;
-    ls.blo = z0l;
+    ls.blo = P.z0l[lane];
     ls.qx = 3.0e38f;
     ls.thr = 0.0f;
     ls.zu = __double2float_ru(z0 - g.oz);
@@ -500,11 +606,10 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     ls.overflow = false;
     ls.chain = false;
     ls.chain_thr = 3.0e38f;
-    ls.self = i;
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, cx, cy, z0l, xmin, xmax, ymin, ymax);
+    scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, xmin, xmax, ymin, ymax);
     ls.thr = ls.blo;
     if (KIND != 0) {
         uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
@@ -521,9 +626,8 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                 br.qlo[w][lane] = br.qlo[j][lane];
                 br.qhi[w][lane] = br.qhi[j][lane];
                 br.hi[w][lane] = br.hi[j][lane];
-                br.W[w][lane] = NEG_INF32;
-                br.H[w][lane] = ls.zu;
-                br.wtri[w][lane] = 0xFFFFFFFFu;
+                br.Wp[w][lane] = 0ull;  // no witness yet
+                br.H[w][lane] = f2o(ls.zu);
                 if (br.qlo[w][lane] < ls.blo) ls.pending |= 1u << w;
                 else ls.resolved |= 1u << w;
                 ++w;
@@ -551,11 +655,12 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                 if ((ls.pending >> j) & 1u) cut = fminf(cut, br.qlo[j][lane]);
             ls.thr = cut;
             const unsigned was = ls.pending;
-            scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, cx, cy, z0l, xmin, xmax, ymin, ymax);
+            scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, xmin, xmax, ymin, ymax);
             for (int j = 0; j < ls.nb; ++j) {
                 if (!((was >> j) & 1u)) continue;
-                const bool above = br.W[j][lane] > br.qhi[j][lane] + gd;
-                const bool below = br.H[j][lane] < br.qlo[j][lane] - gd;
+                const unsigned long long wp = br.Wp[j][lane];
+                const bool above = wp != 0ull && u2f((unsigned)(wp >> 32)) > br.qhi[j][lane] + gd;
+                const bool below = o2f(br.H[j][lane]) < br.qlo[j][lane] - gd;
                 if (above || below) ls.resolved |= 1u << j;
             }
             ls.pending = 0;
@@ -600,7 +705,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                     ls.chain = false;
                     ls.chain_thr = 3.0e38f;
                 }
-                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active && !done, cx, cy, z0l, xmin, xmax, ymin, ymax);
+                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, xmin, xmax, ymin, ymax);
                 ls.thr = keep_thr;
                 const bool again = !done && ls.chain && !ls.overflow && round < 3;
                 if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
@@ -615,8 +720,9 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
             float* lhw = ctx.cand_hi + (size_t)i * ctx.cand_cap;
             for (int j = 0; j < ls.nb; ++j) {
                 if (!((ls.resolved >> j) & 1u)) continue;
-                const uint32_t wt = br.wtri[j][lane];
-                if (wt == 0xFFFFFFFFu || !(br.W[j][lane] > br.qhi[j][lane] + gd)) continue;
+                const unsigned long long wp = br.Wp[j][lane];
+                if (wp == 0ull || !(u2f((unsigned)(wp >> 32)) > br.qhi[j][lane] + gd)) continue;
+                const uint32_t wt = (uint32_t)(wp & 0xFFFFFFFFull);
                 bool have = false;
                 for (int q = 0; q < ls.nc && !have; ++q)
                     have = ((lt[q] & ~CAND_VERIFY) == wt && lhw[q] >= ls.thr - gd);
@@ -664,8 +770,12 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
 
 // One step of dropCutter5's fold (batchdropcutter.cpp:187-231): the overlap
 // and below tests, then MillingCutter::dropCutter on the triangle.
+// zfloor (local frame): for the cutters whose fold is a plain maximum
+// (cyl/ball/bull: a lifting facet contact is the plane's highest contact), a
+// height the final result is certified to reach; an edge that cannot reach
+// it cannot give the result, and its FP64 evaluation is skipped.
 __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t tri, float cxl, float cyl,
-                                         int& capped) {
+                                         int& capped, float zfloor = -3.0e38f) {
     const Tri64& t = ctx.t64[tri];
     if (!(overlaps64(ctx.cp.radius, cl.x, cl.y, t) && cl.z < t.bb[5])) return;
     uint32_t fl = ctx.t32[tri].flags;
@@ -675,7 +785,7 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
         // solves) leaves the fold unchanged
         const Tri32 t3 = ctx.t32[tri];
         const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
-        const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
+        const float zr = fmaxf(__double2float_rd(cl.z - ctx.g.oz), zfloor) - t3.v0[2];
         const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
         const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
         const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
@@ -708,6 +818,7 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
     // collection threshold less the guard: triangles left out lie below it
     const double tcut = (double)ctx.blo[i] + ctx.g.oz - (double)ctx.guard;
+    const float zfloor = ctx.composite_screen || ctx.cp.kind == OCL_CUTTER_CONE ? -3.0e38f : ctx.blo[i];
     for (int q = 0; q < n; ++q) {
         const uint32_t tq = tri[q] & ~CAND_VERIFY;
         if ((tri[q] & CAND_VERIFY) && cl.z < tcut) {
@@ -721,7 +832,7 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
                 return;
             }
         }
-        fold_one(ctx, cl, tq, cxl, cyl, capped);
+        fold_one(ctx, cl, tq, cxl, cyl, capped, zfloor);
     }
     const uint32_t o = ctx.perm[i];
     ctx.out_z[o] = cl.z;
