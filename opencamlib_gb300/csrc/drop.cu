@@ -779,7 +779,27 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
     const Tri64& t = ctx.t64[tri];
     if (!(overlaps64(ctx.cp.radius, cl.x, cl.y, t) && cl.z < t.bb[5])) return;
     uint32_t fl = ctx.t32[tri].flags;
-    if (!ctx.composite_screen) {
+    uint32_t sub_skip = 0;
+    if (ctx.composite_screen) {
+        // a sub-cutter's edge contact at or below the running height cannot
+        // lift the sub-cutter's drop (its window is tested on what lifts), so
+        // edges whose FP32 upper bound lies below it are left out
+        const Tri32 t3 = ctx.t32[tri];
+        const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
+        const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
+        const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
+        const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
+        const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
+        for (int n = 0; n < ctx.comp.nsub; ++n) {
+            for (int e = 0; e < 3; ++e) {
+                if (fl & (TF_EDGE0_SKIP << e)) continue;
+                const int k = (e + 1) % 3;
+                Iv v = edge32(ctx.comp.sub[n], px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E,
+                              (fl & (TF_EDGE0_HORIZ << e)) != 0);
+                if (v.hi - ctx.comp.zoff[n] + 2.0f * ctx.E < zr - ctx.guard) sub_skip |= 1u << (3 * n + e);
+            }
+        }
+    } else {
         // an edge whose FP32 upper bound is below the running height cannot
         // lift it; skipping its FP64 evaluation (for the bull: two Brent
         // solves) leaves the fold unchanged
@@ -797,7 +817,7 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
             if (v.hi + ctx.E < zr - ctx.guard) fl |= (TF_EDGE0_SKIP << e);
         }
     }
-    drop_triangle64(ctx.cp, cl, t, fl, &capped);
+    drop_triangle64(ctx.cp, cl, t, fl, &capped, sub_skip);
 }
 
 // ---------------------------------------------------------------------------

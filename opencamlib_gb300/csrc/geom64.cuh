@@ -415,8 +415,10 @@ __device__ __forceinline__ bool facet_drop_sub(const BasicP& c, CL64& cl, const 
     return c.kind == OCL_CUTTER_CONE ? facet_drop_cone(c, cl, t, flags) : facet_drop_base(c, cl, t, flags);
 }
 
-// CompositeCutter::facetDrop / edgeDrop (compositecutter.cpp:152-193)
-__device__ inline bool comp_drop(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, bool facet, int* capped) {
+// CompositeCutter::facetDrop / edgeDrop (compositecutter.cpp:152-193).
+// sub_skip bit 3n+e: edge e of sub-cutter n cannot lift it (left out).
+__device__ inline bool comp_drop(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, bool facet, int* capped,
+                                 uint32_t sub_skip = 0) {
     bool result = false;
     for (int n = 0; n < c.nsub; ++n) {
         CL64 tmp;
@@ -425,7 +427,8 @@ __device__ inline bool comp_drop(const CutterP& c, CL64& cl, const Tri64& t, uin
         tmp.z = cl.z + c.zoffset[n];
         tmp.cc = d3(0, 0, 0);
         tmp.type = OCL_CC_NONE;
-        bool hit = facet ? facet_drop_sub(c.sub[n], tmp, t, flags) : edge_drop_basic(c.sub[n], tmp, t, flags, capped);
+        bool hit = facet ? facet_drop_sub(c.sub[n], tmp, t, flags)
+                         : edge_drop_basic(c.sub[n], tmp, t, flags | (((sub_skip >> (3 * n)) & 7u) << 2), capped);
         if (hit && tmp.type != OCL_CC_NONE) {
             double dd = xynorm(d3(tmp.x, tmp.y, tmp.z) - tmp.cc);
             double lo = (n == 0) ? -1E-6 : c.radiusvec[n - 1] - 1E-6;
@@ -495,7 +498,8 @@ __device__ inline double branch_low64(const CutterP& c, double x, double y, cons
 }
 
 // MillingCutter::dropCutter for one triangle, from cl.z; cl is updated.
-__device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped) {
+__device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped,
+                                       uint32_t sub_skip = 0) {
     if (!(cl.z < t.bb[5])) return;
     bool facet;
     if (c.kind == OCL_CUTTER_COMPOSITE) facet = comp_drop(c, cl, t, flags, true, capped);
@@ -508,7 +512,7 @@ __device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& 
         if (q <= c.radius) liftz(cl, p.z - height_any(c, q), p, OCL_CC_VERTEX);
     }
     if (!(cl.z < t.bb[5])) return;
-    if (c.kind == OCL_CUTTER_COMPOSITE) comp_drop(c, cl, t, flags, false, capped);
+    if (c.kind == OCL_CUTTER_COMPOSITE) comp_drop(c, cl, t, flags, false, capped, sub_skip);
     else edge_drop_basic(c.b, cl, t, flags, capped);
 }
 
