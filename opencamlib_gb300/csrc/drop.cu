@@ -258,6 +258,11 @@ __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx
 // ---------------------------------------------------------------------------
 constexpr int SCREEN_WARPS = 4;
 constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
+// resident screen blocks per SM the register allocation aims at (measured:
+// more warps hide the FP32 dependency chains until spills start to cost)
+constexpr int screen_min_blocks(int kind, int ck) {
+    return kind == 2 ? 5 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
+}
 
 enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
 
@@ -368,8 +373,9 @@ __device__ __forceinline__ int prune_list(const DropCtx& ctx, uint32_t self, int
 //               stops once every pending triangle has a witness;
 //   PH_COLLECT  collect everything reaching thr, noting branch thresholds
 //               below it that are not decided (chains).
-// KIND: 0 cyl/ball/bull, 1 cone, 2 composite.
-template <int KIND>
+// KIND: 0 cyl/ball/bull, 1 cone, 2 composite; CK: the cutter kind for KIND
+// 0/1 (a compile-time constant, so each kernel carries one contact model).
+template <int KIND, int CK>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
                                            uint32_t base, double xmin, double xmax, double ymin, double ymax) {
     const int lane = threadIdx.x & 31;
@@ -383,6 +389,8 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     const float inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
     const int cap = ctx.cand_cap;
+    Prof32 prof = ctx.prof;
+    prof.kind = CK;
     // publish this lane's point state
     P.blo[lane] = f2o(ls.blo);
     P.qx[lane] = f2o(ls.qx);
@@ -487,7 +495,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                         Iv v = (KIND == 2)
                                    ? screen_composite(ctx.comp, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
                                                       qt, qth)
-                                   : screen_triangle(ctx.prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
+                                   : screen_triangle(prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
                                                      qt, qth);
                         ++screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
@@ -575,8 +583,9 @@ done:
 //   then    a branch still undecided is checked exactly by the refinement
 //           (the triangle is flagged in the list), or, for untracked ones, the
 //           list is collected again at the lowest open branch threshold.
-template <int KIND>
-__global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __grid_constant__ DropCtx ctx) {
+template <int KIND, int CK>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
+    k_drop_screen(const __grid_constant__ DropCtx ctx) {
     __shared__ ScanShared sh;
     for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
     __syncthreads();
@@ -609,7 +618,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    scan_cells<KIND>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, xmin, xmax, ymin, ymax);
+    scan_cells<KIND, CK>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, xmin, xmax, ymin, ymax);
     ls.thr = ls.blo;
     if (KIND != 0) {
         uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
@@ -655,7 +664,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                 if ((ls.pending >> j) & 1u) cut = fminf(cut, br.qlo[j][lane]);
             ls.thr = cut;
             const unsigned was = ls.pending;
-            scan_cells<KIND>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, xmin, xmax, ymin, ymax);
+            scan_cells<KIND, CK>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, xmin, xmax, ymin, ymax);
             for (int j = 0; j < ls.nb; ++j) {
                 if (!((was >> j) & 1u)) continue;
                 const unsigned long long wp = br.Wp[j][lane];
@@ -705,7 +714,7 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, 4) k_drop_screen(const __gr
                     ls.chain = false;
                     ls.chain_thr = 3.0e38f;
                 }
-                scan_cells<KIND>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, xmin, xmax, ymin, ymax);
+                scan_cells<KIND, CK>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, xmin, xmax, ymin, ymax);
                 ls.thr = keep_thr;
                 const bool again = !done && ls.chain && !ls.overflow && round < 3;
                 if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
@@ -1044,6 +1053,20 @@ struct DropWork {
 
 static thread_local DropWork* tl_work = nullptr;
 
+static void launch_screen(const DropCtx& h, const CutterP& cp, unsigned blocks, cudaStream_t stream) {
+    const dim3 tb(SCREEN_WARPS * 32);
+    if (cp.kind == OCL_CUTTER_COMPOSITE)
+        k_drop_screen<2, -1><<<blocks, tb, 0, stream>>>(h);
+    else if (cp.kind == OCL_CUTTER_CONE)
+        k_drop_screen<1, OCL_CUTTER_CONE><<<blocks, tb, 0, stream>>>(h);
+    else if (cp.b.kind == OCL_CUTTER_CYL)
+        k_drop_screen<0, OCL_CUTTER_CYL><<<blocks, tb, 0, stream>>>(h);
+    else if (cp.b.kind == OCL_CUTTER_BALL)
+        k_drop_screen<0, OCL_CUTTER_BALL><<<blocks, tb, 0, stream>>>(h);
+    else
+        k_drop_screen<0, OCL_CUTTER_BULL><<<blocks, tb, 0, stream>>>(h);
+}
+
 // k_drop_exact over the handed-back points (count on the device).
 static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
                         uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
@@ -1149,12 +1172,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         launches += 1;
     } else {
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
-        if (cp.kind == OCL_CUTTER_COMPOSITE)
-            k_drop_screen<2><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
-        else if (cp.kind == OCL_CUTTER_CONE)
-            k_drop_screen<1><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
-        else
-            k_drop_screen<0><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(*h);
+        launch_screen(*h, cp, sblocks, stream);
         CK(cudaEventRecord(ev[2], stream));
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
         CK(cudaEventRecord(ev[3], stream));
@@ -1310,12 +1328,7 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
     } else {
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
-        if (cp.kind == OCL_CUTTER_COMPOSITE)
-            k_drop_screen<2><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
-        else if (cp.kind == OCL_CUTTER_CONE)
-            k_drop_screen<1><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
-        else
-            k_drop_screen<0><<<sblocks, SCREEN_WARPS * 32, 0, stream>>>(h);
+        launch_screen(h, cp, sblocks, stream);
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
         k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
         st = launch_exact(h, composite, sc->list, sc->counters + C_FALLBACK, sc->list2, sc->counters + C_PLAIN,
