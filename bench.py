@@ -248,6 +248,10 @@ def main():
         dist.barrier()
     step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
+    # per-stage device times of the timed calls (CUDA events the library
+    # records on the launching stream; read after the timed region)
+    from opencamlib_gb300 import _native
+    stage = _native.stage_times(len(cuts) * args.steps)
     if dist:
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -308,17 +312,24 @@ def main():
                            "speedup": s64.kernel_ms / max(sm.kernel_ms, 1e-9), "points": int(len(pts)),
                            "exact_pairs": int(s64.pairs)}
 
-    # dominant kernel and roofline (algorithmic bytes: N*72 mesh + M*(24 in + 36 out))
-    agg = {"screen": 0.0, "refine": 0.0, "fallback": 0.0}
+    # dominant kernel and roofline (algorithmic bytes: N*72 mesh + M*(24 in + 36 out)),
+    # from the timed region's stage events
+    agg = {"screen": float(stage[:, 0].sum()) / args.steps, "refine": float(stage[:, 1].sum()) / args.steps,
+           "fallback": float(stage[:, 2].sum()) / args.steps}
     launches = 0
     for name, st in breakdown:
-        agg["screen"] += st.screen_ms
-        agg["refine"] += st.refine_ms
-        agg["fallback"] += st.fallback_ms
         launches += int(st.launches)
     dom = max(agg, key=agg.get)
-    per_launch_ms = agg[dom] / len(breakdown)
+    per_launch_ms = float(stage[:, ("screen", "refine", "fallback").index(dom)].mean())
     alg_bytes = tris.shape[0] * 72 + M * (24 + 36)
+    traffic = None
+    if dom == "screen" and not (args.block or args.cutters or args.stride):
+        try:  # DRAM bytes per screen launch from the committed ncu capture
+            for ln in open(os.path.join(ROOT, "profiles", "k_drop_screen_dram_full_size.md")):
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    traffic = int(ln.split(":")[1])
+        except OSError:
+            traffic = None
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -363,9 +374,12 @@ def main():
                 "d2h_bytes_per_step": len(cuts) * M * (8 + 24 + 4)},
         "gpu_launches": launches * args.steps,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
-                     "note": "algorithmic bytes N*72 + M*60 per launch; the kernel is FP32/FP64 issue-bound, "
-                             "not HBM-bound (peak of measured copy bandwidth)"},
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                     "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_bytes,
+                     "note": "algorithmic bytes N*72 + M*60 per launch over the mean launch time of the dominant "
+                             "stage in the timed region; the kernel is FP32-issue and latency bound, not HBM-bound "
+                             "(traffic: ncu DRAM bytes per launch of the full-size workload)"},
         "kernel_ms_per_step": agg,
         "precision": prec,
         "fp64_block": fp64_rate,

@@ -205,6 +205,13 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
                                  uint64_t* count, ocl_gb300_stats* stats);
 
 /* ---- misc ----------------------------------------------------------------- */
+/* Device time of the stages of the calling thread's last `count` (<= 256)
+ * ocl_gb300_drop / _drop_device calls, oldest first: out[4k..4k+3] = FP32
+ * screen, FP64 refinement, handed-back points, whole call (ms, CUDA events
+ * recorded on the call's stream).  Waits for those calls to finish; it does
+ * not synchronise the calls themselves, so a timed loop can read it after.
+ * No counterpart in the reference (instrumentation). */
+int ocl_gb300_stage_times(uint64_t count, double* out);
 const char* ocl_gb300_last_error(void);
 const char* ocl_gb300_version(void);
 /* 1 if a CUDA device is usable, else 0 (no compute). */

@@ -24,7 +24,8 @@ _u64p = C.POINTER(C.c_uint64)
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
-    "ocl_gb300_adaptive_path_drop", "ocl_gb300_last_error", "ocl_gb300_version", "ocl_gb300_device_available",
+    "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_last_error", "ocl_gb300_version",
+    "ocl_gb300_device_available",
 ]
 
 _lib = None
@@ -60,6 +61,7 @@ def lib():
                                       C.c_uint64, _u64p, st]
     L.ocl_gb300_adaptive_path_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, C.c_double, C.c_double,
                                                _dp, _dp, _ip, C.c_uint64, _u64p, st]
+    L.ocl_gb300_stage_times.argtypes = [C.c_uint64, _dp]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -69,6 +71,14 @@ def lib():
 def check(status):
     if status != 0:
         raise OclError(status, lib().ocl_gb300_last_error().decode())
+
+
+def stage_times(count: int) -> np.ndarray:
+    """(count, 4) ms of screen / refine / handed-back / whole call for this
+    thread's last `count` drop calls (CUDA events on each call's stream)."""
+    out = np.zeros(4 * max(count, 1))
+    check(lib().ocl_gb300_stage_times(count, _p(out)))
+    return out[:4 * count].reshape(count, 4)
 
 
 def device_available() -> bool:

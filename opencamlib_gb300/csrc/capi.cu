@@ -180,6 +180,14 @@ struct ocl_gb300_mesh_s {
 
 extern "C" {
 
+int ocl_gb300_stage_times(uint64_t count, double* out) {
+    if (count && !out) {
+        set_error("stage times: null output");
+        return OCL_GB300_BAD_ARG;
+    }
+    return drop_stage_times(count, out);
+}
+
 const char* ocl_gb300_last_error(void) { return tl_error.c_str(); }
 const char* ocl_gb300_version(void) { return "opencamlib_gb300 0.1 (sm_103a)"; }
 

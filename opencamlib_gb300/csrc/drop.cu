@@ -1035,7 +1035,12 @@ struct DropWork {
     DevBuf<unsigned long long> counters;
     DevBuf<uint8_t> sort_tmp;
     DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
-    cudaEvent_t events[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // per-call stage events, a ring over the last STAGE_RING calls (read
+    // afterwards by ocl_gb300_stage_times without syncing the calls)
+    static constexpr int STAGE_RING = 256;
+    cudaEvent_t ring[STAGE_RING][5] = {};
+    int ring_pos = 0;
+    uint64_t ring_count = 0;
     size_t cap = 0;
     bool ensure(size_t M, size_t sort_bytes) {
         if (M > cap || !counters.p) {
@@ -1139,10 +1144,12 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     h->E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
     h->guard = 4.0f * h->E + 1e-5f * (float)cp.radius;
 
-    if (!w.events[0]) {
-        for (int k = 0; k < 5; ++k) CK(cudaEventCreate(&w.events[k]));
+    cudaEvent_t* ev = w.ring[w.ring_pos];
+    if (!ev[0]) {
+        for (int k = 0; k < 5; ++k) CK(cudaEventCreate(&ev[k]));
     }
-    cudaEvent_t* ev = w.events;
+    w.ring_pos = (w.ring_pos + 1) % DropWork::STAGE_RING;
+    ++w.ring_count;
     uint64_t launches = 0;
     CK(cudaEventRecord(ev[0], stream));
     CK(cudaMemsetAsync(w.counters.p, 0, (C_NCOUNTERS + 1) * sizeof(unsigned long long), stream));
@@ -1217,6 +1224,31 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     return OCL_GB300_OK;
 }
 
+
+int drop_stage_times(uint64_t count, double* out) {
+    if (!tl_work) return count == 0 ? OCL_GB300_OK : OCL_GB300_BAD_ARG;
+    DropWork& w = *tl_work;
+    if (count > w.ring_count || count > (uint64_t)DropWork::STAGE_RING) {
+        set_error("stage times: fewer recorded calls than requested");
+        return OCL_GB300_BAD_ARG;
+    }
+    for (uint64_t k = 0; k < count; ++k) {
+        const int slot = (int)((w.ring_pos - (int64_t)count + (int64_t)k + 4 * DropWork::STAGE_RING) %
+                               DropWork::STAGE_RING);
+        cudaEvent_t* ev = w.ring[slot];
+        CK(cudaEventSynchronize(ev[4]));
+        float t_all = 0, t_scr = 0, t_ref = 0, t_fb = 0;
+        CK(cudaEventElapsedTime(&t_all, ev[0], ev[4]));
+        CK(cudaEventElapsedTime(&t_scr, ev[1], ev[2]));
+        CK(cudaEventElapsedTime(&t_ref, ev[2], ev[3]));
+        CK(cudaEventElapsedTime(&t_fb, ev[3], ev[4]));
+        out[4 * k] = t_scr;
+        out[4 * k + 1] = t_ref;
+        out[4 * k + 2] = t_fb;
+        out[4 * k + 3] = t_all;
+    }
+    return OCL_GB300_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Drop without any device allocation (ocl_gb300_drop_device_noalloc).

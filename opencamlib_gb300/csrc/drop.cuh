@@ -60,6 +60,10 @@ struct DropWork;
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats);
 
+// Stage times (screen, refine, fallback, total; ms) of this thread's last
+// count drop calls, oldest first.
+int drop_stage_times(uint64_t count, double* out);
+
 int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, double* d_z, double* d_cc,
                      int32_t* d_type, cudaStream_t stream);
 
