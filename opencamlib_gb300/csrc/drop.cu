@@ -830,6 +830,133 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
 }
 
 // ---------------------------------------------------------------------------
+// Bull edges ahead of the fold.  The bull's FP64 edge contact (offset-ellipse
+// Brent search) does not depend on the running height, so the edges a fold
+// may need are listed per CL point (k_bull_plan: every edge of a listed
+// triangle whose FP32 bound reaches the point's certified floor), evaluated
+// one edge per thread (k_bull_eval: whole warps run the same search), and the
+// fold reads the results in its own order.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float bull_edge_hi(const DropCtx& ctx, const Tri32& t3, int e, float wx, float wy) {
+    const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
+    const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
+    const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
+    const int k = (e + 1) % 3;
+    return edge32(ctx.prof, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E, false).hi;
+}
+
+__global__ void __launch_bounds__(128) k_bull_plan(const __grid_constant__ DropCtx ctx, uint2* __restrict__ queue,
+                                                  unsigned long long* __restrict__ qcount) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int cnt = 0;
+    if (i < (uint32_t)ctx.M) {
+        const int n = ctx.ncand[i];
+        if (n != 0xFFFF) {
+            const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1];
+            const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
+            const float zfloor = ctx.blo[i];
+            const uint32_t* tri = ctx.cand + (size_t)i * ctx.cand_cap;
+            for (int q = 0; q < n; ++q) {
+                const uint32_t tq = tri[q] & ~CAND_VERIFY;
+                if (!overlaps64(ctx.cp.radius, x, y, ctx.t64[tq])) continue;
+                const Tri32 t3 = ctx.t32[tq];
+                const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1], zf = zfloor - t3.v0[2];
+                for (int e = 0; e < 3; ++e) {
+                    if (t3.flags & ((TF_EDGE0_SKIP | TF_EDGE0_HORIZ) << e)) continue;
+                    if (bull_edge_hi(ctx, t3, e, wx, wy) + ctx.E < zf - ctx.guard) continue;
+                    if (cnt < EDGE_SLOTS) ctx.edge_slots[(size_t)i * EDGE_SLOTS + cnt] = (tq << 2) | (uint32_t)e;
+                    ++cnt;
+                }
+            }
+        }
+        ctx.edge_n[i] = (uint8_t)min(cnt, 255);
+    }
+    // one queue reservation per warp
+    const int mine = min(cnt, EDGE_SLOTS);
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(qcount, (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    for (int k = 0; k < mine; ++k) queue[base + incl - mine + k] = make_uint2(i, (uint32_t)k);
+}
+
+__global__ void __launch_bounds__(128) k_bull_eval(const __grid_constant__ DropCtx ctx, const uint2* __restrict__ queue,
+                                                  const unsigned long long* __restrict__ qcount) {
+    const unsigned long long nq = *qcount;
+    int capped = 0;
+    for (unsigned long long w = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; w < nq;
+         w += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 it = queue[w];
+        const uint32_t s = ctx.edge_slots[(size_t)it.x * EDGE_SLOTS + it.y];
+        const Tri64& t = ctx.t64[s >> 2];
+        const int e = (int)(s & 3u);
+        double clz = 0.0;
+        D3 cc = d3(0, 0, 0);
+        const bool ok = edge_contact64(ctx.cp.b, ctx.cl[3 * it.x], ctx.cl[3 * it.x + 1], tri_p(t, e),
+                                       tri_p(t, (e + 1) % 3), clz, cc, &capped);
+        EdgeRes r;
+        r.clz = clz;
+        r.ccx = cc.x;
+        r.ccy = cc.y;
+        r.ccz = cc.z;
+        r.valid = ok ? 1 : 0;
+        r.pad = 0;
+        ctx.edge_res[(size_t)it.x * EDGE_SLOTS + it.y] = r;
+    }
+    if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+}
+
+// MillingCutter::dropCutter for a bull, edges from k_bull_eval where planned
+// (the plan test is repeated here to walk the point's slots in step).
+__device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t i, uint32_t tq, float cxl, float cyl,
+                                          float zfloor, int& slot, int nplan, int& capped) {
+    const Tri64& t = ctx.t64[tq];
+    if (!overlaps64(ctx.cp.radius, cl.x, cl.y, t)) return;
+    const Tri32 t3 = ctx.t32[tq];
+    const uint32_t fl = t3.flags;
+    const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
+    const float zf = zfloor - t3.v0[2];
+    float hi[3];
+    int k_of[3] = {-1, -1, -1};
+    for (int e = 0; e < 3; ++e) {
+        hi[e] = NEG_INF32;
+        if (fl & ((TF_EDGE0_SKIP | TF_EDGE0_HORIZ) << e)) continue;
+        hi[e] = bull_edge_hi(ctx, t3, e, wx, wy);
+        if (hi[e] + ctx.E < zf - ctx.guard) continue;
+        k_of[e] = slot++;
+    }
+    const BasicP& b = ctx.cp.b;
+    if (!(cl.z < t.bb[5])) return;
+    if (facet_drop_base(b, cl, t, fl)) return;
+    for (int k = 0; k < 3; ++k) {
+        const D3 p = tri_p(t, k);
+        const double q = xynorm(d3(cl.x, cl.y, cl.z) - p);
+        if (q <= b.radius) liftz(cl, p.z - height_basic(b, q), p, OCL_CC_VERTEX);
+    }
+    if (!(cl.z < t.bb[5])) return;
+    const float zr = fmaxf(__double2float_rd(cl.z - ctx.g.oz), zfloor) - t3.v0[2];
+    for (int e = 0; e < 3; ++e) {
+        if (fl & (TF_EDGE0_SKIP << e)) continue;
+        const bool horiz = (fl & (TF_EDGE0_HORIZ << e)) != 0;
+        if (!horiz && hi[e] + ctx.E < zr - ctx.guard) continue;  // cannot lift
+        double clz;
+        D3 cc;
+        if (!horiz && k_of[e] >= 0 && k_of[e] < EDGE_SLOTS && k_of[e] < nplan) {
+            const EdgeRes r = ctx.edge_res[(size_t)i * EDGE_SLOTS + k_of[e]];
+            if (r.valid) liftz(cl, r.clz, d3(r.ccx, r.ccy, r.ccz), OCL_CC_EDGE);
+        } else if (edge_contact64(b, cl.x, cl.y, tri_p(t, e), tri_p(t, (e + 1) % 3), clz, cc, &capped)) {
+            liftz(cl, clz, cc, OCL_CC_EDGE);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 refinement: one thread per CL point folds its candidates in the
 // reference's visit order (ascending KD rank) against a running height, as
 // dropCutter5 does over its KD candidates.  Triangles left out can neither
@@ -848,8 +975,14 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     // collection threshold less the guard: triangles left out lie below it
     const double tcut = (double)ctx.blo[i] + ctx.g.oz - (double)ctx.guard;
     const float zfloor = ctx.composite_screen || ctx.cp.kind == OCL_CUTTER_CONE ? -3.0e38f : ctx.blo[i];
+    int slot = 0;
+    const int nplan = ctx.edge_res ? ctx.edge_n[i] : 0;
     for (int q = 0; q < n; ++q) {
         const uint32_t tq = tri[q] & ~CAND_VERIFY;
+        if (ctx.edge_res) {
+            fold_bull(ctx, cl, i, tq, cxl, cyl, zfloor, slot, nplan, capped);
+            continue;
+        }
         if ((tri[q] & CAND_VERIFY) && cl.z < tcut) {
             // a branch the screen could not decide.  From a running height at
             // or above the cut every fold agrees; below it, the folds agree
@@ -1033,6 +1166,21 @@ struct DropWork {
     DevBuf<float> blo;
     DevBuf<uint32_t> list, list2;
     DevBuf<unsigned long long> counters;
+    // bull edges ahead of the fold (allocated on first use)
+    DevBuf<uint32_t> edge_slots;
+    DevBuf<uint8_t> edge_n;
+    DevBuf<EdgeRes> edge_res;
+    DevBuf<uint2> edge_queue;
+    size_t edge_cap = 0;
+    bool ensure_edges(size_t M) {
+        if (M <= edge_cap) return true;
+        const size_t c = std::max<size_t>(M, 1024);
+        if (!edge_slots.alloc(c * EDGE_SLOTS) || !edge_n.alloc(c) || !edge_res.alloc(c * EDGE_SLOTS) ||
+            !edge_queue.alloc(c * EDGE_SLOTS))
+            return false;
+        edge_cap = c;
+        return true;
+    }
     DevBuf<uint8_t> sort_tmp;
     DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
     // per-call stage events, a ring over the last STAGE_RING calls (read
@@ -1181,6 +1329,16 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
         launch_screen(*h, cp, sblocks, stream);
         CK(cudaEventRecord(ev[2], stream));
+        if (cp.kind == OCL_CUTTER_BULL && m.n < (1ull << 30)) {
+            if (!w.ensure_edges(M)) return OCL_GB300_OOM;
+            h->edge_slots = w.edge_slots.p;
+            h->edge_n = w.edge_n.p;
+            h->edge_res = w.edge_res.p;
+            k_bull_plan<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h, w.edge_queue.p, w.counters.p + C_EDGEQ);
+            const unsigned eb = (unsigned)std::min<uint64_t>((M * EDGE_SLOTS + 127) / 128, 152u * 16u);
+            k_bull_eval<<<eb, 128, 0, stream>>>(*h, w.edge_queue.p, w.counters.p + C_EDGEQ);
+            launches += 2;
+        }
         k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
         CK(cudaEventRecord(ev[3], stream));
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);

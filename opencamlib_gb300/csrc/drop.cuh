@@ -9,6 +9,13 @@ constexpr int HLB_N = 256;   // entries of the height lower-bound table
 constexpr int CAND_K = 256;  // refinement candidates kept per CL point (drop_run)
 constexpr int CAND_K_NOALLOC = 64;  // the same for the no-allocation entry point
 constexpr uint32_t CAND_VERIFY = 0x80000000u;  // list flag: decide this triangle's branch in FP64
+constexpr int EDGE_SLOTS = 8;  // bull edge contacts evaluated ahead of the fold, per CL point
+
+struct EdgeRes {  // one edge contact (MillingCutter::singleEdgeDrop), running-height independent
+    double clz, ccx, ccy, ccz;
+    int valid;
+    int pad;
+};
 
 enum Counter {
     C_PAIRS = 0,      // exact-overlap pairs evaluated (plain FP64 path)
@@ -23,7 +30,8 @@ enum Counter {
     C_UNTRACKED = 9,  // of those: more branching triangles than tracked
     C_PLAIN = 10,     // handed-back points whose candidates exceed the exact kernel's buffer
     C_VFAIL = 11,     // points whose undecided branch lay below the collection threshold
-    C_NCOUNTERS = 12
+    C_EDGEQ = 12,     // bull edges queued for evaluation ahead of the fold
+    C_NCOUNTERS = 13
 };
 
 struct DropCtx {
@@ -48,6 +56,10 @@ struct DropCtx {
     uint16_t* ncand;        // per CL: count, or 0xFFFF = handed to the plain path
     int cand_cap;           // list capacity per CL point
     float* blo;             // per CL: certified lower bound (local frame)
+    // bull: edge contacts evaluated ahead of the fold (null: evaluated inline)
+    uint32_t* edge_slots;   // M x EDGE_SLOTS: (triangle << 2 | edge) in fold order
+    uint8_t* edge_n;        // per CL: planned edges (may exceed EDGE_SLOTS)
+    struct EdgeRes* edge_res;  // M x EDGE_SLOTS results
     unsigned long long* counters;
     float E;                // FP32 position error budget
     float guard;            // margin for the bound tests

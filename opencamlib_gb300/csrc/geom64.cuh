@@ -347,25 +347,33 @@ __device__ inline void edge_canonical(const BasicP& c, D3 u1, D3 u2, double& ccu
 __device__ __forceinline__ D3 tri_p(const Tri64& t, int k) { return d3(t.p[3 * k], t.p[3 * k + 1], t.p[3 * k + 2]); }
 
 // MillingCutter::edgeDrop + singleEdgeDrop for one basic cutter.
+// MillingCutter::singleEdgeDrop (millingcutter.cpp:100-136) for one edge of a
+// CL point at (x, y): the contact height and CC point, true when the CC lies
+// on the segment.  Independent of the CL point's running height.
+__device__ inline bool edge_contact64(const BasicP& c, double x, double y, D3 p1, D3 p2, double& clz, D3& cc,
+                                      int* capped) {
+    double d = xy_dist_line(d3(x, y, 0.0), p1, p2);
+    if (!(d <= c.radius)) return false;
+    D3 v = p2 - p1;
+    D3 vxy = xynormalize(d3(v.x, v.y, 0.0));
+    D3 sc = xy_closest(d3(x, y, 0.0), p1, p2);
+    D3 u1 = d3(dot(p1 - sc, vxy), d, p1.z);
+    D3 u2 = d3(dot(p2 - sc, vxy), d, p2.z);
+    double ccu;
+    edge_canonical(c, u1, u2, ccu, clz, capped);
+    cc = sc + ccu * vxy;
+    cc.z = z_proj(cc, p1, p2);
+    return in_seg(cc, p1, p2);
+}
+
 __device__ inline bool edge_drop_basic(const BasicP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped) {
     bool result = false;
     for (int n = 0; n < 3; ++n) {
         if (flags & (TF_EDGE0_SKIP << n)) continue;  // isZero_tol(dx) && isZero_tol(dy)
-        D3 p1 = tri_p(t, n), p2 = tri_p(t, (n + 1) % 3);
-        double d = xy_dist_line(d3(cl.x, cl.y, cl.z), p1, p2);
-        if (d <= c.radius) {
-            D3 v = p2 - p1;
-            D3 vxy = xynormalize(d3(v.x, v.y, 0.0));
-            D3 sc = xy_closest(d3(cl.x, cl.y, cl.z), p1, p2);
-            D3 u1 = d3(dot(p1 - sc, vxy), d, p1.z);
-            D3 u2 = d3(dot(p2 - sc, vxy), d, p2.z);
-            double ccu, clz;
-            edge_canonical(c, u1, u2, ccu, clz, capped);
-            D3 cc = sc + ccu * vxy;
-            cc.z = z_proj(cc, p1, p2);
-            if (in_seg(cc, p1, p2))
-                if (liftz(cl, clz, cc, OCL_CC_EDGE)) result = true;
-        }
+        double clz;
+        D3 cc;
+        if (edge_contact64(c, cl.x, cl.y, tri_p(t, n), tri_p(t, (n + 1) % 3), clz, cc, capped))
+            if (liftz(cl, clz, cc, OCL_CC_EDGE)) result = true;
     }
     return result;
 }
