@@ -27,7 +27,9 @@
 #include <cub/cub.cuh>
 
 #include "drop.cuh"
+#include "drop_util.cuh"
 #include "geom64.cuh"
+#include "screen.cuh"
 #include "util.cuh"
 
 namespace oclg {
@@ -62,62 +64,6 @@ __global__ void k_gather_cl(const double* cl, const uint32_t* perm, uint64_t M, 
     out[3 * i] = cl[3 * j];
     out[3 * i + 1] = cl[3 * j + 1];
     out[3 * i + 2] = cl[3 * j + 2];
-}
-
-// ---------------------------------------------------------------------------
-// helpers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float warp_min(float v) {
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_max(float v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ double warp_mind(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ double warp_maxd(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-
-// k-th element of the centre-out sequence over [lo, hi] starting at c.
-__device__ __forceinline__ int centre_out(int k, int c, int lo, int hi) {
-    // sequence c, c+1, c-1, c+2, c-2, ... skipping values outside [lo, hi]
-    int up = hi - c, dn = c - lo;
-    int m = min(up, dn);
-    if (k <= 2 * m) {
-        if (k == 0) return c;
-        int s = (k + 1) / 2;
-        return (k & 1) ? c + s : c - s;
-    }
-    int rest = k - 2 * m;
-    return (up > dn) ? c + m + rest : c - m - rest;
-}
-
-// Query rectangle of a warp at grid level L in cell coordinates, widened by
-// one cell to the left and below (a triangle's home cell is its min corner's
-// and its extent is at most one cell); returns false if empty.
-__device__ __forceinline__ bool warp_rect(const GridP& g, int L, double xmin, double xmax, double ymin, double ymax,
-                                          double reach, int& c0, int& c1, int& r0, int& r1) {
-    const double inv = g.inv_cs[L];
-    double a0 = floor((xmin - reach - g.x0) * inv) - 1.0, a1 = floor((xmax + reach - g.x0) * inv);
-    double b0 = floor((ymin - reach - g.y0) * inv) - 1.0, b1 = floor((ymax + reach - g.y0) * inv);
-    if (a1 < 0 || b1 < 0 || a0 > g.ncol[L] - 1 || b0 > g.nrow[L] - 1) return false;
-    c0 = (int)fmax(a0, 0.0);
-    c1 = (int)fmin(a1, (double)(g.ncol[L] - 1));
-    r0 = (int)fmax(b0, 0.0);
-    r1 = (int)fmin(b1, (double)(g.nrow[L] - 1));
-    return true;
-}
-
-__device__ __forceinline__ float hlb_at(const float* hlb, float d, float inv_step) {
-    int k = (int)(fmaxf(d, 0.0f) * inv_step);
-    k = min(k, HLB_N - 1);
-    return hlb[k];
 }
 
 struct Best64 {
@@ -251,530 +197,6 @@ __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp * 32 < nlist; warp += nwarps)
         drop_kd_warp<FAST>(ctx, s_hlb, list, nlist, warp, s_stack[wl], lane);
-}
-
-// ---------------------------------------------------------------------------
-// FP32 screen
-// ---------------------------------------------------------------------------
-constexpr int SCREEN_WARPS = 4;
-constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
-// resident screen blocks per SM the register allocation aims at (measured:
-// more warps hide the FP32 dependency chains until spills start to cost)
-constexpr int screen_min_blocks(int kind, int ck) {
-    return kind == 2 ? 5 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
-}
-
-enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
-
-// Float <-> int keys whose integer order is the float order (for atomicMax /
-// atomicMin on floats held in shared memory).
-__device__ __forceinline__ int f2o(float f) {
-    const int b = __float_as_int(f);
-    return b >= 0 ? b : b ^ 0x7FFFFFFF;
-}
-__device__ __forceinline__ float o2f(int o) { return __int_as_float(o >= 0 ? o : o ^ 0x7FFFFFFF); }
-__device__ __forceinline__ unsigned f2u(float f) {
-    const unsigned b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float u2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u); }
-
-// Branching triangles of one warp's points ([slot][point]): triangles whose
-// effect on the running height Z has a branch point in [qlo, qhi] (cone tip
-// and rim, composite facet short-circuits).  Wp: the highest certified lower
-// bound among triangles visited before it (lower KD rank), packed with that
-// triangle's id; H: the highest upper bound among them (or the start height).
-//   W > qhi: every fold reaches the triangle with Z above all branch points;
-//   H < qlo: every fold reaches it with Z below all branch points;
-// either way its branch is decided without the triangles below the bound.
-struct BranchTab {
-    uint32_t tri[NBRANCH][32];
-    uint32_t rank[NBRANCH][32];
-    float qlo[NBRANCH][32];
-    float qhi[NBRANCH][32];
-    float hi[NBRANCH][32];
-    unsigned long long Wp[NBRANCH][32];
-    int H[NBRANCH][32];  // ordered key of a float
-};
-
-// Per-warp state of the 32 points, shared by the lanes that screen
-// (point, triangle) pairs on their behalf.
-struct WarpPoints {
-    float cx[32], cy[32], z0l[32], thr[32];
-    int blo[32];       // ordered key of the certified lower bound
-    int qx[32];        // ordered key: lowest threshold of untracked branching triangles
-    int chain_thr[32]; // ordered key: lowest branch threshold among chained triangles
-    int nc[32];        // candidates in the point's list
-    int nb[32];        // tracked branching triangles (may run past NBRANCH)
-    unsigned pending[32];
-    unsigned resolved[32];
-    int flags[32];     // PF_*
-    unsigned msk[32];  // entries of the current chunk the point wants screened
-    int pre[32];       // exclusive prefix of the masks' popcounts
-};
-constexpr int PF_OVERFLOW = 1, PF_CHAIN = 2;
-
-struct ScanShared {
-    float hlb[HLB_N];
-    Entry ent[SCREEN_WARPS][32];
-    BranchTab br[SCREEN_WARPS];
-    WarpPoints pt[SCREEN_WARPS];
-};
-
-struct LaneState {
-    float blo;          // certified lower bound of the final height
-    float qx;           // lowest branch threshold of relevant triangles not tracked
-    float thr;          // PH_RESOLVE: cut; PH_COLLECT: collection threshold
-    float zu;           // start height rounded up (local frame)
-    int nc;
-    int nb;             // tracked branching triangles
-    unsigned resolved;  // bit j: branch of tracked triangle j is decided
-    unsigned pending;   // bit j: PH_RESOLVE still looks for a witness of j
-    bool overflow;
-    bool chain;         // a collected triangle's branch depends on uncollected ones
-    float chain_thr;    // lowest branch threshold among chained triangles
-    unsigned long long screened;
-};
-
-__device__ __forceinline__ bool is_resolved(const BranchTab& b, int nb, unsigned resolved, int p, uint32_t tri) {
-    for (int j = 0; j < nb; ++j)
-        if (((resolved >> j) & 1u) && b.tri[j][p] == tri) return true;
-    return false;
-}
-
-// Lazy prune of point p's list against keep (its owner lane, between chunks).
-__device__ __forceinline__ int prune_list(const DropCtx& ctx, uint32_t self, int nc, float keep) {
-    const int cap = ctx.cand_cap;
-    uint32_t* lt = ctx.cand + (size_t)self * cap;
-    float* lh = ctx.cand_hi + (size_t)self * cap;
-    float* ll = ctx.cand_lo + (size_t)self * cap;
-    int w = 0;
-    for (int q = 0; q < min(nc, cap); ++q) {
-        const float hq = lh[q];
-        if (hq >= keep) {
-            lt[w] = lt[q];
-            lh[w] = hq;
-            ll[w] = ll[q];
-            ++w;
-        }
-    }
-    return w;
-}
-
-// One pass over the cells under the warp's footprint (coarse levels first,
-// centre rows first).  Per chunk of 32 grid entries every lane marks the
-// entries its own point wants screened; the marked (point, triangle) pairs are
-// then spread over all 32 lanes, and each lane applies its results to the
-// pair's point through shared memory.
-//   PH_SINGLE   raise blo; collect triangles whose upper bound reaches the
-//               running blo; KIND 1/2: track branching ones;
-//   PH_RESOLVE  for the pending tracked triangles, the best witness and the
-//               highest upper bound among earlier-ranked triangles; a point
-//               stops once every pending triangle has a witness;
-//   PH_COLLECT  collect everything reaching thr, noting branch thresholds
-//               below it that are not decided (chains).
-// KIND: 0 cyl/ball/bull, 1 cone, 2 composite; CK: the cutter kind for KIND
-// 0/1 (a compile-time constant, so each kernel carries one contact model).
-template <int KIND, int CK>
-__device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
-                                           uint32_t base, double xmin, double xmax, double ymin, double ymax) {
-    const int lane = threadIdx.x & 31;
-    const int wl = threadIdx.x >> 5;
-    BranchTab& br = sh.br[wl];
-    WarpPoints& P = sh.pt[wl];
-    const GridP& g = ctx.g;
-    const float R = ctx.prof.R;
-    const float gd = ctx.guard;
-    const float Rg = R + gd;
-    const float inv_step = (float)HLB_N / R;
-    const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    const int cap = ctx.cand_cap;
-    Prof32 prof = ctx.prof;
-    prof.kind = CK;
-    // publish this lane's point state
-    P.blo[lane] = f2o(ls.blo);
-    P.qx[lane] = f2o(ls.qx);
-    P.chain_thr[lane] = f2o(ls.chain_thr);
-    P.thr[lane] = ls.thr;
-    P.nc[lane] = ls.nc;
-    P.nb[lane] = ls.nb;
-    P.pending[lane] = ls.pending;
-    P.resolved[lane] = ls.resolved;
-    P.flags[lane] = (ls.overflow ? PF_OVERFLOW : 0) | (ls.chain ? PF_CHAIN : 0);
-    const float cx = P.cx[lane], cy = P.cy[lane], z0l = P.z0l[lane];
-    unsigned long long screened = 0;
-    __syncwarp();
-    for (int L = g.nlev - 1; L >= 0; --L) {
-        int c0, c1, r0, r1;
-        if (!warp_rect(g, L, xmin, xmax, ymin, ymax, reach, c0, c1, r0, r1)) continue;
-        const int rc = clampi((int)floor((0.5 * (ymin + ymax) - g.y0) * g.inv_cs[L]), r0, r1);
-        const int cc = clampi((int)floor((0.5 * (xmin + xmax) - g.x0) * g.inv_cs[L]), c0, c1);
-        const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
-        const Cell* cells = ctx.cells + g.cell_off[L];
-        const int ncol = g.ncol[L];
-    for (int kr = 0; kr < nr; ++kr) {
-        const int r = centre_out(kr, rc, r0, r1);
-        if (phase == PH_RESOLVE) {
-            if (P.pending[lane] == 0) active = false;
-            if (!__any_sync(0xffffffffu, active)) goto done;
-        }
-        for (int kc = 0; kc < ncl; ++kc) {
-            const int c = centre_out(kc, cc, c0, c1);
-            const Cell cell = cells[r * ncol + c];
-            if (cell.count == 0) continue;
-            // the threshold below which a triangle is of no interest in this phase
-            const float cut = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
-            float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
-            float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
-            float d = sqrtf(dx * dx + dy * dy);
-            bool pass = active && d <= Rg && cell.maxz - hlb_at(sh.hlb, d - gd, inv_step) >= cut - gd;
-            if (!__any_sync(0xffffffffu, pass)) continue;
-            for (uint32_t j0 = 0; j0 < cell.count; j0 += 32) {
-                const int nj = min(32, (int)(cell.count - j0));
-                __syncwarp();
-                if (lane < nj) sh.ent[wl][lane] = ctx.entries[cell.start + j0 + lane];
-                __syncwarp();
-                // 1. the entries this lane's point wants screened
-                unsigned m = 0;
-                if (pass) {
-                    const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
-                    for (int jj = 0; jj < nj; ++jj) {
-                        const Entry& e = sh.ent[wl][jj];
-                        float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
-                        float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
-                        float de = sqrtf(ex * ex + ey * ey);
-                        float ub = e.maxz - hlb_at(sh.hlb, de - gd, inv_step);
-                        if (de <= Rg && ub >= cut2 - gd && ub > z0l - gd) m |= 1u << jj;
-                    }
-                }
-                const int cnt = __popc(m);
-                // 2. room in the point's list for what this chunk may add
-                if (phase != PH_RESOLVE && cnt && P.nc[lane] + cnt > cap && !(P.flags[lane] & PF_OVERFLOW)) {
-                    const float keep = (phase == PH_COLLECT) ? ls.thr : o2f(P.blo[lane]);
-                    P.nc[lane] = prune_list(ctx, base + lane, P.nc[lane], keep - gd);
-                }
-                if (KIND != 0 && phase == PH_SINGLE && P.nb[lane] >= NBRANCH) {
-                    // drop tracked triangles that can no longer reach blo
-                    const float keep = o2f(P.blo[lane]) - gd;
-                    int w = 0;
-                    for (int j = 0; j < NBRANCH; ++j) {
-                        if (br.hi[j][lane] < keep) continue;
-                        br.tri[w][lane] = br.tri[j][lane];
-                        br.rank[w][lane] = br.rank[j][lane];
-                        br.qlo[w][lane] = br.qlo[j][lane];
-                        br.qhi[w][lane] = br.qhi[j][lane];
-                        br.hi[w][lane] = br.hi[j][lane];
-                        ++w;
-                    }
-                    P.nb[lane] = w;
-                }
-                int incl = cnt;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
-                }
-                const int total = __shfl_sync(0xffffffffu, incl, 31);
-                if (total == 0) continue;
-                P.msk[lane] = m;
-                P.pre[lane] = incl - cnt;
-                __syncwarp();
-                // 3. screen the marked pairs, 32 at a time
-                for (int k = lane; k < total; k += 32) {
-                    int p = 0;
-#pragma unroll
-                    for (int s = 16; s > 0; s >>= 1)
-                        if (p + s < 32 && P.pre[p + s] <= k) p += s;
-                    const int jj = __fns(P.msk[p], 0, k - P.pre[p] + 1);
-                    const Entry& e = sh.ent[wl][jj];
-                    const float px = P.cx[p], py = P.cy[p], pz0 = P.z0l[p];
-                    const float ub = e.maxz;  // refined below by the screen
-                    float lo, hi, qt = 3.0e38f, qth = NEG_INF32;
-                    uint32_t rank;
-                    {
-                        const Tri32 t = ctx.t32[e.tri];
-                        Iv v = (KIND == 2)
-                                   ? screen_composite(ctx.comp, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
-                                                      qt, qth)
-                                   : screen_triangle(prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
-                                                     qt, qth);
-                        ++screened;
-                        lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
-                        hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, ub + gd) : NEG_INF32;
-                        if (qt < 3.0e38f) {
-                            qt = qt + t.v0[2] - ctx.E;
-                            qth = qth + t.v0[2] + ctx.E;
-                        }
-                        rank = t.kd_rank;
-                    }
-                    if (phase == PH_RESOLVE) {
-                        const int nbp = min(P.nb[p], NBRANCH);
-                        for (int j = 0; j < nbp; ++j) {
-                            if (((P.pending[p] >> j) & 1u) && rank < br.rank[j][p]) {
-                                atomicMax(&br.Wp[j][p], ((unsigned long long)f2u(lo) << 32) | (unsigned)e.tri);
-                                atomicMax(&br.H[j][p], f2o(hi));
-                                if (lo > br.qhi[j][p] + gd) atomicAnd(&P.pending[p], ~(1u << j));
-                            }
-                        }
-                        continue;
-                    }
-                    if (phase == PH_SINGLE) {
-                        if (lo > o2f(P.blo[p])) atomicMax(&P.blo[p], f2o(lo));
-                        // track triangles that branch and may still matter
-                        if (KIND != 0 && qt < 3.0e38f && hi >= o2f(P.blo[p]) - gd) {
-                            const int slot = atomicAdd(&P.nb[p], 1);
-                            if (slot < NBRANCH) {
-                                br.tri[slot][p] = e.tri;
-                                br.rank[slot][p] = rank;
-                                br.qlo[slot][p] = qt;
-                                br.qhi[slot][p] = qth;
-                                br.hi[slot][p] = hi;
-                            } else {
-                                atomicMin(&P.qx[p], f2o(qt));
-                            }
-                        }
-                    }
-                    // collect (PH_SINGLE: lazily pruned against the rising bound)
-                    const float keep = (phase == PH_COLLECT) ? P.thr[p] : o2f(P.blo[p]);
-                    if (!(hi >= keep - gd && hi > pz0 - gd) || (P.flags[p] & PF_OVERFLOW)) continue;
-                    if (phase == PH_COLLECT && qt < P.thr[p] - gd &&
-                        !is_resolved(br, min(P.nb[p], NBRANCH), P.resolved[p], p, e.tri)) {
-                        atomicOr(&P.flags[p], PF_CHAIN);
-                        atomicMin(&P.chain_thr[p], f2o(qt));
-                    }
-                    const int slot = atomicAdd(&P.nc[p], 1);
-                    if (slot < cap) {
-                        const size_t o = (size_t)(base + p) * cap + slot;
-                        ctx.cand[o] = (uint32_t)e.tri;
-                        ctx.cand_hi[o] = hi;
-                        ctx.cand_lo[o] = lo;
-                    } else {
-                        atomicOr(&P.flags[p], PF_OVERFLOW);
-                    }
-                }
-                __syncwarp();
-                if (P.nc[lane] > cap) P.nc[lane] = cap;
-                __syncwarp();
-            }
-        }
-    }
-    }
-done:
-    __syncwarp();
-    ls.blo = o2f(P.blo[lane]);
-    ls.qx = o2f(P.qx[lane]);
-    ls.chain_thr = o2f(P.chain_thr[lane]);
-    ls.nc = min(P.nc[lane], cap);
-    ls.nb = min(P.nb[lane], NBRANCH);
-    ls.pending = P.pending[lane];
-    ls.overflow = (P.flags[lane] & PF_OVERFLOW) != 0;
-    ls.chain = (P.flags[lane] & PF_CHAIN) != 0;
-    ls.screened += screened;
-    __syncwarp();
-}
-
-// Screen kernel.  KIND 0: one pass.  KIND 1/2 (cone, composite): the effect
-// of a triangle on the running height can depend on the height reached before
-// it (tip/rim short-circuits), so
-//   pass 1  blo, the list at blo, and the branching triangles that matter;
-//           a branch point below blo is decided by a witness in the list (an
-//           earlier-ranked triangle certainly above it);
-//   pass 2  (only points with an undecided branch) witnesses among all
-//           triangles, or every earlier-ranked triangle below the branch;
-//   then    a branch still undecided is checked exactly by the refinement
-//           (the triangle is flagged in the list), or, for untracked ones, the
-//           list is collected again at the lowest open branch threshold.
-template <int KIND, int CK>
-__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
-    k_drop_screen(const __grid_constant__ DropCtx ctx) {
-    __shared__ ScanShared sh;
-    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int wl = threadIdx.x >> 5;
-    const int base = (blockIdx.x * SCREEN_WARPS + wl) * 32;
-    if (base >= ctx.M) return;
-    const bool active = base + lane < ctx.M;
-    const uint32_t i = (uint32_t)(active ? base + lane : base);
-    const GridP& g = ctx.g;
-    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
-    const float gd = ctx.guard;
-    BranchTab& br = sh.br[wl];
-    WarpPoints& P = sh.pt[wl];
-    P.cx[lane] = (float)(x - g.ox);
-    P.cy[lane] = (float)(y - g.oy);
-    P.z0l[lane] = __double2float_rd(z0 - g.oz);
-    LaneState ls;
-    ls.blo = P.z0l[lane];
-    ls.qx = 3.0e38f;
-    ls.thr = 0.0f;
-    ls.zu = __double2float_ru(z0 - g.oz);
-    ls.nc = 0;
-    ls.nb = 0;
-    ls.resolved = 0;
-    ls.pending = 0;
-    ls.overflow = false;
-    ls.chain = false;
-    ls.chain_thr = 3.0e38f;
-    ls.screened = 0;
-    double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
-    double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    scan_cells<KIND, CK>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, xmin, xmax, ymin, ymax);
-    ls.thr = ls.blo;
-    if (KIND != 0) {
-        uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
-        const float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
-        const float* ll = ctx.cand_lo + (size_t)i * ctx.cand_cap;
-        // keep the branching triangles that can still reach blo; those whose
-        // branch points lie at or above blo need no decision
-        {
-            int w = 0;
-            for (int j = 0; j < ls.nb; ++j) {
-                if (br.hi[j][lane] < ls.blo - gd) continue;
-                br.tri[w][lane] = br.tri[j][lane];
-                br.rank[w][lane] = br.rank[j][lane];
-                br.qlo[w][lane] = br.qlo[j][lane];
-                br.qhi[w][lane] = br.qhi[j][lane];
-                br.hi[w][lane] = br.hi[j][lane];
-                br.Wp[w][lane] = 0ull;  // no witness yet
-                br.H[w][lane] = f2o(ls.zu);
-                if (br.qlo[w][lane] < ls.blo) ls.pending |= 1u << w;
-                else ls.resolved |= 1u << w;
-                ++w;
-            }
-            ls.nb = w;
-        }
-        // witnesses in the list (they are folded anyway)
-        if (active && ls.pending && !ls.overflow) {
-            for (int q = 0; q < ls.nc; ++q) {
-                if (!(lh[q] >= ls.blo - gd)) continue;
-                const float lq = ll[q];
-                const uint32_t rq = ctx.t32[lt[q]].kd_rank;
-                for (int j = 0; j < ls.nb; ++j)
-                    if (((ls.pending >> j) & 1u) && rq < br.rank[j][lane] && lq > br.qhi[j][lane] + gd) {
-                        ls.pending &= ~(1u << j);
-                        ls.resolved |= 1u << j;
-                    }
-                if (!ls.pending) break;
-            }
-        }
-        if (!active || ls.overflow || ls.qx < ls.blo) ls.pending = 0;
-        if (__any_sync(0xffffffffu, ls.pending != 0)) {
-            float cut = 3.0e38f;
-            for (int j = 0; j < ls.nb; ++j)
-                if ((ls.pending >> j) & 1u) cut = fminf(cut, br.qlo[j][lane]);
-            ls.thr = cut;
-            const unsigned was = ls.pending;
-            scan_cells<KIND, CK>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, xmin, xmax, ymin, ymax);
-            for (int j = 0; j < ls.nb; ++j) {
-                if (!((was >> j) & 1u)) continue;
-                const unsigned long long wp = br.Wp[j][lane];
-                const bool above = wp != 0ull && u2f((unsigned)(wp >> 32)) > br.qhi[j][lane] + gd;
-                const bool below = o2f(br.H[j][lane]) < br.qlo[j][lane] - gd;
-                if (above || below) ls.resolved |= 1u << j;
-            }
-            ls.pending = 0;
-        }
-        // a branch still undecided: the refinement decides it exactly (FP64)
-        // for a tracked triangle, which is in the list (flagged); untracked
-        // ones lower the collection threshold instead
-        float open = 3.0e38f;
-        bool verify = false;
-        if (active && !ls.overflow) {
-            int pos[NBRANCH];
-            bool all_found = ls.qx >= ls.blo;
-            for (int j = 0; j < ls.nb; ++j) {
-                pos[j] = -1;
-                if ((ls.resolved >> j) & 1u) continue;
-                open = fminf(open, br.qlo[j][lane]);
-                for (int q = 0; q < ls.nc && pos[j] < 0; ++q)
-                    if (lt[q] == br.tri[j][lane] && lh[q] >= ls.blo - gd) pos[j] = q;
-                if (pos[j] < 0) all_found = false;
-            }
-            if (all_found && open < ls.blo) {
-                for (int j = 0; j < ls.nb; ++j)
-                    if (pos[j] >= 0) lt[pos[j]] |= CAND_VERIFY;
-                verify = true;
-                open = 3.0e38f;
-            }
-            open = fminf(open, ls.qx);
-        }
-        ls.thr = ls.blo;
-        const bool need = active && open < ls.blo && !ls.overflow;
-        if (need || (active && verify)) atomicAdd(&ctx.counters[C_OPEN], 1ull);
-        if (need) atomicAdd(&ctx.counters[C_UNTRACKED], 1ull);
-        if (__any_sync(0xffffffffu, need)) {
-            // collect at the lowest open threshold; if a collected triangle's
-            // branch threshold lies below it, lower it and collect again
-            ls.thr = need ? open : 3.0e38f;
-            bool done = !need;
-            for (int round = 0; round < 4; ++round) {
-                const float keep_thr = ls.thr;
-                if (!done) {
-                    ls.nc = 0;
-                    ls.chain = false;
-                    ls.chain_thr = 3.0e38f;
-                }
-                scan_cells<KIND, CK>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, xmin, xmax, ymin, ymax);
-                ls.thr = keep_thr;
-                const bool again = !done && ls.chain && !ls.overflow && round < 3;
-                if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
-                else done = true;
-                if (!__any_sync(0xffffffffu, again)) break;
-            }
-            if (!need) ls.thr = ls.blo;
-        }
-        // witnesses found outside the list must be folded before their
-        // triangles: add them (pinned against pruning)
-        if (active && !ls.overflow && !ls.chain) {
-            float* lhw = ctx.cand_hi + (size_t)i * ctx.cand_cap;
-            for (int j = 0; j < ls.nb; ++j) {
-                if (!((ls.resolved >> j) & 1u)) continue;
-                const unsigned long long wp = br.Wp[j][lane];
-                if (wp == 0ull || !(u2f((unsigned)(wp >> 32)) > br.qhi[j][lane] + gd)) continue;
-                const uint32_t wt = (uint32_t)(wp & 0xFFFFFFFFull);
-                bool have = false;
-                for (int q = 0; q < ls.nc && !have; ++q)
-                    have = ((lt[q] & ~CAND_VERIFY) == wt && lhw[q] >= ls.thr - gd);
-                if (have) continue;
-                if (ls.nc == ctx.cand_cap) {
-                    ls.overflow = true;
-                    break;
-                }
-                lt[ls.nc] = wt;
-                lhw[ls.nc] = 3.0e38f;
-                ++ls.nc;
-            }
-        }
-    }
-    __syncwarp();
-    if (active) {
-        if (ls.overflow || ls.chain) {
-            ctx.ncand[i] = 0xFFFF;
-            atomicAdd(&ctx.counters[ls.overflow ? C_OVERFLOW : C_CHAIN], 1ull);
-        } else {
-            uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
-            const float* lh = ctx.cand_hi + (size_t)i * ctx.cand_cap;
-            int w = 0;
-            for (int q = 0; q < ls.nc; ++q)
-                if (lh[q] >= ls.thr - gd) lt[w++] = lt[q];
-            // order the list by the reference's visit order (ascending KD rank)
-            for (int a = 1; a < w; ++a) {
-                const uint32_t t = lt[a];
-                const uint32_t rk = ctx.t32[t & ~CAND_VERIFY].kd_rank;
-                int b = a - 1;
-                while (b >= 0 && ctx.t32[lt[b] & ~CAND_VERIFY].kd_rank > rk) {
-                    lt[b + 1] = lt[b];
-                    --b;
-                }
-                lt[b + 1] = t;
-            }
-            ctx.ncand[i] = (uint16_t)w;
-        }
-        ctx.blo[i] = ls.blo;
-    }
-    unsigned long long scr = ls.screened;
-    for (int o = 16; o > 0; o >>= 1) scr += __shfl_xor_sync(0xffffffffu, scr, o);
-    if (lane == 0 && scr) atomicAdd(&ctx.counters[C_SCREENED], scr);
 }
 
 // One step of dropCutter5's fold (batchdropcutter.cpp:187-231): the overlap
@@ -1207,17 +629,14 @@ struct DropWork {
 static thread_local DropWork* tl_work = nullptr;
 
 static void launch_screen(const DropCtx& h, const CutterP& cp, unsigned blocks, cudaStream_t stream) {
-    const dim3 tb(SCREEN_WARPS * 32);
-    if (cp.kind == OCL_CUTTER_COMPOSITE)
-        k_drop_screen<2, -1><<<blocks, tb, 0, stream>>>(h);
-    else if (cp.kind == OCL_CUTTER_CONE)
-        k_drop_screen<1, OCL_CUTTER_CONE><<<blocks, tb, 0, stream>>>(h);
-    else if (cp.b.kind == OCL_CUTTER_CYL)
-        k_drop_screen<0, OCL_CUTTER_CYL><<<blocks, tb, 0, stream>>>(h);
-    else if (cp.b.kind == OCL_CUTTER_BALL)
-        k_drop_screen<0, OCL_CUTTER_BALL><<<blocks, tb, 0, stream>>>(h);
-    else
-        k_drop_screen<0, OCL_CUTTER_BULL><<<blocks, tb, 0, stream>>>(h);
+    if (cp.kind == OCL_CUTTER_COMPOSITE) {
+        // the presets' make-ups (compositecutter.cpp:298-383) get their own kernels
+        const int sig = cp.nsub == 3 ? comp_sig(cp.sub[0].kind, cp.sub[1].kind, cp.sub[2].kind) : -1;
+        if (!screen_launch_comp_a(h, sig, blocks, stream) && !screen_launch_comp_b(h, sig, blocks, stream))
+            screen_launch_comp_any(h, blocks, stream);
+    } else {
+        screen_launch_basic(h, cp.kind == OCL_CUTTER_CONE ? OCL_CUTTER_CONE : cp.b.kind, blocks, stream);
+    }
 }
 
 // k_drop_exact over the handed-back points (count on the device).
