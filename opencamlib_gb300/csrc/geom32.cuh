@@ -272,6 +272,75 @@ __device__ inline Iv edge32(const Prof32& c, float ax, float ay, float az, float
     return gate(st, clz - err, clz + err);
 }
 
+// The bull's three edge contacts of one triangle at once (same bounds as
+// edge32): the three maximisations along the edge lines run interleaved,
+// 16 bisection steps each, and the contact position's uncertainty includes
+// the final bracket.  Horizontal and skipped edges take edge32's paths.
+__device__ inline void bull_edges32(const Prof32& c, const float* px, const float* py, const float* pz, uint32_t flags,
+                                    float wx, float wy, float E, Iv* out) {
+    float u1[3], u2[3], m[3], dm[3], lo_u[3], hi_u[3], L[3];
+    bool run[3];
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        out[n] = iv_none();
+        run[n] = false;
+        u1[n] = u2[n] = m[n] = dm[n] = lo_u[n] = hi_u[n] = 0.0f;
+        L[n] = 1.0f;
+        if (flags & (TF_EDGE0_SKIP << n)) continue;
+        const int k = (n + 1) % 3;
+        if (flags & (TF_EDGE0_HORIZ << n)) {
+            out[n] = edge32(c, px[n], py[n], pz[n], px[k], py[k], pz[k], wx, wy, E, true);
+            continue;
+        }
+        const float dx = px[k] - px[n], dy = py[k] - py[n];
+        L[n] = sqrtf(dx * dx + dy * dy);
+        const float ux = dx / L[n], uy = dy / L[n];
+        const float qx = wx - px[n], qy = wy - py[n];
+        const float d = fabsf(ux * qy - uy * qx);
+        if (d - E > c.R) continue;
+        const float along = ux * qx + uy * qy;
+        u1[n] = -along;
+        u2[n] = L[n] - along;
+        m[n] = (pz[k] - pz[n]) / L[n];
+        dm[n] = fminf(d, c.R);
+        const float s = sqrtf(fmaxf(c.R * c.R - dm[n] * dm[n], 0.0f));
+        lo_u[n] = -s;
+        hi_u[n] = s;
+        run[n] = true;
+    }
+    // maximise f(u) = az + (u - u1) m - h(sqrt(u^2 + d^2)) on |u| < s
+    for (int it = 0; it < 16; ++it) {
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+            const float mid = 0.5f * (lo_u[n] + hi_u[n]);
+            const float rho = sqrtf(mid * mid + dm[n] * dm[n]);
+            const float fp = m[n] - dh32(c, rho) * (rho > 0 ? mid / rho : 0.0f);
+            if (fp > 0) lo_u[n] = mid; else hi_u[n] = mid;
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < 3; ++n) {
+        if (!run[n]) continue;
+        const float ccu = 0.5f * (lo_u[n] + hi_u[n]);
+        const float rho = sqrtf(ccu * ccu + dm[n] * dm[n]);
+        const float clz = pz[n] + (ccu - u1[n]) * m[n] - h32(c, rho);
+        const float rl = sqrtf(lo_u[n] * lo_u[n] + dm[n] * dm[n]);
+        const float fpl = fabsf(m[n] - dh32(c, rl) * (rl > 0 ? lo_u[n] / rl : 0.0f));
+        const float width = hi_u[n] - lo_u[n];
+        const float slack = fminf(fpl * width, 1.0f);
+        const float rd = rho > 1e-20f ? dm[n] / rho : 0.0f;
+        const float err = E * (3.0f + fabsf(m[n]) + dh32(c, fminf(rho + E, c.R)) * (1.0f + rd)) + slack;
+        const float curv = 1.0f + dh32(c, fminf(rho + 4.0f * E, c.R));
+        const float Eu = E * (2.0f + curv) + 1e-4f * c.r2 + width;
+        // CC inside the segment (Point::isInside(p1,p2), param in [0,1])
+        const float tcc = (ccu - u1[n]) / (u2[n] - u1[n]);
+        const float et = (Eu + 1e-6f) / L[n];
+        int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
+        if (dm[n] + E > c.R && st > 0) st = 0;
+        out[n] = gate(st, clz - err, clz + err);
+    }
+}
+
 // Whole-triangle screen for the basic cutters, local frame (relative to v0).
 // Returns the interval of the triangle's effect on the running z
 // (dropCutter applied to a CL point already at some height Z >= z0).
@@ -293,12 +362,20 @@ __device__ inline Iv screen_triangle(const Prof32& c, const Tri32& t, float wx, 
     const float px[3] = {0.0f, t.e1[0], t.e2[0]};
     const float py[3] = {0.0f, t.e1[1], t.e2[1]};
     const float pz[3] = {0.0f, t.e1[2], t.e2[2]};
+    if (c.kind == OCL_CUTTER_BULL) {
+        Iv ev[3];
+        bull_edges32(c, px, py, pz, t.flags, wx, wy, E, ev);
+        iv_max(best, ev[0]);
+        iv_max(best, ev[1]);
+        iv_max(best, ev[2]);
+    } else {
 #pragma unroll
-    for (int n = 0; n < 3; ++n) {
-        if (t.flags & (TF_EDGE0_SKIP << n)) continue;
-        const int k = (n + 1) % 3;
-        const bool horiz = (t.flags & (TF_EDGE0_HORIZ << n)) != 0;
-        iv_max(best, edge32(c, px[n], py[n], pz[n], px[k], py[k], pz[k], wx, wy, E, horiz));
+        for (int n = 0; n < 3; ++n) {
+            if (t.flags & (TF_EDGE0_SKIP << n)) continue;
+            const int k = (n + 1) % 3;
+            const bool horiz = (t.flags & (TF_EDGE0_HORIZ << n)) != 0;
+            iv_max(best, edge32(c, px[n], py[n], pz[n], px[k], py[k], pz[k], wx, wy, E, horiz));
+        }
     }
     if (c.kind == OCL_CUTTER_CONE) {
         // ConeCutter::facetDrop (conecutter.cpp:70-105): the tip contact, when
