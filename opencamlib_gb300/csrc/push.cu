@@ -111,6 +111,13 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     if (ctx.dir == OCL_GB300_XFIBER) { clx = 0; cly = fb.p1.y; }
     else { clx = fb.p1.x; cly = 0; }
     const double bb[6] = {clx - r, clx + r, cly - r, cly + r, fb.p1.z, fb.p1.z + ctx.cp.length};
+    // a triangle's interval lies where the cutter's axis passes within the
+    // cutter radius of the triangle's bbox: [bb_min - r, bb_max + r] along the
+    // fiber, in fiber parameter units (with a margin for rounding)
+    const bool xf = ctx.dir == OCL_GB300_XFIBER;
+    const double f0 = xf ? fb.p1.x : fb.p1.y;
+    const double fl = xf ? fb.p2.x - fb.p1.x : fb.p2.y - fb.p1.y;
+    const double finv = fl != 0.0 ? 1.0 / fl : 0.0;
     Ival64 local_ints[PUSH_CAP];
     Ival64* ints = list ? scratch + (size_t)slot * PUSH_CAP_BIG : local_ints;
     const int cap = list ? PUSH_CAP_BIG : PUSH_CAP;
@@ -136,6 +143,56 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
             for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
                 if (!in) continue;
                 const Tri64& t = ctx.t64[ctx.order[k]];
+                double halfw = r;  // how far along the fiber the axis can be from the triangle
+                // the KD walk accepts whole leaves; every push contact lies on the
+                // cutter's surface: within the radius of the axis and no lower
+                // than the profile height at its distance.  A triangle farther
+                // than the radius from the fiber's line, or entirely below the
+                // profile at its nearest distance, has an empty interval.
+                {
+                    const double cr = xf ? fb.p1.y : fb.p1.x;
+                    const double lo = xf ? t.bb[2] : t.bb[0], hi = xf ? t.bb[3] : t.bb[1];
+                    const double gap = fmax(lo - cr, cr - hi);
+                    const double mg = 1e-9 * (1.0 + fabs(cr) + r + fabs(fb.p1.z));
+                    if (gap > r + mg) {
+                        ++calls;
+                        continue;
+                    }
+                    const double hmin = gap > mg ? height_any(ctx.cp, fmin(gap - mg, r)) : 0.0;
+                    if (t.bb[5] < fb.p1.z + fmax(hmin, 0.0) - mg) {
+                        ++calls;
+                        continue;
+                    }
+                    // a contact at distance q across the fiber and height h above
+                    // the tip lies within sqrt(r^2 - q^2), and within the
+                    // cutter's width at h, of the axis
+                    const double g = fmax(gap - mg, 0.0);
+                    halfw = sqrt(fmax(r * r - g * g, 0.0));
+                    if (ctx.cp.kind != OCL_CUTTER_COMPOSITE) {
+                        const double wz = width_basic(ctx.cp.b, t.bb[5] - fb.p1.z + mg);
+                        if (wz >= 0.0) halfw = fmin(halfw, wz);
+                    }
+                    halfw += mg;
+                }
+                if (n > 0 && !overflow && finv != 0.0) {
+                    // Fiber::addInterval ignores an interval strictly inside one
+                    // it holds: pass over triangles whose bound already is
+                    double a = ((xf ? t.bb[0] : t.bb[2]) - halfw - f0) * finv;
+                    double b = ((xf ? t.bb[1] : t.bb[3]) + halfw - f0) * finv;
+                    if (a > b) {
+                        const double s = a;
+                        a = b;
+                        b = s;
+                    }
+                    a -= 1e-9 * (1.0 + fabs(a));
+                    b += 1e-9 * (1.0 + fabs(b));
+                    bool inside = false;
+                    for (int q = 0; q < n && !inside; ++q) inside = a > ints[q].lower && b < ints[q].upper;
+                    if (inside) {
+                        ++calls;
+                        continue;
+                    }
+                }
                 Ival64 iv;
                 iv_init(iv);
                 push_triangle64(ctx.cp, fb, iv, t, &capped);
