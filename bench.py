@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1024, help="CL points per cutter in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-aux", action="store_true", help="skip the push and path measurements")
     ap.add_argument("--cutters", default="", help="comma list of cutters (default: all five); for profiling")
     ap.add_argument("--block", type=int, default=0,
                     help="only an N x N block of the raster (a small case for profiling)")
@@ -141,6 +142,91 @@ def cpu_baseline(tris, cl, sample, nthreads=0):
     return {"value": n / total, "unit": "CL-points/s", "cores": cores, "kind": "port",
             "sample": f"{len(pts)} CL points per cutter x {len(cutters())} cutters "
                       f"(seeded uniform sample of the 0.1 mm raster), {total:.2f} s of CPU loop time"}
+
+
+def aux_measurements(cl_mesh, cuts, with_cpu):
+    """The other operations on the path, measured beside the headline:
+    BatchPushCutter on a waterline-like fiber set (sphere-on-plate + torus,
+    499,202 triangles; 10 z levels x 2,000 X- and 2,000 Y-fibers, extent the
+    mesh bbox +- 2 radii) and PathDropCutter / AdaptivePathDropCutter on a
+    zig-zag of 100 line spans across the 1,048,576-triangle mesh.  Device time
+    from the library's CUDA events; the CPU figures are the oracle port on
+    every 50th fiber / every 10th span (OpenMP on all host cores)."""
+    import ctypes as C
+    from opencamlib_gb300 import _abi, _native, cutters as cu, workloads as w
+    out = {}
+    L = _native.lib()
+    tris = w.sphere_torus(1)
+    mesh = _native.DeviceMesh(tris)
+    push = {}
+    for name, c in (("ball", cu.BallCutter(6.0, 20.0)), ("bull", cu.BullCutter(6.0, 1.0, 20.0))):
+        r = c.radius
+        tot_ms, tot_f, cpu_s, cpu_f = 0.0, 0, 0.0, 0
+        for d in (0, 1):
+            fib = np.ascontiguousarray(np.concatenate(
+                [w.fibers(d, 1.0 + 48.0 * k / 49.0, 0.0, 100.0, 2000, -2 * r, 100.0 + 2 * r) for k in range(0, 50, 5)]))
+            F = fib.shape[0]
+            offsets = np.zeros(F + 1, dtype=np.uint64)
+            cap = 8 * F
+            iv, cc, ty = np.empty(2 * cap), np.empty(6 * cap), np.empty(2 * cap, dtype=np.int32)
+            desc = c.desc()
+            st = _abi.Stats()
+            for _ in range(2):
+                s = L.ocl_gb300_push(mesh.handle, C.byref(desc), d, fib.ctypes.data_as(C.POINTER(C.c_double)), F,
+                                     offsets.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                     iv.ctypes.data_as(C.POINTER(C.c_double)), cc.ctypes.data_as(C.POINTER(C.c_double)),
+                                     ty.ctypes.data_as(C.POINTER(C.c_int32)), cap, C.byref(st))
+                if s != 0:
+                    raise RuntimeError(L.ocl_gb300_last_error().decode())
+            tot_ms += st.kernel_ms
+            tot_f += F
+            if with_cpu:
+                from oracle import checker
+                sub = fib[::50]
+                t0 = time.perf_counter()
+                checker.push(tris, c, d, sub, "port")
+                cpu_s += time.perf_counter() - t0
+                cpu_f += len(sub)
+        push[name] = {"fibers": tot_f, "gpu_ms": tot_ms, "gpu_fibers_per_s": tot_f / (tot_ms / 1e3),
+                      "cpu_fibers_per_s": (cpu_f / cpu_s) if cpu_s else None,
+                      "cpu_sample": f"{cpu_f} fibers (every 50th), KD build included"}
+    out["push"] = push
+    mesh.release()
+    # paths: zig-zag of 100 lines across the bump mesh
+    m2 = _native.DeviceMesh(cl_mesh)
+    spans = []
+    for k in range(100):
+        y = 0.5 + k
+        a, b = (0.0, 100.0) if k % 2 == 0 else (100.0, 0.0)
+        spans.append([0, a, y, 0, b, y, 0, 0, 0, 0, 0])
+    spans = np.array(spans, dtype=np.float64)
+    paths = {}
+    for name, c in cuts:
+        if name not in ("ball", "ballcone"):
+            continue
+        m2.path_drop(c, spans, 0.1, -50.0)
+        t0 = time.perf_counter()
+        xyz, _, _, st = m2.path_drop(c, spans, 0.1, -50.0)
+        pdc_s = time.perf_counter() - t0
+        m2.adaptive_path_drop(c, spans, 1.0, 0.01)
+        t0 = time.perf_counter()
+        axyz, _, _, ast = m2.adaptive_path_drop(c, spans, 1.0, 0.01)
+        apdc_s = time.perf_counter() - t0
+        rec = {"pdc_points": int(len(xyz)), "pdc_wall_ms": pdc_s * 1e3, "pdc_points_per_s": len(xyz) / pdc_s,
+               "apdc_points": int(len(axyz)), "apdc_wall_ms": apdc_s * 1e3, "apdc_points_per_s": len(axyz) / apdc_s}
+        if with_cpu:
+            from oracle import checker
+            t0 = time.perf_counter()
+            cx = checker.pdc(cl_mesh, c, spans[::10], 0.1, -50.0, "port")[0]
+            rec["cpu_pdc_points_per_s"] = len(cx) / (time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            ca = checker.apdc(cl_mesh, c, spans[::10], 1.0, 0.01, 0.999, "port")[0]
+            rec["cpu_apdc_points_per_s"] = len(ca) / (time.perf_counter() - t0)
+            rec["cpu_sample"] = "every 10th span, KD build included; APDC restatement is single-threaded as the reference's"
+        paths[name] = rec
+    out["paths"] = paths
+    m2.release()
+    return out
 
 
 def sample_indices(sample, seed=17):
@@ -339,6 +425,12 @@ def main():
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
     kname = {"screen": "k_drop_screen", "refine": "k_drop_refine", "fallback": "k_drop_kd"}[dom]
 
+    aux = None
+    if not args.no_aux and not (args.block or args.cutters or args.stride):
+        try:
+            aux = aux_measurements(tris, cuts, not args.no_cpu_baseline)
+        except Exception as e:  # reported, never required
+            aux = {"error": str(e)}
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -384,6 +476,7 @@ def main():
         "precision": prec,
         "fp64_block": fp64_rate,
         "cpu_baseline": cpu,
+        "other_operations": aux,
     }
     print(json.dumps(line), flush=True)
     if dist:
