@@ -187,7 +187,7 @@ class DeviceMesh:
 
     def path_drop(self, cutter, spans, sampling, min_z):
         spans = _d(spans, _abi.SPAN_DOUBLES)
-        cap = 4096
+        cap = max(4096, getattr(self, "_path_cap", 0))
         desc = cutter.desc()
         while True:
             xyz = np.empty((cap, 3))
@@ -199,6 +199,7 @@ class DeviceMesh:
                                                _p(xyz), _p(cc), _p(ty, _ip), cap, C.byref(n), C.byref(st))
             if status == _abi.CAPACITY:
                 cap = int(n.value)
+                self._path_cap = cap
                 continue
             check(status)
             k = int(n.value)
@@ -206,7 +207,7 @@ class DeviceMesh:
 
     def adaptive_path_drop(self, cutter, spans, sampling, min_sampling, cos_limit=0.999):
         spans = _d(spans, _abi.SPAN_DOUBLES)
-        cap = 4096
+        cap = max(4096, getattr(self, "_path_cap", 0))
         desc = cutter.desc()
         while True:
             xyz = np.empty((cap, 3))
@@ -219,6 +220,7 @@ class DeviceMesh:
                                                         C.byref(n), C.byref(st))
             if status == _abi.CAPACITY:
                 cap = int(n.value)
+                self._path_cap = cap
                 continue
             check(status)
             k = int(n.value)

@@ -586,7 +586,7 @@ struct DropWork {
     DevBuf<float> cand_hi, cand_lo;
     DevBuf<uint16_t> ncand;
     DevBuf<float> blo;
-    DevBuf<uint32_t> list, list2;
+    DevBuf<uint32_t> list, list2, sparse;
     DevBuf<unsigned long long> counters;
     // bull edges ahead of the fold (allocated on first use)
     DevBuf<uint32_t> edge_slots;
@@ -616,7 +616,7 @@ struct DropWork {
         if (M > cap || !counters.p) {
             size_t c = std::max<size_t>(M, 1024);
             if (!keys.alloc(c) || !keys2.alloc(c) || !perm0.alloc(c) || !perm.alloc(c) || !cls.alloc(3 * c) ||
-                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !cand_lo.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) || !list2.alloc(c) ||
+                !cand.alloc(c * CAND_K) || !cand_hi.alloc(c * CAND_K) || !cand_lo.alloc(c * CAND_K) || !ncand.alloc(c) || !blo.alloc(c) || !list.alloc(c) || !list2.alloc(c) || !sparse.alloc(c / 32 + 1) ||
                 !counters.alloc(C_NCOUNTERS + 1))
                 return false;
             cap = c;
@@ -628,14 +628,29 @@ struct DropWork {
 
 static thread_local DropWork* tl_work = nullptr;
 
+// The dense screen kernel over all warps, then the sparse one over the warps
+// whose points it found spread out (a fixed grid striding over the list).
+// Seeding kernel (bounds of spread-out warps), the dense screen kernel over
+// all warps, then the sparse one over the warps it found scattered (a fixed
+// grid striding over the list).  `h` must have `seeded` set.
 static void launch_screen(const DropCtx& h, const CutterP& cp, unsigned blocks, cudaStream_t stream) {
+    const unsigned sblocks = std::min<unsigned>(blocks, 152u * 4u);
     if (cp.kind == OCL_CUTTER_COMPOSITE) {
         // the presets' make-ups (compositecutter.cpp:298-383) get their own kernels
         const int sig = cp.nsub == 3 ? comp_sig(cp.sub[0].kind, cp.sub[1].kind, cp.sub[2].kind) : -1;
+        if (!screen_launch_comp_a_sparse(h, sig, blocks, stream, 0) &&
+            !screen_launch_comp_b_sparse(h, sig, blocks, stream, 0))
+            screen_launch_comp_any_sparse(h, blocks, stream, 0);
         if (!screen_launch_comp_a(h, sig, blocks, stream) && !screen_launch_comp_b(h, sig, blocks, stream))
             screen_launch_comp_any(h, blocks, stream);
+        if (!screen_launch_comp_a_sparse(h, sig, sblocks, stream, 1) &&
+            !screen_launch_comp_b_sparse(h, sig, sblocks, stream, 1))
+            screen_launch_comp_any_sparse(h, sblocks, stream, 1);
     } else {
-        screen_launch_basic(h, cp.kind == OCL_CUTTER_CONE ? OCL_CUTTER_CONE : cp.b.kind, blocks, stream);
+        const int kind = cp.kind == OCL_CUTTER_CONE ? OCL_CUTTER_CONE : cp.b.kind;
+        screen_launch_basic_sparse(h, kind, blocks, stream, 0);
+        screen_launch_basic(h, kind, blocks, stream);
+        screen_launch_basic_sparse(h, kind, sblocks, stream, 1);
     }
 }
 
@@ -699,6 +714,9 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     h->cand_cap = CAND_K;
     h->ncand = w.ncand.p;
     h->blo = w.blo.p;
+    h->sparse_list = w.sparse.p;
+    h->seeded = true;
+    h->sparse_n = w.counters.p + C_SPARSE;
     h->counters = w.counters.p;
     h->kd_nodes = m.drop_kd.d_nodes;
     h->kd_order = m.drop_kd.d_order;
@@ -767,7 +785,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         if (st) return st;
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
         k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list2.p, w.counters.p + C_PLAIN);
-        launches += 5;
+        launches += 7;  // seed, dense and sparse screen, refine, collect, exact, plain
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[4], stream));
@@ -847,6 +865,7 @@ struct NoAllocScratch {
     float cand_lo[OCL_GB300_NOALLOC_MAX_POINTS * CAND_K_NOALLOC];
     uint32_t list[OCL_GB300_NOALLOC_MAX_POINTS];
     uint32_t list2[OCL_GB300_NOALLOC_MAX_POINTS];
+    uint32_t sparse[OCL_GB300_NOALLOC_MAX_POINTS / 32 + 1];
     float blo[OCL_GB300_NOALLOC_MAX_POINTS];
     uint16_t ncand[OCL_GB300_NOALLOC_MAX_POINTS];
     unsigned long long counters[C_NCOUNTERS + 1];
@@ -916,6 +935,9 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     h.cand_cap = CAND_K_NOALLOC;
     h.ncand = sc->ncand;
     h.blo = sc->blo;
+    h.sparse_list = sc->sparse;
+    h.seeded = true;
+    h.sparse_n = sc->counters + C_SPARSE;
     h.counters = sc->counters;
     bool composite = false;
     fill_prof(cp, h.prof, h.hlb, composite);

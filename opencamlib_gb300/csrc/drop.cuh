@@ -31,7 +31,8 @@ enum Counter {
     C_PLAIN = 10,     // handed-back points whose candidates exceed the exact kernel's buffer
     C_VFAIL = 11,     // points whose undecided branch lay below the collection threshold
     C_EDGEQ = 12,     // bull edges queued for evaluation ahead of the fold
-    C_NCOUNTERS = 13
+    C_SPARSE = 13,    // warps handed to the sparse screen kernel
+    C_NCOUNTERS = 14
 };
 
 struct DropCtx {
@@ -56,6 +57,9 @@ struct DropCtx {
     uint16_t* ncand;        // per CL: count, or 0xFFFF = handed to the plain path
     int cand_cap;           // list capacity per CL point
     float* blo;             // per CL: certified lower bound (local frame)
+    bool seeded;            // blo holds the seeding kernel's bounds on entry to the screen
+    uint32_t* sparse_list;  // warps handed from the dense to the sparse screen kernel
+    unsigned long long* sparse_n;
     // bull: edge contacts evaluated ahead of the fold (null: evaluated inline)
     uint32_t* edge_slots;   // M x EDGE_SLOTS: (triangle << 2 | edge) in fold order
     uint8_t* edge_n;        // per CL: planned edges (may exceed EDGE_SLOTS)

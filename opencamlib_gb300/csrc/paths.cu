@@ -96,6 +96,39 @@ static void span_point(const SpanH& s, double t, double* out) {
 }
 
 // Batch drop of host points through the device path.
+// Device and pinned host buffers of the path drivers, kept by the calling
+// thread across batches (the adaptive driver drops one batch per level).
+struct PathIO {
+    DevBuf<double> dcl, dz, dcc;
+    DevBuf<int32_t> dty;
+    double* hcl = nullptr;
+    double* hz = nullptr;
+    double* hcc = nullptr;
+    int32_t* hty = nullptr;
+    uint64_t cap = 0;
+    bool ensure(uint64_t M) {
+        if (M <= cap) return true;
+        const uint64_t c = std::max<uint64_t>(M, 4096);
+        if (!dcl.alloc(3 * c) || !dz.alloc(c) || !dcc.alloc(3 * c) || !dty.alloc(c)) return false;
+        cudaFreeHost(hcl);
+        cudaFreeHost(hz);
+        cudaFreeHost(hcc);
+        cudaFreeHost(hty);
+        hcl = hz = hcc = nullptr;
+        hty = nullptr;
+        if (cudaMallocHost(&hcl, 3 * c * sizeof(double)) != cudaSuccess ||
+            cudaMallocHost(&hz, c * sizeof(double)) != cudaSuccess ||
+            cudaMallocHost(&hcc, 3 * c * sizeof(double)) != cudaSuccess ||
+            cudaMallocHost(&hty, c * sizeof(int32_t)) != cudaSuccess) {
+            cap = 0;
+            return false;
+        }
+        cap = c;
+        return true;
+    }
+};
+static thread_local PathIO tl_path_io;
+
 static int drop_host(Mesh& m, const CutterP& cp, const std::vector<double>& cl, std::vector<double>& z,
                      std::vector<double>& cc, std::vector<int32_t>& ty, ocl_gb300_stats* acc) {
     const uint64_t M = cl.size() / 3;
@@ -103,17 +136,21 @@ static int drop_host(Mesh& m, const CutterP& cp, const std::vector<double>& cl, 
     cc.resize(3 * M);
     ty.resize(M);
     if (M == 0) return OCL_GB300_OK;
-    DevBuf<double> dcl(3 * M), dz(M), dcc(3 * M);
-    DevBuf<int32_t> dty(M);
-    if (!dcl.ok() || !dz.ok() || !dcc.ok() || !dty.ok()) return OCL_GB300_OOM;
-    CK(cudaMemcpy(dcl.p, cl.data(), 3 * M * sizeof(double), cudaMemcpyHostToDevice));
+    PathIO& io = tl_path_io;
+    if (!io.ensure(M)) return OCL_GB300_OOM;
+    std::memcpy(io.hcl, cl.data(), 3 * M * sizeof(double));
+    CK(cudaMemcpyAsync(io.dcl.p, io.hcl, 3 * M * sizeof(double), cudaMemcpyHostToDevice, 0));
     ocl_gb300_stats st;
     std::memset(&st, 0, sizeof(st));
-    int r = drop_run(m, cp, dcl.p, M, OCL_GB300_PREC_MIXED, dz.p, dcc.p, dty.p, 0, &st);
+    int r = drop_run(m, cp, io.dcl.p, M, OCL_GB300_PREC_MIXED, io.dz.p, io.dcc.p, io.dty.p, 0, acc ? &st : nullptr);
     if (r) return r;
-    CK(cudaMemcpy(z.data(), dz.p, M * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(cc.data(), dcc.p, 3 * M * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ty.data(), dty.p, M * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(io.hz, io.dz.p, M * sizeof(double), cudaMemcpyDeviceToHost, 0));
+    CK(cudaMemcpyAsync(io.hcc, io.dcc.p, 3 * M * sizeof(double), cudaMemcpyDeviceToHost, 0));
+    CK(cudaMemcpyAsync(io.hty, io.dty.p, M * sizeof(int32_t), cudaMemcpyDeviceToHost, 0));
+    CK(cudaStreamSynchronize(0));
+    std::memcpy(z.data(), io.hz, M * sizeof(double));
+    std::memcpy(cc.data(), io.hcc, 3 * M * sizeof(double));
+    std::memcpy(ty.data(), io.hty, M * sizeof(int32_t));
     if (acc) {
         acc->pairs += st.pairs;
         acc->refined += st.refined;

@@ -30,10 +30,18 @@ constexpr int SIG_CONECONE = comp_sig(OCL_CUTTER_CONE, OCL_CUTTER_CONE, OCL_CUTT
 
 // Launchers, one translation unit each (screen_basic.cu, screen_comp_*.cu).
 // The composite ones return false when the make-up is not theirs.
+// The *_sparse launchers run the kernels for the warps the dense kernels
+// handed over (their grid of `blocks` strides over them); own units too.
 void screen_launch_basic(const DropCtx& h, int kind, unsigned blocks, cudaStream_t stream);
 bool screen_launch_comp_a(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream);
 bool screen_launch_comp_b(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream);
 void screen_launch_comp_any(const DropCtx& h, unsigned blocks, cudaStream_t stream);
+// stage 0: the seeding kernel (before the dense one; `blocks` covers the
+// points), stage 1: the sparse kernel (after it)
+void screen_launch_basic_sparse(const DropCtx& h, int kind, unsigned blocks, cudaStream_t stream, int stage);
+bool screen_launch_comp_a_sparse(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream, int stage);
+bool screen_launch_comp_b_sparse(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream, int stage);
+void screen_launch_comp_any_sparse(const DropCtx& h, unsigned blocks, cudaStream_t stream, int stage);
 
 // Float <-> int keys whose integer order is the float order (for atomicMax /
 // atomicMin on floats held in shared memory).
@@ -85,6 +93,7 @@ constexpr int PF_OVERFLOW = 1, PF_CHAIN = 2;
 
 struct ScanShared {
     float hlb[HLB_N];
+    Cell cel[SCREEN_WARPS][32];  // a row's cells, 32 at a time
     Entry ent[SCREEN_WARPS][32];
     BranchTab br[SCREEN_WARPS];
     WarpPoints pt[SCREEN_WARPS];
@@ -143,8 +152,9 @@ __device__ __forceinline__ int prune_list(const DropCtx& ctx, uint32_t self, int
 //   PH_COLLECT  collect everything reaching thr, noting branch thresholds
 //               below it that are not decided (chains).
 // KIND: 0 cyl/ball/bull, 1 cone, 2 composite; CK: the cutter kind for KIND
-// 0/1 (a compile-time constant, so each kernel carries one contact model).
-template <int KIND, int CK>
+// 0/1 (a compile-time constant, so each kernel carries one contact model);
+// SPARSE: the kernel for warps whose points are spread out.
+template <int KIND, int CK, bool SPARSE>
 __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool active,
                                            uint32_t base, double xmin, double xmax, double ymin, double ymax) {
     const int lane = threadIdx.x & 31;
@@ -180,6 +190,12 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     P.flags[lane] = (ls.overflow ? PF_OVERFLOW : 0) | (ls.chain ? PF_CHAIN : 0);
     const float cx = P.cx[lane], cy = P.cy[lane], z0l = P.z0l[lane];
     unsigned long long screened = 0;
+    // a single point in this pass (the per-point scans of a scattered warp)
+    int solo = -1;
+    if (SPARSE) {
+        const unsigned am = __ballot_sync(0xffffffffu, active);
+        if (__popc(am) == 1) solo = __ffs(am) - 1;
+    }
     __syncwarp();
     for (int L = g.nlev - 1; L >= 0; --L) {
         int c0, c1, r0, r1;
@@ -195,9 +211,29 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
             if (P.pending[lane] == 0) active = false;
             if (!__any_sync(0xffffffffu, active)) goto done;
         }
-        for (int kc = 0; kc < ncl; ++kc) {
-            const int c = centre_out(kc, cc, c0, c1);
-            const Cell cell = cells[r * ncol + c];
+        for (int kc0 = 0; kc0 < ncl; kc0 += 32) {
+            const int nck = min(32, ncl - kc0);
+            __syncwarp();
+            if (lane < nck) sh.cel[wl][lane] = cells[r * ncol + centre_out(kc0 + lane, cc, c0, c1)];
+            __syncwarp();
+            unsigned cmask = nck == 32 ? 0xffffffffu : ((1u << nck) - 1u);
+            if (solo >= 0) {
+                // one point: each lane culls one of the staged cells for it
+                const float scut = __shfl_sync(0xffffffffu, (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr, solo);
+                const float sx = __shfl_sync(0xffffffffu, cx, solo), sy = __shfl_sync(0xffffffffu, cy, solo);
+                bool keep = false;
+                if (lane < nck) {
+                    const Cell& cl = sh.cel[wl][lane];
+                    const float ex = fmaxf(0.0f, fmaxf(cl.minx - sx, sx - cl.maxx));
+                    const float ey = fmaxf(0.0f, fmaxf(cl.miny - sy, sy - cl.maxy));
+                    const float de = sqrtf(ex * ex + ey * ey);
+                    keep = cl.count > 0 && de <= Rg && cl.maxz - hlb_at(sh.hlb, de - gd, inv_step) >= scut - gd;
+                }
+                cmask = __ballot_sync(0xffffffffu, keep);
+            }
+        for (; cmask; cmask &= cmask - 1) {
+            const int kk = __ffs(cmask) - 1;
+            const Cell cell = sh.cel[wl][kk];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
             const float cut = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
@@ -333,6 +369,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
             }
         }
+        }
     }
     }
 done:
@@ -349,6 +386,29 @@ done:
     __syncwarp();
 }
 
+// One pass for the warp: over the common rectangle of its points, or, for
+// scattered points, over each point's own rectangle in turn (for that point).
+template <int KIND, int CK, bool SPARSE>
+__device__ __forceinline__ void scan_warp(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls, bool act,
+                                          uint32_t base, double x, double y, bool scattered, double xmin, double xmax,
+                                          double ymin, double ymax) {
+    const int lane = threadIdx.x & 31;
+    if (!SPARSE) {
+        scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act, base, xmin, xmax, ymin, ymax);
+        return;
+    }
+    const unsigned want = __ballot_sync(0xffffffffu, act);
+    for (int o = 0; o < (scattered ? 32 : 1); ++o) {
+        if (scattered && !((want >> o) & 1u)) continue;
+        double x0 = xmin, x1 = xmax, y0 = ymin, y1 = ymax;
+        if (scattered) {
+            x0 = x1 = __shfl_sync(0xffffffffu, x, o);
+            y0 = y1 = __shfl_sync(0xffffffffu, y, o);
+        }
+        scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act && (!scattered || lane == o), base, x0, x1, y0, y1);
+    }
+}
+
 // Screen kernel.  KIND 0: one pass.  KIND 1/2 (cone, composite): the effect
 // of a triangle on the running height can depend on the height reached before
 // it (tip/rim short-circuits), so
@@ -360,16 +420,69 @@ done:
 //   then    a branch still undecided is checked exactly by the refinement
 //           (the triangle is flagged in the list), or, for untracked ones, the
 //           list is collected again at the lowest open branch threshold.
+// A certified lower bound of a point's result from the triangles of its own
+// finest-level cells (the 2 x 2 cells whose triangles may contain it).  Used
+// for warps whose points are spread out: the common scan order reaches most
+// of them late, so their bounds would rise late and cull little.
 template <int KIND, int CK>
-__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
-    k_drop_screen(const __grid_constant__ DropCtx ctx) {
-    __shared__ ScanShared sh;
-    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
-    __syncthreads();
+__device__ __forceinline__ float seed_blo(const DropCtx& ctx, double x, double y, bool active, float z0l) {
+    const GridP& g = ctx.g;
+    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
+    Prof32 prof = ctx.prof;
+    prof.kind = CK;
+    Comp32 comp = ctx.comp;
+    if (KIND == 2 && CK >= 0) {
+        comp.nsub = CK >> 16;
+#pragma unroll
+        for (int k = 0; k < OCL_GB300_MAX_SUB; ++k) comp.sub[k].kind = (CK >> (4 * k)) & 15;
+    }
+    float blo = z0l;
+    const int c = clampi((int)floor((x - g.x0) * g.inv_cs[0]), 0, g.ncol[0] - 1);
+    const int r = clampi((int)floor((y - g.y0) * g.inv_cs[0]), 0, g.nrow[0] - 1);
+    for (int q = 0; q < 4; ++q) {
+        const int cq = c - (q & 1), rq = r - (q >> 1);
+        uint32_t start = 0, cnt = 0;
+        if (active && cq >= 0 && rq >= 0) {
+            const Cell cell = ctx.cells[g.cell_off[0] + rq * g.ncol[0] + cq];
+            start = cell.start;
+            cnt = min(cell.count, 8u);
+        }
+        uint32_t most = cnt;
+        for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+        for (uint32_t k = 0; k < most; ++k) {
+            if (k >= cnt) continue;
+            const Tri32 t = ctx.t32[start + k];
+            float qt, qth;
+            Iv v = (KIND == 2) ? screen_composite(comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth)
+                               : screen_triangle(prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
+            if (v.lo > NEG_INF32) blo = fmaxf(blo, v.lo + t.v0[2] - ctx.E);
+        }
+    }
+    return blo;
+}
+
+// One warp per 32 sorted points: seeds the bounds of spread-out warps into
+// ctx.blo (the screen starts from them); other warps get the start height.
+template <int KIND, int CK>
+__global__ void __launch_bounds__(128) k_drop_seed(const __grid_constant__ DropCtx ctx) {
+    const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    if (base >= ctx.M) return;
+    const int lane = threadIdx.x & 31;
+    const bool active = base + lane < ctx.M;
+    const uint32_t i = (uint32_t)(active ? base + lane : base);
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1];
+    const float z0l = __double2float_rd(ctx.cl[3 * i + 2] - ctx.g.oz);
+    const double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
+    const double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
+    float blo = z0l;
+    if ((xmax - xmin) + (ymax - ymin) > ctx.cp.radius) blo = seed_blo<KIND, CK>(ctx, x, y, active, z0l);
+    if (active) ctx.blo[i] = blo;
+}
+
+template <int KIND, int CK, bool SPARSE>
+__device__ __forceinline__ void screen_warp(const DropCtx& ctx, ScanShared& sh, const int base) {
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
-    const int base = (blockIdx.x * SCREEN_WARPS + wl) * 32;
-    if (base >= ctx.M) return;
     const bool active = base + lane < ctx.M;
     const uint32_t i = (uint32_t)(active ? base + lane : base);
     const GridP& g = ctx.g;
@@ -395,7 +508,25 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK)
     ls.screened = 0;
     double xmin = warp_mind(active ? x : 1e300), xmax = warp_maxd(active ? x : -1e300);
     double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
-    scan_cells<KIND, CK>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, xmin, xmax, ymin, ymax);
+    // scattered points (their common rectangle is larger than their own
+    // rectangles together, e.g. sparse path samples): each point's rectangle
+    // is scanned in turn instead
+    bool scattered;
+    {
+        const double reach = 2.0 * ctx.cp.radius + 2.0 * ctx.g.cs[0];
+        const double own = active ? reach * reach : 0.0;
+        double sum_own = own;
+        for (int o = 16; o > 0; o >>= 1) sum_own += __shfl_xor_sync(0xffffffffu, sum_own, o);
+        scattered = (xmax - xmin + reach) * (ymax - ymin + reach) > sum_own;
+    }
+    if (!SPARSE && scattered) {
+        // scattered points go to the sparse kernel
+        if (lane == 0) ctx.sparse_list[atomicAdd(ctx.sparse_n, 1ull)] = (uint32_t)(base >> 5);
+        return;
+    }
+    // the seeding kernel's bound (spread-out warps), else the start height
+    if (ctx.seeded && active) ls.blo = fmaxf(ls.blo, ctx.blo[i]);
+    scan_warp<KIND, CK, SPARSE>(ctx, sh, PH_SINGLE, ls, active, (uint32_t)base, x, y, scattered, xmin, xmax, ymin, ymax);
     ls.thr = ls.blo;
     if (KIND != 0) {
         uint32_t* lt = ctx.cand + (size_t)i * ctx.cand_cap;
@@ -441,7 +572,8 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK)
                 if ((ls.pending >> j) & 1u) cut = fminf(cut, br.qlo[j][lane]);
             ls.thr = cut;
             const unsigned was = ls.pending;
-            scan_cells<KIND, CK>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, xmin, xmax, ymin, ymax);
+            scan_warp<KIND, CK, SPARSE>(ctx, sh, PH_RESOLVE, ls, ls.pending != 0, (uint32_t)base, x, y, scattered, xmin, xmax,
+                                ymin, ymax);
             for (int j = 0; j < ls.nb; ++j) {
                 if (!((was >> j) & 1u)) continue;
                 const unsigned long long wp = br.Wp[j][lane];
@@ -491,7 +623,8 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK)
                     ls.chain = false;
                     ls.chain_thr = 3.0e38f;
                 }
-                scan_cells<KIND, CK>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, xmin, xmax, ymin, ymax);
+                scan_warp<KIND, CK, SPARSE>(ctx, sh, PH_COLLECT, ls, active && !done, (uint32_t)base, x, y, scattered, xmin,
+                                    xmax, ymin, ymax);
                 ls.thr = keep_thr;
                 const bool again = !done && ls.chain && !ls.overflow && round < 3;
                 if (again) ls.thr = fminf(ls.thr, ls.chain_thr);
@@ -552,6 +685,24 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK)
     unsigned long long scr = ls.screened;
     for (int o = 16; o > 0; o >>= 1) scr += __shfl_xor_sync(0xffffffffu, scr, o);
     if (lane == 0 && scr) atomicAdd(&ctx.counters[C_SCREENED], scr);
+}
+
+template <int KIND, int CK, bool SPARSE>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
+    k_drop_screen(const __grid_constant__ DropCtx ctx) {
+    __shared__ ScanShared sh;
+    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = ctx.hlb[k];
+    __syncthreads();
+    const int wl = threadIdx.x >> 5;
+    if (!SPARSE) {
+        const int base = (blockIdx.x * SCREEN_WARPS + wl) * 32;
+        if (base < ctx.M) screen_warp<KIND, CK, SPARSE>(ctx, sh, base);
+        return;
+    }
+    // the warps the dense kernel handed over (count on the device)
+    const unsigned long long n = *ctx.sparse_n;
+    for (unsigned long long w = blockIdx.x * SCREEN_WARPS + wl; w < n; w += (unsigned long long)gridDim.x * SCREEN_WARPS)
+        screen_warp<KIND, CK, SPARSE>(ctx, sh, (int)(ctx.sparse_list[w] << 5));
 }
 
 

@@ -6,10 +6,10 @@ namespace oclg {
 void screen_launch_basic(const DropCtx& h, int kind, unsigned blocks, cudaStream_t stream) {
     const dim3 tb(SCREEN_WARPS * 32);
     switch (kind) {
-    case OCL_CUTTER_CONE: k_drop_screen<1, OCL_CUTTER_CONE><<<blocks, tb, 0, stream>>>(h); break;
-    case OCL_CUTTER_CYL: k_drop_screen<0, OCL_CUTTER_CYL><<<blocks, tb, 0, stream>>>(h); break;
-    case OCL_CUTTER_BALL: k_drop_screen<0, OCL_CUTTER_BALL><<<blocks, tb, 0, stream>>>(h); break;
-    default: k_drop_screen<0, OCL_CUTTER_BULL><<<blocks, tb, 0, stream>>>(h); break;
+    case OCL_CUTTER_CONE: k_drop_screen<1, OCL_CUTTER_CONE, false><<<blocks, tb, 0, stream>>>(h); break;
+    case OCL_CUTTER_CYL: k_drop_screen<0, OCL_CUTTER_CYL, false><<<blocks, tb, 0, stream>>>(h); break;
+    case OCL_CUTTER_BALL: k_drop_screen<0, OCL_CUTTER_BALL, false><<<blocks, tb, 0, stream>>>(h); break;
+    default: k_drop_screen<0, OCL_CUTTER_BULL, false><<<blocks, tb, 0, stream>>>(h); break;
     }
 }
 

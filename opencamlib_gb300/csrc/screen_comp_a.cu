@@ -5,8 +5,8 @@ namespace oclg {
 
 bool screen_launch_comp_a(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream) {
     const dim3 tb(SCREEN_WARPS * 32);
-    if (sig == SIG_BALLCONE) k_drop_screen<2, SIG_BALLCONE><<<blocks, tb, 0, stream>>>(h);
-    else if (sig == SIG_BULLCONE) k_drop_screen<2, SIG_BULLCONE><<<blocks, tb, 0, stream>>>(h);
+    if (sig == SIG_BALLCONE) k_drop_screen<2, SIG_BALLCONE, false><<<blocks, tb, 0, stream>>>(h);
+    else if (sig == SIG_BULLCONE) k_drop_screen<2, SIG_BULLCONE, false><<<blocks, tb, 0, stream>>>(h);
     else return false;
     return true;
 }

@@ -1,10 +1,15 @@
-// screen_comp_any.cu -- FP32 screen kernel of any other composite cutter.
+// screen_comp_any.cu -- FP32 screen kernels of any other composite cutter (dense and spread-out warps).
 #include "screen.cuh"
 
 namespace oclg {
 
 void screen_launch_comp_any(const DropCtx& h, unsigned blocks, cudaStream_t stream) {
-    k_drop_screen<2, -1><<<blocks, dim3(SCREEN_WARPS * 32), 0, stream>>>(h);
+    k_drop_screen<2, -1, false><<<blocks, dim3(SCREEN_WARPS * 32), 0, stream>>>(h);
+}
+
+void screen_launch_comp_any_sparse(const DropCtx& h, unsigned blocks, cudaStream_t stream, int stage) {
+    if (stage == 0) k_drop_seed<2, -1><<<blocks, dim3(SCREEN_WARPS * 32), 0, stream>>>(h);
+    else k_drop_screen<2, -1, true><<<blocks, dim3(SCREEN_WARPS * 32), 0, stream>>>(h);
 }
 
 }  // namespace oclg
