@@ -509,12 +509,19 @@ __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx,
         const Prof32& s = c.sub[n];
         const float zo = c.zoff[n];
         const float wlo = (n == 0 ? 0.0f : c.rlim[n - 1]) - 1e-6f, whi = c.rlim[n] + 1e-6f;
-#pragma unroll
+        // one copy of the contact model per sub-cutter (instruction cache):
+        // the edges' end points are selected, not indexed
+#pragma unroll 1
         for (int e = 0; e < 3; ++e) {
             if (t.flags & (TF_EDGE0_SKIP << e)) continue;
-            const int k = (e + 1) % 3;
+            const float ax = e == 0 ? 0.0f : (e == 1 ? t.e1[0] : t.e2[0]);
+            const float ay = e == 0 ? 0.0f : (e == 1 ? t.e1[1] : t.e2[1]);
+            const float az = e == 0 ? 0.0f : (e == 1 ? t.e1[2] : t.e2[2]);
+            const float bx = e == 0 ? t.e1[0] : (e == 1 ? t.e2[0] : 0.0f);
+            const float by = e == 0 ? t.e1[1] : (e == 1 ? t.e2[1] : 0.0f);
+            const float bz = e == 0 ? t.e1[2] : (e == 1 ? t.e2[2] : 0.0f);
             const bool horiz = (t.flags & (TF_EDGE0_HORIZ << e)) != 0;
-            Iv v = edge32(s, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, E, horiz, wlo, whi);
+            Iv v = edge32(s, ax, ay, az, bx, by, bz, wx, wy, E, horiz, wlo, whi);
             if (v.hi > NEG_INF32) ohi = fmaxf(ohi, v.hi - zo + E);
         }
     }
