@@ -210,25 +210,51 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
     const Tri64& t = ctx.t64[tri];
     if (!(overlaps64(ctx.cp.radius, cl.x, cl.y, t) && cl.z < t.bb[5])) return;
     uint32_t fl = ctx.t32[tri].flags;
-    uint32_t sub_skip = 0;
+    uint32_t sub_skip = 0, part_skip = 0;
     if (ctx.composite_screen) {
-        // a sub-cutter's edge contact at or below the running height cannot
-        // lift the sub-cutter's drop (its window is tested on what lifts), so
-        // edges whose FP32 upper bound lies below it are left out
+        // Parts whose FP32 upper bound lies below the running height cannot
+        // lift it and are left out of the FP64 evaluation:
+        //   a vertex (composite profile);
+        //   a sub-cutter's facet drop, when none of its facet contacts that
+        //   may lie in its radius window can (only such a contact lifts);
+        //   a sub-cutter's edge (the edge drop keeps the highest of its
+        //   edges, and the window is tested on that one: an edge below the
+        //   running height never becomes it);
+        //   a sub-cutter's whole edge drop, when none of its edges' contacts
+        //   that may lie in its window can lift.
         const Tri32 t3 = ctx.t32[tri];
         const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
         const float zr = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2];
+        const float lim = zr - ctx.guard - 2.0f * ctx.E;
         const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
         const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
         const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float dx = px[k] - wx, dy = py[k] - wy;
+            const float qlo = sqrtf(dx * dx + dy * dy) - ctx.E;
+            if (qlo > ctx.comp.R || pz[k] - hcomp32(ctx.comp, fmaxf(qlo, 0.0f)) + ctx.E < lim) part_skip |= 1u << k;
+        }
         for (int n = 0; n < ctx.comp.nsub; ++n) {
+            if (comp_facet_hi32(ctx.comp, t3, n, wx, wy, ctx.E) < lim) part_skip |= 1u << (8 + n);
+            const float zo = ctx.comp.zoff[n];
+            const float wlo = (n == 0 ? 0.0f : ctx.comp.rlim[n - 1]) - 1e-6f, whi = ctx.comp.rlim[n] + 1e-6f;
+            bool any_in_window = false;
             for (int e = 0; e < 3; ++e) {
                 if (fl & (TF_EDGE0_SKIP << e)) continue;
                 const int k = (e + 1) % 3;
-                Iv v = edge32(ctx.comp.sub[n], px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E,
-                              (fl & (TF_EDGE0_HORIZ << e)) != 0);
-                if (v.hi - ctx.comp.zoff[n] + 2.0f * ctx.E < zr - ctx.guard) sub_skip |= 1u << (3 * n + e);
+                const bool horiz = (fl & (TF_EDGE0_HORIZ << e)) != 0;
+                Iv v = edge32(ctx.comp.sub[n], px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E, horiz);
+                if (v.hi - zo < lim) {
+                    sub_skip |= 1u << (3 * n + e);
+                    continue;
+                }
+                if (!any_in_window) {
+                    v = edge32(ctx.comp.sub[n], px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E, horiz, wlo, whi);
+                    any_in_window = !(v.hi - zo < lim);
+                }
             }
+            if (!any_in_window) sub_skip |= 7u << (3 * n);
         }
     } else {
         // an edge whose FP32 upper bound is below the running height cannot
@@ -247,8 +273,15 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
                           (fl & (TF_EDGE0_HORIZ << e)) != 0);
             if (v.hi + ctx.E < zr - ctx.guard) fl |= (TF_EDGE0_SKIP << e);
         }
+        // a vertex whose FP32 upper bound is below the running height cannot
+        // lift it (the running height, not the floor: vertices come before
+        // the edges and after a facet drop that did not lift)
+        const float lim = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2] - ctx.guard - ctx.E;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (vertex32(ctx.prof, px[k] - wx, py[k] - wy, pz[k], ctx.E).hi < lim) part_skip |= 1u << k;
     }
-    drop_triangle64(ctx.cp, cl, t, fl, &capped, sub_skip);
+    drop_triangle64(ctx.cp, cl, t, fl, &capped, sub_skip, part_skip);
 }
 
 // ---------------------------------------------------------------------------
@@ -356,7 +389,13 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
     const BasicP& b = ctx.cp.b;
     if (!(cl.z < t.bb[5])) return;
     if (facet_drop_base(b, cl, t, fl)) return;
+    // vertices whose FP32 upper bound lies below the running height cannot lift it
+    const float vlim = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2] - ctx.guard - ctx.E;
+    const float vx[3] = {0.0f, t3.e1[0], t3.e2[0]};
+    const float vy[3] = {0.0f, t3.e1[1], t3.e2[1]};
+    const float vz[3] = {0.0f, t3.e1[2], t3.e2[2]};
     for (int k = 0; k < 3; ++k) {
+        if (vertex32(ctx.prof, vx[k] - wx, vy[k] - wy, vz[k], ctx.E).hi < vlim) continue;
         const D3 p = tri_p(t, k);
         const double q = xynorm(d3(cl.x, cl.y, cl.z) - p);
         if (q <= b.radius) liftz(cl, p.z - height_basic(b, q), p, OCL_CC_VERTEX);
@@ -530,7 +569,14 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
                 __syncthreads();
             }
         }
-        // fold in KD order (warp 0; every lane computes the same fold)
+        // fold in KD order (warp 0), 32 triangles at a time: every lane folds
+        // its own triangle from the running height; the first lane that lifts
+        // gives the next running height (the triangles before it did not lift
+        // from there, so the sequential fold passes them by).  A triangle that
+        // does not lift from a height does not lift from any higher one, so
+        // for the plain cutters only the later lanes that lifted fold again;
+        // a composite sub-cutter's facet can turn from a hidden contact to a
+        // lifting one as the height rises, so there every later lane does.
         if (tid < 32) {
             CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
             int capped = 0;
@@ -541,16 +587,30 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
                 const uint32_t slot = q < n ? (uint32_t)s_key[q] : 0u;
                 const float h = q < n ? s_hi[slot] : NEG_INF32;
                 const uint32_t tr = q < n ? s_tri[slot] : 0u;
-                unsigned m = __ballot_sync(0xffffffffu, h + gd >= __double2float_rd(cl.z - g.oz));
-                while (m) {
-                    const int b = __ffs(m) - 1;
-                    m &= m - 1;
-                    const float hb = __shfl_sync(0xffffffffu, h, b);
-                    const uint32_t tb = __shfl_sync(0xffffffffu, tr, b);
-                    if (hb + gd < __double2float_rd(cl.z - g.oz)) continue;  // passed by the rising height
-                    fold_one(ctx, cl, tb, cxl, cyl, capped);
-                    ++evals;
+                bool pend = q < n;
+                while (true) {
+                    const bool go = pend && h + gd >= __double2float_rd(cl.z - g.oz);
+                    if (!__any_sync(0xffffffffu, go)) break;
+                    CL64 mine = cl;
+                    if (go) {
+                        fold_one(ctx, mine, tr, cxl, cyl, capped);
+                        ++evals;
+                    }
+                    const bool lifted = go && mine.z > cl.z;
+                    const unsigned L = __ballot_sync(0xffffffffu, lifted);
+                    if (!L) break;
+                    const int b = __ffs(L) - 1;
+                    cl.z = __shfl_sync(0xffffffffu, mine.z, b);
+                    cl.cc.x = __shfl_sync(0xffffffffu, mine.cc.x, b);
+                    cl.cc.y = __shfl_sync(0xffffffffu, mine.cc.y, b);
+                    cl.cc.z = __shfl_sync(0xffffffffu, mine.cc.z, b);
+                    cl.type = __shfl_sync(0xffffffffu, mine.type, b);
+                    pend = go && lane > b && (COMP || lifted);
                 }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                evals += __shfl_xor_sync(0xffffffffu, evals, o);
+                capped += __shfl_xor_sync(0xffffffffu, capped, o);
             }
             if (lane == 0) {
                 const uint32_t o = ctx.perm[i];

@@ -675,4 +675,47 @@ __device__ inline Iv screen_composite(const Comp32& c, const Tri32& t, float wx,
     return r;
 }
 
+// Upper bound (composite frame, local to the triangle's first vertex) of the
+// facet contacts of sub-cutter n that may lift the composite: contacts that
+// may lie inside the triangle and in the sub-cutter's radius window, with the
+// error bounds of screen_composite.  Whatever contact the sub-cutter's facet
+// drop ends on, it lifts the composite only if it is one of these.
+__device__ inline float comp_facet_hi32(const Comp32& c, const Tri32& t, int n, float wx, float wy, float E) {
+    const uint32_t mode = t.flags & TF_FACET_MASK;
+    if (mode == TF_FACET_NONE) return NEG_INF32;
+    const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
+    const float nx = t.nn[0], ny = t.nn[1], nz = t.nn[2];
+    const float xyl = sqrtf(nx * nx + ny * ny);
+    const float slope = (mode == TF_FACET_HORIZ) ? 0.0f : (fabsf(nx) + fabsf(ny)) / nz;
+    const float ev = E * (3.0f + 2.0f * slope);
+    const Prof32& s = c.sub[n];
+    const float zo = c.zoff[n];
+    float hi = NEG_INF32;
+    if (s.kind == OCL_CUTTER_CONE) {
+        const float zt = (mode == TF_FACET_HORIZ) ? 0.0f : -(nx * wx + ny * wy) / nz;
+        if (inside32(t, wx, wy, eps_b) >= 0 && comp_window(c, n, 0.0f, 0.0f) >= 0) hi = zt - zo + ev;
+        if (mode == TF_FACET_GENERAL) {
+            const float rx = wx - s.R * nx / xyl, ry = wy - s.R * ny / xyl;
+            if (inside32(t, rx, ry, eps_b) >= 0 && comp_window(c, n, s.R, 1e-9f + s.R * 1e-9f) >= 0)
+                hi = fmaxf(hi, -(nx * rx + ny * ry) / nz - s.length - zo + ev);
+        }
+        return hi;
+    }
+    float ccx, ccy, tip, dist, ed;
+    if (mode == TF_FACET_HORIZ) {
+        ccx = wx; ccy = wy; tip = 0.0f;
+        dist = 0.0f;
+        ed = 0.0f;
+    } else {
+        const float xnx = nx / xyl, xny = ny / xyl;
+        const float rvx = s.xynl * xnx + s.nl * nx, rvy = s.xynl * xny + s.nl * ny, rvz = s.nl * nz;
+        ccx = wx - rvx; ccy = wy - rvy;
+        tip = -(nx * ccx + ny * ccy) / nz + rvz - s.center_height;
+        dist = s.xynl + s.nl * xyl;
+        ed = s.nl * xyl * 3e-7f + 1e-9f;
+    }
+    if (inside32(t, ccx, ccy, eps_b) >= 0 && comp_window(c, n, dist, ed) >= 0) hi = tip - zo + ev;
+    return hi;
+}
+
 }  // namespace oclg

@@ -424,11 +424,13 @@ __device__ __forceinline__ bool facet_drop_sub(const BasicP& c, CL64& cl, const 
 }
 
 // CompositeCutter::facetDrop / edgeDrop (compositecutter.cpp:152-193).
-// sub_skip bit 3n+e: edge e of sub-cutter n cannot lift it (left out).
+// sub_skip bit 3n+e: edge e of sub-cutter n cannot lift it (left out);
+// facet_skip bit n: no facet contact of sub-cutter n can lift the composite.
 __device__ inline bool comp_drop(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, bool facet, int* capped,
-                                 uint32_t sub_skip = 0) {
+                                 uint32_t sub_skip = 0, uint32_t facet_skip = 0) {
     bool result = false;
     for (int n = 0; n < c.nsub; ++n) {
+        if (facet ? ((facet_skip >> n) & 1u) : ((sub_skip >> (3 * n)) & 7u) == 7u) continue;
         CL64 tmp;
         tmp.x = cl.x;
         tmp.y = cl.y;
@@ -506,15 +508,18 @@ __device__ inline double branch_low64(const CutterP& c, double x, double y, cons
 }
 
 // MillingCutter::dropCutter for one triangle, from cl.z; cl is updated.
+// part_skip bit k (k < 3): vertex k cannot lift cl; bit 8 + n: no facet
+// contact of composite sub-cutter n can (both left out).
 __device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped,
-                                       uint32_t sub_skip = 0) {
+                                       uint32_t sub_skip = 0, uint32_t part_skip = 0) {
     if (!(cl.z < t.bb[5])) return;
     bool facet;
-    if (c.kind == OCL_CUTTER_COMPOSITE) facet = comp_drop(c, cl, t, flags, true, capped);
+    if (c.kind == OCL_CUTTER_COMPOSITE) facet = comp_drop(c, cl, t, flags, true, capped, 0, part_skip >> 8);
     else facet = facet_drop_sub(c.b, cl, t, flags);
     if (facet) return;
     // vertexDrop (millingcutter.cpp:36-47) with the cutter's height(r)
     for (int k = 0; k < 3; ++k) {
+        if ((part_skip >> k) & 1u) continue;
         D3 p = tri_p(t, k);
         double q = xynorm(d3(cl.x, cl.y, cl.z) - p);
         if (q <= c.radius) liftz(cl, p.z - height_any(c, q), p, OCL_CC_VERTEX);
