@@ -356,6 +356,180 @@ __device__ inline void bull_edges32(const Prof32& c, const float* px, const floa
     }
 }
 
+// One bull edge in the canonical frame of edge32: f(u) = az + (u - u1) m -
+// h(sqrt(u^2 + dm^2)) is concave on |u| < s, and the reference's contact is
+// its maximiser u* when that lies on the segment [u1, u2].  The FP64 CC lies
+// within Eu0 = E (3 + h'(rho)) + 1e-4 r2 of u*, so only u* in
+// [u1 - M, u2 + M] with M >= Eu0 can give a contact: the search bracket
+// [A, B] is that range (within the chord), and the whole chord where h' is
+// too steep near the segment for a short margin.
+struct BullEdge32 {
+    float u1, u2, m, dm, L, A, B, az;
+};
+
+// f'(u) times rho (same sign as f'; no division)
+__device__ __forceinline__ float bull_fp32(const Prof32& c, const BullEdge32& b, float u) {
+    const float rho = sqrtf(u * u + b.dm * b.dm);
+    return b.m * rho - dh32(c, rho) * u;
+}
+
+// Edge n of the triangle (local vertices px/py/pz); false: no contact.
+__device__ __forceinline__ bool bull_edge_setup32(const Prof32& c, float ax, float ay, float az, float bx, float by,
+                                                  float bz, float wx, float wy, float E, BullEdge32& b) {
+    const float dx = bx - ax, dy = by - ay;
+    b.L = sqrtf(dx * dx + dy * dy);
+    const float ux = dx / b.L, uy = dy / b.L;
+    const float qx = wx - ax, qy = wy - ay;
+    const float d = fabsf(ux * qy - uy * qx);
+    if (d - E > c.R) return false;
+    const float along = ux * qx + uy * qy;
+    b.u1 = -along;
+    b.u2 = b.L - along;
+    b.m = (bz - az) / b.L;
+    b.dm = fminf(d, c.R);
+    b.az = az;
+    // half chord of the disc at the largest line distance d may stand for
+    const float dl = fmaxf(d - E, 0.0f);
+    const float s = sqrtf(fmaxf(c.R * c.R - dl * dl, 0.0f));
+    const float r1 = sqrtf(b.u1 * b.u1 + b.dm * b.dm), r2 = sqrtf(b.u2 * b.u2 + b.dm * b.dm);
+    // rho on [u1 - M, u2 + M] stays below max(r1, r2) + M
+    const float M = E * (3.0f + dh32(c, fminf(fmaxf(r1, r2) + 4.0f * E + 0.01f, c.R))) + 1e-4f * c.r2 + 1e-3f;
+    if (M <= 0.01f) {
+        b.A = fmaxf(b.u1 - M, -s);
+        b.B = fminf(b.u2 + M, s);
+    } else {
+        b.A = -s;
+        b.B = s;
+    }
+    return b.A < b.B;
+}
+
+// true when the maximiser may lie in [A, B] (f' does not change sign outside)
+__device__ __forceinline__ bool bull_edge_open32(const Prof32& c, const BullEdge32& b) {
+    return !(bull_fp32(c, b, b.A) < 0.0f) && !(bull_fp32(c, b, b.B) > 0.0f);
+}
+
+// Bound of the edge contact with the maximiser bracketed in [A, B]: 8
+// bisection steps, one Newton step inside the bracket, the concave maximum
+// bounded by the tangent over the bracket (as bull_edges32).
+__device__ inline Iv bull_edge_solve32(const Prof32& c, const BullEdge32& b, float E) {
+    float lo_u = b.A, hi_u = b.B;
+    for (int it = 0; it < 8; ++it) {
+        const float mid = 0.5f * (lo_u + hi_u);
+        if (bull_fp32(c, b, mid) > 0) lo_u = mid; else hi_u = mid;
+    }
+    float ccu = 0.5f * (lo_u + hi_u);
+    {
+        const float rho = sqrtf(ccu * ccu + b.dm * b.dm);
+        const float q = rho - c.r1;
+        if (q > 0.0f && rho > 0.0f) {
+            const float a = fmaxf(c.r2 * c.r2 - q * q, 1e-30f);
+            const float ra = rsqrtf(a);
+            const float hp = q * ra, hpp = c.r2 * c.r2 * ra * ra * ra;
+            const float w = ccu / rho;
+            const float fp = b.m - hp * w;
+            const float fpp = -(hpp * w * w + hp * b.dm * b.dm / (rho * rho * rho));
+            if (fpp < 0.0f) ccu = fminf(fmaxf(ccu - fp / fpp, lo_u), hi_u);
+        }
+    }
+    const float rho = sqrtf(ccu * ccu + b.dm * b.dm);
+    const float clz = b.az + (ccu - b.u1) * b.m - h32(c, rho);
+    const float fpx = fabsf(b.m - dh32(c, rho) * (rho > 0 ? ccu / rho : 0.0f));
+    const float width = hi_u - lo_u;
+    const float slack = fminf(fpx * width, 1.0f);
+    const float rd = rho > 1e-20f ? b.dm / rho : 0.0f;
+    const float err = E * (3.0f + fabsf(b.m) + dh32(c, fminf(rho + E, c.R)) * (1.0f + rd)) + slack;
+    const float curv = 1.0f + dh32(c, fminf(rho + 4.0f * E, c.R));
+    const float Eu = E * (2.0f + curv) + 1e-4f * c.r2 + width;
+    const float tcc = (ccu - b.u1) / (b.u2 - b.u1);
+    const float et = (Eu + 1e-6f) / b.L;
+    int st = (tcc > et && tcc < 1 - et) ? 1 : ((tcc < -et || tcc > 1 + et) ? -1 : 0);
+    if (b.dm + E > c.R && st > 0) st = 0;
+    return gate(st, clz - err, clz + err);
+}
+
+// End points of edge n (0: v0-v1, 1: v1-v2, 2: v2-v0) of t, local frame,
+// selected rather than indexed.
+__device__ __forceinline__ void tri_edge32(const Tri32& t, int n, float& ax, float& ay, float& az, float& bx,
+                                           float& by, float& bz) {
+    ax = n == 0 ? 0.0f : (n == 1 ? t.e1[0] : t.e2[0]);
+    ay = n == 0 ? 0.0f : (n == 1 ? t.e1[1] : t.e2[1]);
+    az = n == 0 ? 0.0f : (n == 1 ? t.e1[2] : t.e2[2]);
+    bx = n == 0 ? t.e1[0] : (n == 1 ? t.e2[0] : 0.0f);
+    by = n == 0 ? t.e1[1] : (n == 1 ? t.e2[1] : 0.0f);
+    bz = n == 0 ? t.e1[2] : (n == 1 ? t.e2[2] : 0.0f);
+}
+
+// Warp-collective bull screen, one (point, triangle) pair per lane (have:
+// the lane holds one; every lane of the warp calls it).  Same effect interval
+// as screen_triangle; the edges whose maximiser may lie on the segment are
+// gathered from all lanes and searched one per lane, so the warp runs the
+// bisection only for those (most edges' maximisers lie off the segment).
+__device__ inline Iv screen_bull_warp(const Prof32& c, const Tri32* __restrict__ t32, uint32_t tri, const Tri32& t,
+                                      float wx, float wy, float E, bool have) {
+    const int lane = threadIdx.x & 31;
+    Iv best = iv_none();
+    unsigned need = 0;  // bit n: edge n's maximiser may lie on the segment
+    if (have) {
+        const float eps_b = E * 4.0f * t.bary_scale + 1e-6f;
+        best = vertex32(c, -wx, -wy, 0.0f, E);
+        iv_max(best, vertex32(c, t.e1[0] - wx, t.e1[1] - wy, t.e1[2], E));
+        iv_max(best, vertex32(c, t.e2[0] - wx, t.e2[1] - wy, t.e2[2], E));
+        // one copy of the edge test (instruction cache): the edges' end
+        // points are selected, not indexed
+#pragma unroll 1
+        for (int n = 0; n < 3; ++n) {
+            if (t.flags & (TF_EDGE0_SKIP << n)) continue;
+            float ax, ay, az, bx, by, bz;
+            tri_edge32(t, n, ax, ay, az, bx, by, bz);
+            if (t.flags & (TF_EDGE0_HORIZ << n)) {
+                iv_max(best, edge32(c, ax, ay, az, bx, by, bz, wx, wy, E, true));
+                continue;
+            }
+            BullEdge32 b;
+            if (bull_edge_setup32(c, ax, ay, az, bx, by, bz, wx, wy, E, b) && bull_edge_open32(c, b)) need |= 1u << n;
+        }
+        iv_max(best, facet32(c, t, wx, wy, E, eps_b));
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, need & 1u);
+    const unsigned m1 = __ballot_sync(0xffffffffu, need & 2u);
+    const unsigned m2 = __ballot_sync(0xffffffffu, need & 4u);
+    const int c0 = __popc(m0), c01 = c0 + __popc(m1), total = c01 + __popc(m2);
+    const unsigned below = (1u << lane) - 1u;
+    // this lane's edges in the gathered order (n-major)
+    const int q0 = __popc(m0 & below), q1 = c0 + __popc(m1 & below), q2 = c01 + __popc(m2 & below);
+    for (int r0 = 0; r0 < total; r0 += 32) {
+        const int q = r0 + lane;
+        int n = 0, owner = lane;
+        if (q < total) {
+            if (q < c0) owner = __fns(m0, 0, q + 1);
+            else if (q < c01) { n = 1; owner = __fns(m1, 0, q - c0 + 1); }
+            else { n = 2; owner = __fns(m2, 0, q - c01 + 1); }
+        }
+        const uint32_t otri = __shfl_sync(0xffffffffu, tri, owner);
+        const float owx = __shfl_sync(0xffffffffu, wx, owner), owy = __shfl_sync(0xffffffffu, wy, owner);
+        Iv r = iv_none();
+        if (q < total) {
+            const Tri32 to = t32[otri];
+            float ax, ay, az, bx, by, bz;
+            tri_edge32(to, n, ax, ay, az, bx, by, bz);
+            BullEdge32 b;
+            bull_edge_setup32(c, ax, ay, az, bx, by, bz, owx, owy, E, b);
+            r = bull_edge_solve32(c, b, E);
+        }
+        // each owner takes its edges' results back
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int qk = k == 0 ? q0 : (k == 1 ? q1 : q2);
+            const bool mine = ((need >> k) & 1u) && qk >= r0 && qk < r0 + 32;
+            const int src = mine ? qk - r0 : lane;
+            const float lo = __shfl_sync(0xffffffffu, r.lo, src), hi = __shfl_sync(0xffffffffu, r.hi, src);
+            if (mine) iv_max(best, Iv{lo, hi});
+        }
+    }
+    return best;
+}
+
 // Whole-triangle screen for the basic cutters, local frame (relative to v0).
 // Returns the interval of the triangle's effect on the running z
 // (dropCutter applied to a CL point already at some height Z >= z0).

@@ -291,13 +291,18 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 P.msk[lane] = m;
                 P.pre[lane] = incl - cnt;
                 __syncwarp();
-                // 3. screen the marked pairs, 32 at a time
-                for (int k = lane; k < total; k += 32) {
+                // 3. screen the marked pairs, 32 at a time (the bull's
+                // screen is warp-collective: every lane takes part in every
+                // round, holding a pair or not)
+                constexpr bool WARP_SCREEN = KIND == 0 && CK == OCL_CUTTER_BULL;
+                for (int k0 = WARP_SCREEN ? 0 : lane; k0 < total; k0 += 32) {
+                    const int k = WARP_SCREEN ? k0 + lane : k0;
+                    const bool have = k < total;
                     int p = 0;
 #pragma unroll
                     for (int s = 16; s > 0; s >>= 1)
                         if (p + s < 32 && P.pre[p + s] <= k) p += s;
-                    const int jj = __fns(P.msk[p], 0, k - P.pre[p] + 1);
+                    const int jj = have ? __fns(P.msk[p], 0, k - P.pre[p] + 1) : 0;
                     const Entry& e = sh.ent[wl][jj];
                     const float px = P.cx[p], py = P.cy[p], pz0 = P.z0l[p];
                     const float ub = e.maxz;  // refined below by the screen
@@ -305,11 +310,14 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     uint32_t rank;
                     {
                         const Tri32 t = ctx.t32[e.tri];
-                        Iv v = (KIND == 2)
-                                   ? screen_composite(comp, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
-                                                      qt, qth)
-                                   : screen_triangle(prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2],
-                                                     qt, qth);
+                        Iv v;
+                        if (WARP_SCREEN)
+                            v = screen_bull_warp(prof, ctx.t32, e.tri, t, px - t.v0[0], py - t.v0[1], ctx.E, have);
+                        else if (KIND == 2)
+                            v = screen_composite(comp, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2], qt, qth);
+                        else
+                            v = screen_triangle(prof, t, px - t.v0[0], py - t.v0[1], ctx.E, pz0 - t.v0[2], qt, qth);
+                        if (!have) continue;
                         ++screened;
                         lo = v.lo > NEG_INF32 ? v.lo + t.v0[2] - ctx.E : NEG_INF32;
                         hi = v.hi > NEG_INF32 ? fminf(v.hi + t.v0[2] + ctx.E, ub + gd) : NEG_INF32;
