@@ -394,6 +394,15 @@ done:
     __syncwarp();
 }
 
+// The cone and composite kernels run three phases of scan_cells; one
+// out-of-line copy serves them all (instruction cache).
+template <int KIND, int CK, bool SPARSE>
+__device__ __noinline__ void scan_cells_shared(const DropCtx& ctx, ScanShared& sh, int phase, LaneState& ls,
+                                               bool active, uint32_t base, double xmin, double xmax, double ymin,
+                                               double ymax) {
+    scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, active, base, xmin, xmax, ymin, ymax);
+}
+
 // One pass for the warp: over the common rectangle of its points, or, for
 // scattered points, over each point's own rectangle in turn (for that point).
 template <int KIND, int CK, bool SPARSE>
@@ -402,7 +411,8 @@ __device__ __forceinline__ void scan_warp(const DropCtx& ctx, ScanShared& sh, in
                                           double ymin, double ymax) {
     const int lane = threadIdx.x & 31;
     if (!SPARSE) {
-        scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act, base, xmin, xmax, ymin, ymax);
+        if (KIND == 0) scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act, base, xmin, xmax, ymin, ymax);
+        else scan_cells_shared<KIND, CK, SPARSE>(ctx, sh, phase, ls, act, base, xmin, xmax, ymin, ymax);
         return;
     }
     const unsigned want = __ballot_sync(0xffffffffu, act);
@@ -413,7 +423,8 @@ __device__ __forceinline__ void scan_warp(const DropCtx& ctx, ScanShared& sh, in
             x0 = x1 = __shfl_sync(0xffffffffu, x, o);
             y0 = y1 = __shfl_sync(0xffffffffu, y, o);
         }
-        scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act && (!scattered || lane == o), base, x0, x1, y0, y1);
+        if (KIND == 0) scan_cells<KIND, CK, SPARSE>(ctx, sh, phase, ls, act && (!scattered || lane == o), base, x0, x1, y0, y1);
+        else scan_cells_shared<KIND, CK, SPARSE>(ctx, sh, phase, ls, act && (!scattered || lane == o), base, x0, x1, y0, y1);
     }
 }
 
