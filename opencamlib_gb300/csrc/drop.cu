@@ -292,12 +292,17 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
 // one edge per thread (k_bull_eval: whole warps run the same search), and the
 // fold reads the results in its own order.
 // ---------------------------------------------------------------------------
+// FP32 upper bound of a bull edge's contact (the screen's bound: an edge
+// whose maximiser cannot lie on the segment gives none, else the bracketed
+// search); the plan and the fold compute it alike.
 __device__ __forceinline__ float bull_edge_hi(const DropCtx& ctx, const Tri32& t3, int e, float wx, float wy) {
-    const float px[3] = {0.0f, t3.e1[0], t3.e2[0]};
-    const float py[3] = {0.0f, t3.e1[1], t3.e2[1]};
-    const float pz[3] = {0.0f, t3.e1[2], t3.e2[2]};
-    const int k = (e + 1) % 3;
-    return edge32(ctx.prof, px[e], py[e], pz[e], px[k], py[k], pz[k], wx, wy, ctx.E, false).hi;
+    Prof32 c = ctx.prof;
+    c.kind = OCL_CUTTER_BULL;
+    float ax, ay, az, bx, by, bz;
+    tri_edge32(t3, e, ax, ay, az, bx, by, bz);
+    BullEdge32 b;
+    if (!bull_edge_setup32(c, ax, ay, az, bx, by, bz, wx, wy, ctx.E, b) || !bull_edge_open32(c, b)) return NEG_INF32;
+    return bull_edge_solve32(c, b, ctx.E).hi;
 }
 
 __global__ void __launch_bounds__(128) k_bull_plan(const __grid_constant__ DropCtx ctx, uint2* __restrict__ queue,
@@ -386,7 +391,8 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
         if (hi[e] + ctx.E < zf - ctx.guard) continue;
         k_of[e] = slot++;
     }
-    const BasicP& b = ctx.cp.b;
+    BasicP b = ctx.cp.b;
+    b.kind = OCL_CUTTER_BULL;  // one contact model in the kernel
     if (!(cl.z < t.bb[5])) return;
     if (facet_drop_base(b, cl, t, fl)) return;
     // vertices whose FP32 upper bound lies below the running height cannot lift it
@@ -423,6 +429,9 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
 // dropCutter5 does over its KD candidates.  Triangles left out can neither
 // reach the final height nor change a branch choice of a collected triangle.
 // ---------------------------------------------------------------------------
+// BULL_PLAN: the bull with its edges evaluated ahead (fold_bull only); else
+// every other case (fold_one only), so each kernel carries one fold.
+template <bool BULL_PLAN>
 __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ DropCtx ctx) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (uint32_t)ctx.M) return;
@@ -440,7 +449,7 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     const int nplan = ctx.edge_res ? ctx.edge_n[i] : 0;
     for (int q = 0; q < n; ++q) {
         const uint32_t tq = tri[q] & ~CAND_VERIFY;
-        if (ctx.edge_res) {
+        if (BULL_PLAN) {
             fold_bull(ctx, cl, i, tq, cxl, cyl, zfloor, slot, nplan, capped);
             continue;
         }
@@ -814,7 +823,7 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         CK(cudaMemsetAsync(w.ncand.p, 0, M * sizeof(uint16_t), stream));
         CK(cudaMemsetAsync(w.blo.p, 0xFF, M * sizeof(float), stream));
         CK(cudaEventRecord(ev[2], stream));
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
+        k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
         CK(cudaEventRecord(ev[3], stream));
         launches += 1;
     } else if (precision == OCL_GB300_PREC_FP64) {
@@ -836,7 +845,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
             k_bull_eval<<<eb, 128, 0, stream>>>(*h, w.edge_queue.p, w.counters.p + C_EDGEQ);
             launches += 2;
         }
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
+        if (h->edge_res) k_drop_refine<true><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
+        else k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
         CK(cudaEventRecord(ev[3], stream));
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
         // the fallback grids stride over however many points were handed back
@@ -1016,11 +1026,11 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     if (m.n == 0) {
         CK(cudaMemsetAsync(sc->ncand, 0, M * sizeof(uint16_t), stream));
         CK(cudaMemsetAsync(sc->blo, 0xFF, M * sizeof(float), stream));
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+        k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
     } else {
         const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
         launch_screen(h, cp, sblocks, stream);
-        k_drop_refine<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+        k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
         k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
         st = launch_exact(h, composite, sc->list, sc->counters + C_FALLBACK, sc->list2, sc->counters + C_PLAIN,
                           (unsigned)std::min<uint64_t>(M, 152u * 3u), stream);
