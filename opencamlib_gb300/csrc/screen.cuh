@@ -15,7 +15,7 @@ constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 // resident screen blocks per SM the register allocation aims at (measured:
 // more warps hide the FP32 dependency chains until spills start to cost)
 constexpr int screen_min_blocks(int kind, int ck) {
-    return kind == 2 ? 5 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
+    return kind == 2 ? 4 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
 }
 
 enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
@@ -189,6 +189,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     P.resolved[lane] = ls.resolved;
     P.flags[lane] = (ls.overflow ? PF_OVERFLOW : 0) | (ls.chain ? PF_CHAIN : 0);
     const float cx = P.cx[lane], cy = P.cy[lane], z0l = P.z0l[lane];
+    const float lthr = ls.thr;  // kept in a register across the scan
     unsigned long long screened = 0;
     // a single point in this pass (the per-point scans of a scattered warp)
     int solo = -1;
@@ -219,7 +220,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
             unsigned cmask = nck == 32 ? 0xffffffffu : ((1u << nck) - 1u);
             if (solo >= 0) {
                 // one point: each lane culls one of the staged cells for it
-                const float scut = __shfl_sync(0xffffffffu, (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr, solo);
+                const float scut = __shfl_sync(0xffffffffu, (phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr, solo);
                 const float sx = __shfl_sync(0xffffffffu, cx, solo), sy = __shfl_sync(0xffffffffu, cy, solo);
                 bool keep = false;
                 if (lane < nck) {
@@ -236,7 +237,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
             const Cell cell = sh.cel[wl][kk];
             if (cell.count == 0) continue;
             // the threshold below which a triangle is of no interest in this phase
-            const float cut = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
+            const float cut = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr;
             float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
             float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
             float d = sqrtf(dx * dx + dy * dy);
@@ -250,7 +251,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 // 1. the entries this lane's point wants screened
                 unsigned m = 0;
                 if (pass) {
-                    const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : ls.thr;
+                    const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr;
                     for (int jj = 0; jj < nj; ++jj) {
                         const Entry& e = sh.ent[wl][jj];
                         float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
@@ -263,7 +264,7 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 const int cnt = __popc(m);
                 // 2. room in the point's list for what this chunk may add
                 if (phase != PH_RESOLVE && cnt && P.nc[lane] + cnt > cap && !(P.flags[lane] & PF_OVERFLOW)) {
-                    const float keep = (phase == PH_COLLECT) ? ls.thr : o2f(P.blo[lane]);
+                    const float keep = (phase == PH_COLLECT) ? lthr : o2f(P.blo[lane]);
                     P.nc[lane] = prune_list(ctx, base + lane, P.nc[lane], keep - gd);
                 }
                 if (KIND != 0 && phase == PH_SINGLE && P.nb[lane] >= NBRANCH) {
