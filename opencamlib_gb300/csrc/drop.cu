@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
 // ---------------------------------------------------------------------------
 constexpr int EXACT_CAP = 4096;
 constexpr int EXACT_THREADS = 256;
-constexpr size_t EXACT_SMEM = (size_t)EXACT_CAP * (8 + 4 + 4);
+constexpr size_t EXACT_SMEM = (size_t)EXACT_CAP * (8 + 4 + 4 + 4);
 
 template <bool COMP>
 __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_constant__ DropCtx ctx,
@@ -500,8 +500,9 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
     extern __shared__ unsigned long long s_key[];  // EXACT_CAP keys (KD rank << 32 | slot)
     uint32_t* s_tri = reinterpret_cast<uint32_t*>(s_key + EXACT_CAP);
     float* s_hi = reinterpret_cast<float*>(s_tri + EXACT_CAP);
+    float* s_qt = s_hi + EXACT_CAP;  // lowest branch threshold (+inf: none)
     __shared__ float s_hlb[HLB_N];
-    __shared__ int s_n;
+    __shared__ int s_n, s_red;
     for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
     const int tid = threadIdx.x, lane = tid & 31;
     const int nlist = (int)*nlist_dev;
@@ -547,6 +548,7 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
                         s_key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
                         s_tri[slot] = (uint32_t)e.tri;
                         s_hi[slot] = hi;
+                        s_qt[slot] = qt < 3.0e38f ? qt + t.v0[2] - ctx.E : 3.0e38f;
                     }
                 }
             }
@@ -558,6 +560,44 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
             __syncthreads();
             continue;
         }
+        // Only triangles whose upper bound reaches T are folded, T at most
+        // blo - guard (the final height lies above it) and at most every
+        // branch threshold of the triangles kept.  A triangle left out lifts
+        // the running height to below T at most; below its branch points a
+        // kept triangle's effect is max(Z, c) with a fixed c and CC; so
+        // max(Z, T) is the same in both folds after every triangle, and the
+        // final height, above T, is the same with its CC and type.
+        float T = NEG_INF32;
+        if (ctx.blo[i] > NEG_INF32) T = ctx.blo[i] - gd;
+        for (int it = 0; T > NEG_INF32; ++it) {
+            if (it == 64) {  // not settled: fold everything
+                T = NEG_INF32;
+                break;
+            }
+            if (tid == 0) s_red = f2o(3.0e38f);
+            __syncthreads();
+            float m = 3.0e38f;
+            for (int k = tid; k < n; k += blockDim.x)
+                if (s_hi[k] >= T && s_qt[k] - gd < T) m = fminf(m, s_qt[k] - gd);
+            if (m < 3.0e38f) atomicMin(&s_red, f2o(m));
+            __syncthreads();
+            const float mt = o2f(s_red);
+            __syncthreads();
+            if (!(mt < T)) break;
+            T = mt;
+        }
+        if (tid == 0) s_red = 0;
+        __syncthreads();
+        {
+            int kept = 0;
+            for (int k = tid; k < n; k += blockDim.x) {
+                if (s_hi[k] >= T) ++kept;
+                else s_key[k] = ~0ull;  // sorts after the kept keys
+            }
+            if (kept) atomicAdd(&s_red, kept);
+        }
+        __syncthreads();
+        const int nk = s_red;
         // bitonic sort of the keys (padded to a power of two)
         int np = 1;
         while (np < n) np <<= 1;
@@ -591,12 +631,12 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
             int capped = 0;
             unsigned evals = 0;
             const float cxl = cx, cyl = cy;
-            for (int q0 = 0; q0 < n; q0 += 32) {
+            for (int q0 = 0; q0 < nk; q0 += 32) {
                 const int q = q0 + lane;
-                const uint32_t slot = q < n ? (uint32_t)s_key[q] : 0u;
-                const float h = q < n ? s_hi[slot] : NEG_INF32;
-                const uint32_t tr = q < n ? s_tri[slot] : 0u;
-                bool pend = q < n;
+                const uint32_t slot = q < nk ? (uint32_t)s_key[q] : 0u;
+                const float h = q < nk ? s_hi[slot] : NEG_INF32;
+                const uint32_t tr = q < nk ? s_tri[slot] : 0u;
+                bool pend = q < nk;
                 while (true) {
                     const bool go = pend && h + gd >= __double2float_rd(cl.z - g.oz);
                     if (!__any_sync(0xffffffffu, go)) break;

@@ -97,3 +97,21 @@ def test_fallback_on_a_tilted_plate(ocl, oracle_lib):
         z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
         assert st.violations == 0
         _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
+
+
+def test_handed_back_points_on_the_bump_field(ocl):
+    # the 1,048,576-triangle bump field: cone and composite points whose
+    # branch checks fail are redone by the exact kernel, which folds only the
+    # triangles above a branch-safe threshold; mixed must equal plain FP64
+    tris = w.mesh_c2()
+    grid = w.raster_c2().reshape(1000, 1000, 3)
+    cl = np.concatenate([grid[i:i + 100, j:j + 100].reshape(-1, 3)
+                         for i, j in ((100, 100), (450, 600), (700, 250), (850, 850))])
+    mesh = ocl.DeviceMesh(tris)
+    handed_back = 0
+    for c in (cu.ConeCutter(6.0, math.pi / 4, 20.0), cu.BallConeCutter(2.0, 6.0, math.pi / 4)):
+        z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+        assert st.violations == 0
+        handed_back += st.fallback
+        _same((z, cc, ty), mesh.drop(c, cl, precision="fp64")[:3])
+    assert handed_back > 0
