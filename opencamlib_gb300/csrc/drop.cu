@@ -280,6 +280,11 @@ __device__ __forceinline__ void fold_one(const DropCtx& ctx, CL64& cl, uint32_t 
 #pragma unroll
         for (int k = 0; k < 3; ++k)
             if (vertex32(ctx.prof, px[k] - wx, py[k] - wy, pz[k], ctx.E).hi < lim) part_skip |= 1u << k;
+        // the same for the facet contact of cyl/ball/bull (one contact that
+        // lifts or not; the cone's tip/rim choice is left to the FP64 code)
+        if (ctx.prof.kind != OCL_CUTTER_CONE &&
+            facet32(ctx.prof, t3, wx, wy, ctx.E, ctx.E * 4.0f * t3.bary_scale + 1e-6f).hi < lim)
+            part_skip |= PART_SKIP_FACET;
     }
     drop_triangle64(ctx.cp, cl, t, fl, &capped, sub_skip, part_skip);
 }
@@ -394,9 +399,14 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
     BasicP b = ctx.cp.b;
     b.kind = OCL_CUTTER_BULL;  // one contact model in the kernel
     if (!(cl.z < t.bb[5])) return;
-    if (facet_drop_base(b, cl, t, fl)) return;
-    // vertices whose FP32 upper bound lies below the running height cannot lift it
+    // facet and vertices whose FP32 upper bound lies below the running height
+    // cannot lift it
     const float vlim = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2] - ctx.guard - ctx.E;
+    Prof32 pb = ctx.prof;
+    pb.kind = OCL_CUTTER_BULL;
+    if (!(facet32(pb, t3, wx, wy, ctx.E, ctx.E * 4.0f * t3.bary_scale + 1e-6f).hi < vlim) &&
+        facet_drop_base(b, cl, t, fl))
+        return;
     const float vx[3] = {0.0f, t3.e1[0], t3.e2[0]};
     const float vy[3] = {0.0f, t3.e1[1], t3.e2[1]};
     const float vz[3] = {0.0f, t3.e1[2], t3.e2[2]};

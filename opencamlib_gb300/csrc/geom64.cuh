@@ -509,13 +509,15 @@ __device__ inline double branch_low64(const CutterP& c, double x, double y, cons
 
 // MillingCutter::dropCutter for one triangle, from cl.z; cl is updated.
 // part_skip bit k (k < 3): vertex k cannot lift cl; bit 8 + n: no facet
-// contact of composite sub-cutter n can (both left out).
+// contact of composite sub-cutter n can; PART_SKIP_FACET: the facet contact
+// of a basic cutter cannot (all left out).
+constexpr uint32_t PART_SKIP_FACET = 1u << 16;
 __device__ inline void drop_triangle64(const CutterP& c, CL64& cl, const Tri64& t, uint32_t flags, int* capped,
                                        uint32_t sub_skip = 0, uint32_t part_skip = 0) {
     if (!(cl.z < t.bb[5])) return;
     bool facet;
     if (c.kind == OCL_CUTTER_COMPOSITE) facet = comp_drop(c, cl, t, flags, true, capped, 0, part_skip >> 8);
-    else facet = facet_drop_sub(c.b, cl, t, flags);
+    else facet = (part_skip & PART_SKIP_FACET) ? false : facet_drop_sub(c.b, cl, t, flags);
     if (facet) return;
     // vertexDrop (millingcutter.cpp:36-47) with the cutter's height(r)
     for (int k = 0; k < 3; ++k) {
