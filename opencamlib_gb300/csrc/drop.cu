@@ -387,14 +387,20 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
     const uint32_t fl = t3.flags;
     const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
     const float zf = zfloor - t3.v0[2];
-    float hi[3];
+    // the plan's slots in fold order: an edge is planned when it is the next
+    // stored slot; past the stored slots the plan's test is repeated
+    float hi[3] = {3.0e38f, 3.0e38f, 3.0e38f};
     int k_of[3] = {-1, -1, -1};
+    const uint32_t* slots = ctx.edge_slots + (size_t)i * EDGE_SLOTS;
     for (int e = 0; e < 3; ++e) {
-        hi[e] = NEG_INF32;
         if (fl & ((TF_EDGE0_SKIP | TF_EDGE0_HORIZ) << e)) continue;
-        hi[e] = bull_edge_hi(ctx, t3, e, wx, wy);
-        if (hi[e] + ctx.E < zf - ctx.guard) continue;
-        k_of[e] = slot++;
+        if (slot >= nplan) break;  // nothing planned from here on
+        if (slot < EDGE_SLOTS) {
+            if (slots[slot] == ((tq << 2) | (uint32_t)e)) k_of[e] = slot++;
+        } else {
+            hi[e] = bull_edge_hi(ctx, t3, e, wx, wy);
+            if (!(hi[e] + ctx.E < zf - ctx.guard)) k_of[e] = slot++;
+        }
     }
     BasicP b = ctx.cp.b;
     b.kind = OCL_CUTTER_BULL;  // one contact model in the kernel
@@ -421,15 +427,19 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
     for (int e = 0; e < 3; ++e) {
         if (fl & (TF_EDGE0_SKIP << e)) continue;
         const bool horiz = (fl & (TF_EDGE0_HORIZ << e)) != 0;
+        // an edge the plan left out cannot reach the floor: it cannot lift
+        // (a planned result at or below the running height lifts nothing)
+        if (!horiz && k_of[e] < 0) continue;
+        if (!horiz && k_of[e] < EDGE_SLOTS) {
+            const EdgeRes r = ctx.edge_res[(size_t)i * EDGE_SLOTS + k_of[e]];
+            if (r.valid) liftz(cl, r.clz, d3(r.ccx, r.ccy, r.ccz), OCL_CC_EDGE);
+            continue;
+        }
         if (!horiz && hi[e] + ctx.E < zr - ctx.guard) continue;  // cannot lift
         double clz;
         D3 cc;
-        if (!horiz && k_of[e] >= 0 && k_of[e] < EDGE_SLOTS && k_of[e] < nplan) {
-            const EdgeRes r = ctx.edge_res[(size_t)i * EDGE_SLOTS + k_of[e]];
-            if (r.valid) liftz(cl, r.clz, d3(r.ccx, r.ccy, r.ccz), OCL_CC_EDGE);
-        } else if (edge_contact64(b, cl.x, cl.y, tri_p(t, e), tri_p(t, (e + 1) % 3), clz, cc, &capped)) {
+        if (edge_contact64(b, cl.x, cl.y, tri_p(t, e), tri_p(t, (e + 1) % 3), clz, cc, &capped))
             liftz(cl, clz, cc, OCL_CC_EDGE);
-        }
     }
 }
 
