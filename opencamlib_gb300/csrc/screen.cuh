@@ -190,6 +190,11 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
     P.flags[lane] = (ls.overflow ? PF_OVERFLOW : 0) | (ls.chain ? PF_CHAIN : 0);
     const float cx = P.cx[lane], cy = P.cy[lane], z0l = P.z0l[lane];
     const float lthr = ls.thr;  // kept in a register across the scan
+    // the active points' rectangle and lowest start height: an entry that
+    // fails the cull against these fails it for every active point
+    const float rx0 = warp_min(active ? cx : 3.0e38f), rx1 = warp_max(active ? cx : -3.0e38f);
+    const float ry0 = warp_min(active ? cy : 3.0e38f), ry1 = warp_max(active ? cy : -3.0e38f);
+    const float zmin = warp_min(active ? z0l : 3.0e38f);
     unsigned long long screened = 0;
     // a single point in this pass (the per-point scans of a scattered warp)
     int solo = -1;
@@ -248,11 +253,26 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                 __syncwarp();
                 if (lane < nj) sh.ent[wl][lane] = ctx.entries[cell.start + j0 + lane];
                 __syncwarp();
-                // 1. the entries this lane's point wants screened
+                // 1. the entries this lane's point wants screened: one cull
+                // per entry against the whole warp (the points' rectangle,
+                // the lowest threshold), then each lane's own cull of the
+                // entries that pass it
+                const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr;
+                const float wcut = warp_min(pass ? cut2 : 3.0e38f);
+                bool want = false;
+                if (lane < nj) {
+                    const Entry& e = sh.ent[wl][lane];
+                    const float ex = fmaxf(0.0f, fmaxf(e.minx - rx1, rx0 - e.maxx));
+                    const float ey = fmaxf(0.0f, fmaxf(e.miny - ry1, ry0 - e.maxy));
+                    const float de = sqrtf(ex * ex + ey * ey);
+                    const float ub = e.maxz - hlb_at(sh.hlb, de - gd, inv_step);
+                    want = de <= Rg && ub >= wcut - gd && ub > zmin - gd;
+                }
+                const unsigned wmask = __ballot_sync(0xffffffffu, want);
                 unsigned m = 0;
                 if (pass) {
-                    const float cut2 = (phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr;
-                    for (int jj = 0; jj < nj; ++jj) {
+                    for (unsigned rest = wmask; rest; rest &= rest - 1) {
+                        const int jj = __ffs(rest) - 1;
                         const Entry& e = sh.ent[wl][jj];
                         float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
                         float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
