@@ -378,7 +378,9 @@ __global__ void __launch_bounds__(128) k_bull_eval(const __grid_constant__ DropC
 }
 
 // MillingCutter::dropCutter for a bull, edges from k_bull_eval where planned
-// (the plan test is repeated here to walk the point's slots in step).
+// (the fold walks the point's plan slots in step: an edge is planned when it
+// is the next stored slot; past the stored slots the plan's test is
+// repeated and the edge is evaluated here).
 __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t i, uint32_t tq, float cxl, float cyl,
                                           float zfloor, int& slot, int nplan, int& capped) {
     const Tri64& t = ctx.t64[tq];
