@@ -15,7 +15,7 @@ constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 // resident screen blocks per SM the register allocation aims at (measured:
 // more warps hide the FP32 dependency chains until spills start to cost)
 constexpr int screen_min_blocks(int kind, int ck) {
-    return kind == 2 ? 4 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
+    return kind != 0 ? 4 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
 }
 
 enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
