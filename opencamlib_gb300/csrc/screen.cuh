@@ -13,9 +13,12 @@ namespace oclg {
 constexpr int SCREEN_WARPS = 4;
 constexpr int NBRANCH = 4;  // branching triangles tracked per CL point
 // resident screen blocks per SM the register allocation aims at (measured:
-// more warps hide the FP32 dependency chains until spills start to cost)
+// more warps hide the FP32 dependency chains until spills start to cost;
+// the cone and composite kernels, with their out-of-line cell scan, run
+// best with the registers of four)
 constexpr int screen_min_blocks(int kind, int ck) {
-    return kind != 0 ? 4 : (ck == OCL_CUTTER_CYL || ck == OCL_CUTTER_BALL ? 6 : 5);
+    (void)ck;
+    return kind != 0 ? 4 : 6;
 }
 
 enum ScanPhase { PH_SINGLE = 0, PH_RESOLVE = 1, PH_COLLECT = 2 };
