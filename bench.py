@@ -431,6 +431,14 @@ def main():
             aux = aux_measurements(tris, cuts, not args.no_cpu_baseline)
         except Exception as e:  # reported, never required
             aux = {"error": str(e)}
+    compute = None
+    try:  # FP32 / FP64 FMA ceilings of this GPU (the compute bounds of the path)
+        from opencamlib_gb300 import _native
+        f32, f64 = _native.fma_peaks()
+        compute = {"fp32_tflops": f32, "fp64_tflops": f64,
+                   "source": "ocl_gb300_fma_peaks: 8 FMA chains per thread on a full-occupancy grid, this GPU"}
+    except Exception as e:  # reported, never required
+        compute = {"error": str(e)}
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -473,6 +481,7 @@ def main():
                              "stage in the timed region; the kernel is FP32-issue and latency bound, not HBM-bound "
                              "(traffic: ncu DRAM bytes per launch of the full-size workload)"},
         "kernel_ms_per_step": agg,
+        "compute_peaks": compute,
         "precision": prec,
         "fp64_block": fp64_rate,
         "cpu_baseline": cpu,

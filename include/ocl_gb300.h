@@ -212,6 +212,11 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
  * not synchronise the calls themselves, so a timed loop can read it after.
  * No counterpart in the reference (instrumentation). */
 int ocl_gb300_stage_times(uint64_t count, double* out);
+/* Measured fused multiply-add throughput of the current device, TFLOP/s
+ * (2 flops per FMA): FP32, the ceiling of the FP32 screen, and FP64, the
+ * ceiling of the FP64 contact code.  Runs for a few tens of ms.  No
+ * counterpart in the reference (instrumentation). */
+int ocl_gb300_fma_peaks(double* fp32_tflops, double* fp64_tflops);
 const char* ocl_gb300_last_error(void);
 const char* ocl_gb300_version(void);
 /* 1 if a CUDA device is usable, else 0 (no compute). */

@@ -24,7 +24,7 @@ _u64p = C.POINTER(C.c_uint64)
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
-    "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_last_error", "ocl_gb300_version",
+    "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available",
 ]
 
@@ -62,6 +62,7 @@ def lib():
     L.ocl_gb300_adaptive_path_drop.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, C.c_double, C.c_double,
                                                _dp, _dp, _ip, C.c_uint64, _u64p, st]
     L.ocl_gb300_stage_times.argtypes = [C.c_uint64, _dp]
+    L.ocl_gb300_fma_peaks.argtypes = [_dp, _dp]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -71,6 +72,13 @@ def lib():
 def check(status):
     if status != 0:
         raise OclError(status, lib().ocl_gb300_last_error().decode())
+
+
+def fma_peaks() -> tuple:
+    """(FP32, FP64) fused multiply-add throughput of the device, TFLOP/s."""
+    a, b = C.c_double(0.0), C.c_double(0.0)
+    check(lib().ocl_gb300_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def stage_times(count: int) -> np.ndarray:

@@ -1,0 +1,85 @@
+// peak_probe.cu -- fused multiply-add throughput of the device in FP32 and
+// FP64: the compute ceilings of the FP32 screen and the FP64 refinement (the
+// copy bandwidth and the tensor-core rate are measured elsewhere; neither
+// bounds this path).
+//
+// Every thread runs eight independent FMA chains x <- x * a + b (a, b kernel
+// arguments, so nothing folds at compile time; |a| < 1 keeps x bounded) on a
+// full-occupancy grid; the launch time comes from CUDA events, best of three
+// after a warm-up.
+#include <algorithm>
+
+#include "util.cuh"
+
+namespace oclg {
+
+__device__ __forceinline__ float fma_rn(float x, float a, float b) { return __fmaf_rn(x, a, b); }
+__device__ __forceinline__ double fma_rn(double x, double a, double b) { return __fma_rn(x, a, b); }
+
+constexpr int PROBE_CHAINS = 8;
+constexpr int PROBE_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(PROBE_THREADS) k_fma_probe(T* __restrict__ out, int iters, T a, T b) {
+    T x[PROBE_CHAINS];
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; ++k) x[k] = (T)(threadIdx.x + k) * (T)1e-3 + (T)1;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < PROBE_CHAINS; ++k) x[k] = fma_rn(x[k], a, b);
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < PROBE_CHAINS; ++k) s += x[k];
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// TFLOP/s (2 flops per FMA) of one probe configuration, or < 0 on error.
+template <typename T>
+static int probe_rate(int iters, double& tflops) {
+    int dev = 0, sms = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+    const unsigned blocks = (unsigned)sms * (unsigned)std::max(1, per_sm / PROBE_THREADS);
+    DevBuf<T> out((size_t)blocks * PROBE_THREADS);
+    if (!out.ok()) return OCL_GB300_OOM;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 0.0f;
+    for (int rep = 0; rep < 4; ++rep) {
+        CK(cudaEventRecord(e0));
+        k_fma_probe<T><<<blocks, PROBE_THREADS>>>(out.p, iters, (T)0.9999, (T)1e-4);
+        CK(cudaEventRecord(e1));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && (best == 0.0f || ms < best)) best = ms;  // rep 0 warms up
+    }
+    CK(cudaEventDestroy(e0));
+    CK(cudaEventDestroy(e1));
+    const double flops = 2.0 * PROBE_CHAINS * (double)iters * (double)blocks * PROBE_THREADS;
+    tflops = best > 0.0f ? flops / (best * 1e-3) / 1e12 : 0.0;
+    return OCL_GB300_OK;
+}
+
+}  // namespace oclg
+
+using namespace oclg;
+
+extern "C" int ocl_gb300_fma_peaks(double* fp32_tflops, double* fp64_tflops) {
+    if (!fp32_tflops || !fp64_tflops) {
+        set_error("fma peaks: null output");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (!ocl_gb300_device_available()) {
+        set_error("no CUDA device available");
+        return OCL_GB300_NO_DEVICE;
+    }
+    // a few ms per launch at the nominal rates (about 80 and 1.3 TFLOP/s)
+    int st = probe_rate<float>(1 << 16, *fp32_tflops);
+    if (st) return st;
+    return probe_rate<double>(1 << 10, *fp64_tflops);
+}
