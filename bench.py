@@ -226,7 +226,57 @@ def aux_measurements(cl_mesh, cuts, with_cpu):
         paths[name] = rec
     out["paths"] = paths
     m2.release()
+    out["stl_read"] = stl_ingest(cl_mesh)
     return out
+
+
+def stl_ingest(tris):
+    """STLReader on the 1,048,576-triangle mesh written as a binary STL, and
+    on its first 100,000 triangles as an ASCII STL (files in a temporary
+    directory), then the device upload of what was read."""
+    import struct
+    import tempfile
+    from opencamlib_gb300 import _native
+    rec = {}
+    with tempfile.TemporaryDirectory() as d:
+        t32 = np.ascontiguousarray(tris, dtype=np.float32)
+        pb = os.path.join(d, "mesh_bin.stl")
+        rows = np.zeros(len(t32), dtype=[("n", "<f4", 3), ("v", "<f4", 9), ("a", "<u2")])
+        rows["v"] = t32
+        with open(pb, "wb") as f:
+            f.write(b"binary".ljust(80, b" "))
+            f.write(struct.pack("<I", len(t32)))
+            f.write(rows.tobytes())
+        pa = os.path.join(d, "mesh_ascii.stl")
+        sub = t32[:100000]
+        with open(pa, "w") as f:
+            f.write("solid bench\n")
+            for t in sub:
+                f.write("facet normal 0 0 1\nouter loop\n")
+                for k in range(3):
+                    f.write("vertex %.9g %.9g %.9g\n" % (t[3 * k], t[3 * k + 1], t[3 * k + 2]))
+                f.write("endloop\nendfacet\n")
+            f.write("endsolid bench\n")
+        for name, path, n in (("binary", pb, len(t32)), ("ascii", pa, len(sub))):
+            _native.stl_read(path)  # file cache warm
+            t0 = time.perf_counter()
+            got = _native.stl_read(path)
+            dt = time.perf_counter() - t0
+            ok = got.shape == (n, 9) and bool(np.array_equal(got, t32[:n].astype(np.float64)))
+            rec[name] = {"triangles": n, "bytes": os.path.getsize(path), "read_s": dt,
+                         "MB_per_s": os.path.getsize(path) / dt / 1e6, "triangles_per_s": n / dt, "exact": ok}
+        try:
+            got = _native.stl_read(pb)
+            import torch
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m = _native.DeviceMesh(got)
+            torch.cuda.synchronize()
+            rec["device_upload_s"] = time.perf_counter() - t0
+            m.release()
+        except Exception as e:  # reported, never required
+            rec["device_upload_error"] = str(e)
+    return rec
 
 
 def sample_indices(sample, seed=17):

@@ -102,6 +102,16 @@ int ocl_gb300_mesh_release(ocl_gb300_mesh mesh);
 uint64_t ocl_gb300_mesh_size(ocl_gb300_mesh mesh);
 /* Mesh bbox [minx maxx miny maxy minz maxz] (Bbox::operator[] order, src/geo/bbox.cpp:113-139). */
 int ocl_gb300_mesh_bbox(ocl_gb300_mesh mesh, double bb[6]);
+/* The triangles STLReader(path, surface) adds to an STLSurf
+ * (src/geo/stlreader.cpp:57-150), in file order, as tris[9 n] = p1 p2 p3
+ * (float32 coordinates widened to double).  *count receives the number of
+ * triangles; call with tris = NULL, cap = 0 to size the output.  Host code
+ * only (no device needed).  Errors: a file that cannot be opened, a binary
+ * file shorter than its facet count (the complete facets are returned), cap
+ * too small.  Where the reference loops forever (a binary file whose header
+ * starts with "solid"; ASCII lines over 1,023 characters) this reader reads
+ * the binary facets / cuts the line. */
+int ocl_gb300_stl_read(const char* path, double* tris, uint64_t cap, uint64_t* count);
 
 /* ---- drop-cutter ------------------------------------------------------- */
 /* Precision modes. */

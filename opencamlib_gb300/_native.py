@@ -23,6 +23,7 @@ _u64p = C.POINTER(C.c_uint64)
 # every entry point declared in include/ocl_gb300.h
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
+    "ocl_gb300_stl_read",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available",
@@ -63,6 +64,7 @@ def lib():
                                                _dp, _dp, _ip, C.c_uint64, _u64p, st]
     L.ocl_gb300_stage_times.argtypes = [C.c_uint64, _dp]
     L.ocl_gb300_fma_peaks.argtypes = [_dp, _dp]
+    L.ocl_gb300_stl_read.argtypes = [C.c_char_p, _dp, C.c_uint64, _u64p]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -72,6 +74,24 @@ def lib():
 def check(status):
     if status != 0:
         raise OclError(status, lib().ocl_gb300_last_error().decode())
+
+
+def stl_read(path, strict: bool = True) -> np.ndarray:
+    """(n, 9) float64 triangles of an STL file, as STLReader adds them
+    (src/geo/stlreader.cpp:57-150); host code, no device needed.  strict:
+    raise on an unreadable or truncated file; else return what was read
+    (nothing for a file that cannot be opened, as the reference)."""
+    p = os.fsencode(path)
+    n = C.c_uint64(0)
+    st = lib().ocl_gb300_stl_read(p, None, 0, C.byref(n))
+    if strict:
+        check(st)
+    out = np.zeros((n.value, 9), dtype=np.float64)
+    if n.value:
+        st = lib().ocl_gb300_stl_read(p, _p(out), n.value, C.byref(n))
+        if strict:
+            check(st)
+    return out
 
 
 def fma_peaks() -> tuple:

@@ -11,10 +11,11 @@ import math
 import numpy as np
 
 from . import _abi
-from ._native import DeviceMesh
+from ._native import DeviceMesh, stl_read
 
-__all__ = ["Point", "CCPoint", "CLPoint", "Triangle", "STLSurf", "Bbox", "Line", "Arc", "Path", "Interval", "Fiber",
-           "BatchDropCutter", "PathDropCutter", "AdaptivePathDropCutter", "BatchPushCutter", "CCType"]
+__all__ = ["Point", "CCPoint", "CLPoint", "Triangle", "STLSurf", "STLReader", "Bbox", "Line", "Arc", "Path",
+           "Interval", "Fiber", "BatchDropCutter", "PathDropCutter", "AdaptivePathDropCutter", "BatchPushCutter",
+           "CCType"]
 
 
 class CCType:
@@ -137,6 +138,15 @@ class STLSurf:
         self._arr = None
         self._dev = {}
 
+    def _extend(self, tris):
+        # many addTriangle calls at once: tris is (n, 9)
+        tris = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 9)
+        if len(tris) == 0:
+            return
+        self._arr = tris.copy() if self.size() == 0 else np.concatenate([self.array(), tris])
+        self._rows = []
+        self._dev = {}
+
     def _materialize_rows(self):
         if self._arr is not None and not self._rows:
             self._rows = self._arr.tolist()
@@ -176,6 +186,16 @@ class STLSurf:
         return f"STLSurf(N={self.size()})"
 
     __repr__ = str
+
+
+class STLReader:
+    """STLReader(filename, surface) adds the file's triangles to the surface
+    (src/geo/stlreader.cpp:35-37, 57-150; the file is parsed by the library's
+    host code).  A file that cannot be read adds nothing, as in the reference."""
+
+    def __init__(self, filename=None, surface=None):
+        if filename is not None and surface is not None:
+            surface._extend(stl_read(filename, strict=False))
 
 
 class Line:

@@ -1,8 +1,8 @@
 // ocl/ocl.hpp -- header-only C++ facade with the reference library's class
 // API for the drop-cutter / push-cutter path (namespace ocl):
 //
-//   geometry   Point, CCPoint/CCType, CLPoint, Bbox, Triangle, STLSurf
-//              (src/geo/*.hpp), Line, Arc, Path (src/geo/path.hpp)
+//   geometry   Point, CCPoint/CCType, CLPoint, Bbox, Triangle, STLSurf,
+//              STLReader (src/geo/*.hpp), Line, Arc, Path (src/geo/path.hpp)
 //   cutters    MillingCutter, CylCutter, BallCutter, BullCutter, ConeCutter,
 //              CompositeCutter and its presets (src/cutters/*.hpp)
 //   fibers     Interval, Fiber (src/algo/interval.hpp, fiber.hpp)
@@ -218,6 +218,32 @@ class STLSurf {
     };
     mutable std::map<uint32_t, Dev> dev_;
     unsigned long version_ = 0;
+};
+
+// STLReader(filepath, surface) adds the file's triangles to the surface
+// (src/geo/stlreader.hpp); a file that cannot be read adds nothing, as in
+// the reference.  The path's wide characters are narrowed one by one, as the
+// reference does.
+class STLReader {
+   public:
+    STLReader() {}
+    STLReader(const std::wstring& filepath, STLSurf& surface) { read_from_file(filepath, surface); }
+    virtual ~STLReader() {}
+
+   private:
+    void read_from_file(const std::wstring& filepath, STLSurf& surface) {
+        std::string path;
+        for (wchar_t c : filepath) path.push_back(static_cast<char>(c));
+        uint64_t n = 0;
+        ocl_gb300_stl_read(path.c_str(), nullptr, 0, &n);
+        if (n == 0) return;
+        std::vector<double> a(9 * n);
+        ocl_gb300_stl_read(path.c_str(), a.data(), n, &n);
+        for (uint64_t i = 0; i < n; ++i) {
+            const double* t = &a[9 * i];
+            surface.addTriangle(Triangle(Point(t[0], t[1], t[2]), Point(t[3], t[4], t[5]), Point(t[6], t[7], t[8])));
+        }
+    }
 };
 
 // ---------------------------------------------------------------- paths

@@ -75,6 +75,8 @@ def _lib(which: str):
     else:
         L.ref_preset_fields.argtypes = [C.c_int, _dp, _dp]
         L.ref_preset_fields.restype = C.c_int
+        L.ref_stl_read.argtypes = [C.c_char_p, _dp, C.c_long]
+        L.ref_stl_read.restype = C.c_long
     _libs[which] = L
     return L
 
@@ -215,6 +217,17 @@ def ref_preset_fields(preset: int, args):
     out = np.zeros(4 + 9 * _abi.MAX_SUB)
     if L.ref_preset_fields(preset, _ptr(a), _ptr(out)) != 0:
         raise RuntimeError("bad preset")
+    return out
+
+
+def ref_stl_read(path) -> np.ndarray:
+    """The reference's STLReader on a file: (n, 9) triangles in order."""
+    L = _lib("ref")
+    p = os.fsencode(path)
+    n = L.ref_stl_read(p, None, 0)
+    out = np.zeros((n, 9), dtype=np.float64)
+    if n:
+        L.ref_stl_read(p, _ptr(out), n)
     return out
 
 

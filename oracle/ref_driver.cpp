@@ -11,7 +11,10 @@
 #include <vector>
 #include <memory>
 
+#include <string>
+
 #include "stlsurf.hpp"
+#include "stlreader.hpp"
 #include "triangle.hpp"
 #include "clpoint.hpp"
 #include "millingcutter.hpp"
@@ -289,6 +292,26 @@ int ref_kd_order(const double* tris, long ntri, unsigned bucket, int dims, int64
         order[i] = it->second;
     }
     return 0;
+}
+
+// STLReader(path, surface): the surface's triangles in order (p1 p2 p3),
+// up to cap; returns their count.
+long ref_stl_read(const char* path, double* out, long cap) {
+    std::wstring wp;
+    for (const char* c = path; *c; ++c) wp.push_back((wchar_t)(unsigned char)*c);
+    ocl::STLSurf surf;
+    ocl::STLReader reader(wp, surf);
+    long n = 0;
+    for (const ocl::Triangle& t : surf.tris) {
+        if (n < cap)
+            for (int k = 0; k < 3; ++k) {
+                out[9 * n + 3 * k] = t.p[k].x;
+                out[9 * n + 3 * k + 1] = t.p[k].y;
+                out[9 * n + 3 * k + 2] = t.p[k].z;
+            }
+        ++n;
+    }
+    return n;
 }
 
 // preset: 1 CompCyl(d,l) 2 CompBall(d,l) 3 CylCone(d1,d2,a) 4 BallCone(d1,d2,a)
