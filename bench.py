@@ -226,7 +226,10 @@ def aux_measurements(cl_mesh, cuts, with_cpu):
         paths[name] = rec
     out["paths"] = paths
     m2.release()
-    out["stl_read"] = stl_ingest(cl_mesh)
+    try:
+        out["stl_read"] = stl_ingest(cl_mesh)
+    except Exception as e:  # reported, never required
+        out["stl_read"] = {"error": str(e)}
     return out
 
 
