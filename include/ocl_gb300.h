@@ -214,6 +214,13 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
                                  double* xyz, double* cc, int32_t* type, uint64_t cap,
                                  uint64_t* count, ocl_gb300_stats* stats);
 
+/* ---- CL point filter ----------------------------------------------------- */
+/* LineCLFilter::run (src/common/lineclfilter.cpp:40-77) on n points xyz[3 n]:
+ * keep[0 .. *nkeep) receives the indices of the points kept, in order (the
+ * first and the last always; lists of 0 or 1 points unchanged); keep must
+ * hold n entries.  Host code only (no device needed). */
+int ocl_gb300_line_filter(const double* xyz, uint64_t n, double tol, uint64_t* keep, uint64_t* nkeep);
+
 /* ---- misc ----------------------------------------------------------------- */
 /* Device time of the stages of the calling thread's last `count` (<= 256)
  * ocl_gb300_drop / _drop_device calls, oldest first: out[4k..4k+3] = FP32

@@ -23,7 +23,7 @@ _u64p = C.POINTER(C.c_uint64)
 # every entry point declared in include/ocl_gb300.h
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
-    "ocl_gb300_stl_read",
+    "ocl_gb300_stl_read", "ocl_gb300_line_filter",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available",
@@ -65,6 +65,7 @@ def lib():
     L.ocl_gb300_stage_times.argtypes = [C.c_uint64, _dp]
     L.ocl_gb300_fma_peaks.argtypes = [_dp, _dp]
     L.ocl_gb300_stl_read.argtypes = [C.c_char_p, _dp, C.c_uint64, _u64p]
+    L.ocl_gb300_line_filter.argtypes = [_dp, C.c_uint64, C.c_double, _u64p, _u64p]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -92,6 +93,16 @@ def stl_read(path, strict: bool = True) -> np.ndarray:
         if strict:
             check(st)
     return out
+
+
+def line_filter(xyz, tol: float) -> np.ndarray:
+    """Indices of the points LineCLFilter keeps (src/common/lineclfilter.cpp:40-77);
+    host code, no device needed."""
+    a = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    keep = np.zeros(max(len(a), 1), dtype=np.uint64)
+    nk = C.c_uint64(0)
+    check(lib().ocl_gb300_line_filter(_p(a), len(a), float(tol), _p(keep, _u64p), C.byref(nk)))
+    return keep[:nk.value].astype(np.int64)
 
 
 def fma_peaks() -> tuple:

@@ -11,11 +11,11 @@ import math
 import numpy as np
 
 from . import _abi
-from ._native import DeviceMesh, stl_read
+from ._native import DeviceMesh, line_filter, stl_read
 
 __all__ = ["Point", "CCPoint", "CLPoint", "Triangle", "STLSurf", "STLReader", "Bbox", "Line", "Arc", "Path",
            "Interval", "Fiber", "BatchDropCutter", "PathDropCutter", "AdaptivePathDropCutter", "BatchPushCutter",
-           "CCType"]
+           "LineCLFilter", "CCType"]
 
 
 class CCType:
@@ -196,6 +196,33 @@ class STLReader:
     def __init__(self, filename=None, surface=None):
         if filename is not None and surface is not None:
             surface._extend(stl_read(filename, strict=False))
+
+
+class LineCLFilter:
+    """LineCLFilter (src/common/lineclfilter.cpp, Python API of
+    src/pythonlib/ocl_algo.cpp:172-179): addCLPoint copies, run() keeps the
+    points the filter selects (selection in the library), getCLPoints()
+    returns them."""
+
+    def __init__(self):
+        self._pts = []
+        self._tol = 0.0
+
+    def addCLPoint(self, p):
+        cc = p.getCC() if isinstance(p, CLPoint) else None
+        self._pts.append(CLPoint(p.x, p.y, p.z, cc))
+
+    def setTolerance(self, tol):
+        self._tol = float(tol)
+
+    def run(self):
+        if len(self._pts) < 2:
+            return
+        xyz = np.array([[p.x, p.y, p.z] for p in self._pts], dtype=np.float64)
+        self._pts = [self._pts[i] for i in line_filter(xyz, self._tol)]
+
+    def getCLPoints(self):
+        return list(self._pts)
 
 
 class Line:

@@ -6,6 +6,7 @@
 //   cutters    MillingCutter, CylCutter, BallCutter, BullCutter, ConeCutter,
 //              CompositeCutter and its presets (src/cutters/*.hpp)
 //   fibers     Interval, Fiber (src/algo/interval.hpp, fiber.hpp)
+//   filters    CLFilter, LineCLFilter (src/common/*clfilter.hpp)
 //   operations BatchDropCutter, PathDropCutter, AdaptivePathDropCutter,
 //              BatchPushCutter (src/dropcutter/*.hpp, src/algo/batchpushcutter.hpp)
 //
@@ -243,6 +244,51 @@ class STLReader {
             const double* t = &a[9 * i];
             surface.addTriangle(Triangle(Point(t[0], t[1], t[2]), Point(t[3], t[4], t[5]), Point(t[6], t[7], t[8])));
         }
+    }
+};
+
+// ---------------------------------------------------------------- CL filters
+// CLFilter / LineCLFilter (src/common/clfilter.hpp, lineclfilter.hpp):
+// addCLPoint copies, run() replaces clpoints by the points the filter keeps
+// (the selection runs in the library, ocl_gb300_line_filter; the kept points
+// are the caller's copies, CC points included).
+class CLFilter {
+   public:
+    CLFilter() {}
+    virtual ~CLFilter() {}
+    virtual void addCLPoint(const CLPoint& p) = 0;
+    virtual void setTolerance(const double tol) = 0;
+    virtual void run() = 0;
+    std::list<CLPoint> clpoints;
+    double tol = 0.0;
+};
+
+class LineCLFilter : public CLFilter {
+   public:
+    LineCLFilter() { clpoints.clear(); }
+    virtual ~LineCLFilter() {}
+    void addCLPoint(const CLPoint& p) override { clpoints.push_back(p); }
+    void setTolerance(const double tolerance) override { tol = tolerance; }
+    void run() override {
+        const size_t n = clpoints.size();
+        if (n < 2) return;
+        std::vector<double> xyz;
+        xyz.reserve(3 * n);
+        std::vector<const CLPoint*> ptr;
+        ptr.reserve(n);
+        for (const CLPoint& p : clpoints) {
+            xyz.push_back(p.x); xyz.push_back(p.y); xyz.push_back(p.z);
+            ptr.push_back(&p);
+        }
+        std::vector<uint64_t> keep(n);
+        uint64_t nk = 0;
+        if (ocl_gb300_line_filter(xyz.data(), n, tol, keep.data(), &nk) != OCL_GB300_OK) {
+            std::cerr << "ocl::LineCLFilter: " << ocl_gb300_last_error() << "\n";
+            return;
+        }
+        std::list<CLPoint> kept;
+        for (uint64_t k = 0; k < nk; ++k) kept.push_back(*ptr[keep[k]]);
+        clpoints.swap(kept);
     }
 };
 

@@ -77,6 +77,8 @@ def _lib(which: str):
         L.ref_preset_fields.restype = C.c_int
         L.ref_stl_read.argtypes = [C.c_char_p, _dp, C.c_long]
         L.ref_stl_read.restype = C.c_long
+        L.ref_line_filter.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long]
+        L.ref_line_filter.restype = C.c_long
     _libs[which] = L
     return L
 
@@ -229,6 +231,15 @@ def ref_stl_read(path) -> np.ndarray:
     if n:
         L.ref_stl_read(p, _ptr(out), n)
     return out
+
+
+def ref_line_filter(xyz, tol) -> np.ndarray:
+    """The reference's LineCLFilter: the kept points, (k, 3), in order."""
+    L = _lib("ref")
+    a = _d(xyz).reshape(-1, 3)
+    out = np.zeros((max(len(a), 1), 3), dtype=np.float64)
+    k = L.ref_line_filter(_ptr(a), len(a), float(tol), _ptr(out), len(out))
+    return out[:k]
 
 
 def last_loop_seconds() -> float:

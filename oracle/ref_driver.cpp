@@ -15,6 +15,7 @@
 
 #include "stlsurf.hpp"
 #include "stlreader.hpp"
+#include "lineclfilter.hpp"
 #include "triangle.hpp"
 #include "clpoint.hpp"
 #include "millingcutter.hpp"
@@ -312,6 +313,25 @@ long ref_stl_read(const char* path, double* out, long cap) {
         ++n;
     }
     return n;
+}
+
+// LineCLFilter over n points: the kept points' coordinates in order, up to
+// cap; returns their count.
+long ref_line_filter(const double* xyz, long n, double tol, double* out, long cap) {
+    ocl::LineCLFilter f;
+    for (long i = 0; i < n; ++i) f.addCLPoint(ocl::CLPoint(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
+    f.setTolerance(tol);
+    f.run();
+    long k = 0;
+    for (const ocl::CLPoint& p : f.clpoints) {
+        if (k < cap) {
+            out[3 * k] = p.x;
+            out[3 * k + 1] = p.y;
+            out[3 * k + 2] = p.z;
+        }
+        ++k;
+    }
+    return k;
 }
 
 // preset: 1 CompCyl(d,l) 2 CompBall(d,l) 3 CylCone(d1,d2,a) 4 BallCone(d1,d2,a)
