@@ -106,15 +106,9 @@ class ClockSampler:
 
 
 def dist_setup(n):
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        dist.init_process_group("nccl")
-        return rank, world, local, dist
-    return 0, 1, 0, None
+    """One process per GPU (replicas; opencamlib_gb300.replicas)."""
+    from opencamlib_gb300 import replicas
+    return replicas.setup("nccl")
 
 
 def cutters(names=""):
@@ -391,11 +385,9 @@ def main():
     # records on the launching stream; read after the timed region)
     from opencamlib_gb300 import _native
     stage = _native.stage_times(len(cuts) * args.steps)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * len(cuts) * M * args.steps / (total_ms / 1e3)
+    from opencamlib_gb300 import replicas
+    total_ms = replicas.max_over_ranks(total_ms, dist, "cuda")
+    value = replicas.whole_job_rate(len(cuts) * M * args.steps, world, total_ms / 1e3)
 
     # e2e: host-buffer C-ABI call, pinned host memory, copies inside the timed region
     h_cl = torch.from_numpy(cl).pin_memory().numpy()
@@ -424,12 +416,9 @@ def main():
         step_host()
     torch.cuda.synchronize()
     e_el = time.perf_counter() - e_t0
-    if dist:
-        t = torch.tensor([e_el], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e_el = float(t.item())
+    e_el = replicas.max_over_ranks(e_el, dist, "cuda")
     clocks = sampler.stop()
-    e2e = world * len(cuts) * M * args.steps / e_el
+    e2e = replicas.whole_job_rate(len(cuts) * M * args.steps, world, e_el)
 
     if rank != 0:
         if dist:

@@ -221,6 +221,57 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
  * hold n entries.  Host code only (no device needed). */
 int ocl_gb300_line_filter(const double* xyz, uint64_t n, double tol, uint64_t* keep, uint64_t* nkeep);
 
+/* ---- introspection (parity checks of the index and the FP32 screen) ------ */
+/* The KD-tree leaf visit order the device holds: order[k] = insertion index
+ * of the k-th triangle in KDTree::search order (src/common/kdtree.hpp:141-210
+ * build_node, :273-304 search_node, hi child first).  dims 0 = XY (the
+ * drop-cutter tree, BatchDropCutter::setSTL src/dropcutter/batchdropcutter.cpp:54-61),
+ * 1 = YZ (X-fibers), 2 = XZ (Y-fibers) (BatchPushCutter::setSTL
+ * src/algo/batchpushcutter.cpp:55-70).  order holds mesh_size entries.
+ * No counterpart in the reference (its tree is not exposed). */
+int ocl_gb300_mesh_kd_order(ocl_gb300_mesh mesh, int dims, int64_t* order);
+/* The KD visit rank stored in every triangle's device record (the tie-break
+ * of every fold), read back by insertion index.  No counterpart in the reference. */
+int ocl_gb300_mesh_kd_rank(ocl_gb300_mesh mesh, int64_t* rank);
+/* Exact overlap sets through the device grid: for CL point i (host xyz),
+ * the insertion indices of every triangle the grid query finds under a
+ * cutter of this radius and MillingCutter::overlaps accepts
+ * (src/cutters/millingcutter.cpp:422-433), ascending, in
+ * ids[offsets[i] .. offsets[i+1]).  offsets holds M + 1 entries.  If cap is
+ * too small OCL_GB300_CAPACITY is returned and offsets is complete.  The set
+ * the reference forms per CL point in BatchDropCutter::dropCutter5
+ * (src/dropcutter/batchdropcutter.cpp:208-222: KD candidates, then overlaps). */
+int ocl_gb300_overlap_sets(ocl_gb300_mesh mesh, double radius, const double* cl_xyz, uint64_t M,
+                           uint64_t* offsets, int32_t* ids, uint64_t cap);
+
+/* FP32 certificate check: for every exact-overlap (CL point, triangle) pair,
+ * the FP64 contact code on its own (the whole triangle from the CL point's
+ * start height, and each facet, vertex and edge contact) against the FP32
+ * bounds the mixed-precision path relies on to leave work out (the screen's
+ * [lo, hi], the refinement's per-part skips, the grid-entry cull).  Counts
+ * of bounds exceeded; "unsafe" ones exceed it by more than the guard margin
+ * and could change a result.  No counterpart in the reference. */
+typedef struct ocl_gb300_cert {
+    uint64_t pairs;             /* exact-overlap pairs checked */
+    uint64_t lifted;            /* of those: the FP64 drop lifts the start height */
+    uint64_t tri_hi_exceeded;   /* FP64 result above the screen's upper bound */
+    uint64_t tri_hi_unsafe;
+    uint64_t tri_lo_exceeded;   /* FP64 result below the screen's certified lower bound */
+    uint64_t part_hi_exceeded;  /* a facet / vertex / edge contact above its skip bound */
+    uint64_t part_hi_unsafe;
+    uint64_t entry_ub_exceeded; /* a contact above the grid-entry cull's bound */
+    uint64_t entry_ub_unsafe;
+    uint64_t alt_hi_exceeded;   /* bull: above the per-lane screen's bound (handed-back points) */
+    double max_tri_excess;      /* largest excess of each kind (mm; 0 when none) */
+    double max_part_excess;
+    double max_entry_excess;
+    double max_lo_excess;
+    double error_budget;        /* E: FP32 position error budget of the call (mm) */
+    double guard;               /* margin of the bound tests (mm) */
+} ocl_gb300_cert;
+int ocl_gb300_certificate_check(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* cl_xyz,
+                                uint64_t M, ocl_gb300_cert* out);
+
 /* ---- misc ----------------------------------------------------------------- */
 /* Device time of the stages of the calling thread's last `count` (<= 256)
  * ocl_gb300_drop / _drop_device calls, oldest first: out[4k..4k+3] = FP32

@@ -55,3 +55,16 @@ class Stats(C.Structure):
                 ("untracked_branch_points", C.c_uint64), ("plain_points", C.c_uint64),
                 ("verify_failed_points", C.c_uint64), ("launches", C.c_uint64), ("kernel_ms", C.c_double), ("screen_ms", C.c_double),
                 ("refine_ms", C.c_double), ("fallback_ms", C.c_double), ("total_ms", C.c_double)]
+
+
+class Cert(C.Structure):
+    """ocl_gb300_cert: FP64 contacts against the FP32 bounds they are certified by."""
+    _fields_ = [("pairs", C.c_uint64), ("lifted", C.c_uint64), ("tri_hi_exceeded", C.c_uint64),
+                ("tri_hi_unsafe", C.c_uint64), ("tri_lo_exceeded", C.c_uint64), ("part_hi_exceeded", C.c_uint64),
+                ("part_hi_unsafe", C.c_uint64), ("entry_ub_exceeded", C.c_uint64), ("entry_ub_unsafe", C.c_uint64),
+                ("alt_hi_exceeded", C.c_uint64), ("max_tri_excess", C.c_double), ("max_part_excess", C.c_double),
+                ("max_entry_excess", C.c_double), ("max_lo_excess", C.c_double), ("error_budget", C.c_double),
+                ("guard", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

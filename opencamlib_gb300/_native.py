@@ -26,7 +26,8 @@ EXPORTS = [
     "ocl_gb300_stl_read", "ocl_gb300_line_filter",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
-    "ocl_gb300_device_available",
+    "ocl_gb300_device_available", "ocl_gb300_mesh_kd_order", "ocl_gb300_mesh_kd_rank", "ocl_gb300_overlap_sets",
+    "ocl_gb300_certificate_check",
 ]
 
 _lib = None
@@ -66,6 +67,11 @@ def lib():
     L.ocl_gb300_fma_peaks.argtypes = [_dp, _dp]
     L.ocl_gb300_stl_read.argtypes = [C.c_char_p, _dp, C.c_uint64, _u64p]
     L.ocl_gb300_line_filter.argtypes = [_dp, C.c_uint64, C.c_double, _u64p, _u64p]
+    _i64p = C.POINTER(C.c_int64)
+    L.ocl_gb300_mesh_kd_order.argtypes = [C.c_void_p, C.c_int, _i64p]
+    L.ocl_gb300_mesh_kd_rank.argtypes = [C.c_void_p, _i64p]
+    L.ocl_gb300_overlap_sets.argtypes = [C.c_void_p, C.c_double, _dp, C.c_uint64, _u64p, _ip, C.c_uint64]
+    L.ocl_gb300_certificate_check.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.POINTER(_abi.Cert)]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -83,16 +89,26 @@ def stl_read(path, strict: bool = True) -> np.ndarray:
     raise on an unreadable or truncated file; else return what was read
     (nothing for a file that cannot be opened, as the reference)."""
     p = os.fsencode(path)
+    # one parse into a buffer sized from the file (a binary facet takes 50
+    # bytes; an ASCII facet is rarely under 100); only when that guess is
+    # short is the file parsed a second time, with the count the first parse
+    # reported (a file rewritten in between may then read differently)
+    try:
+        size = os.path.getsize(path)
+    except OSError:
+        size = 0
+    cap = max(size // 100, (size - 84) // 50, 0) + 16
     n = C.c_uint64(0)
-    st = lib().ocl_gb300_stl_read(p, None, 0, C.byref(n))
+    for _ in range(2):
+        out = np.zeros((cap, 9), dtype=np.float64)
+        st = lib().ocl_gb300_stl_read(p, _p(out), cap, C.byref(n))
+        if st != _abi.OK and n.value > cap:
+            cap = n.value
+            continue
+        break
     if strict:
         check(st)
-    out = np.zeros((n.value, 9), dtype=np.float64)
-    if n.value:
-        st = lib().ocl_gb300_stl_read(p, _p(out), n.value, C.byref(n))
-        if strict:
-            check(st)
-    return out
+    return out[:min(n.value, cap)].copy()
 
 
 def line_filter(xyz, tol: float) -> np.ndarray:
@@ -264,3 +280,45 @@ class DeviceMesh:
             check(status)
             k = int(n.value)
             return xyz[:k], cc[:k], ty[:k], st
+
+    # ---- introspection (parity checks) -------------------------------------
+    def kd_order(self, dims: int = 0) -> np.ndarray:
+        """Insertion indices in the device's KD leaf visit order (dims 0 XY,
+        1 YZ, 2 XZ), as KDTree::search visits them."""
+        out = np.zeros(len(self), dtype=np.int64)
+        check(lib().ocl_gb300_mesh_kd_order(self._h, dims, _p(out, C.POINTER(C.c_int64))))
+        return out
+
+    def kd_rank(self) -> np.ndarray:
+        """The KD visit rank of every triangle (insertion order) as stored on the device."""
+        out = np.zeros(len(self), dtype=np.int64)
+        check(lib().ocl_gb300_mesh_kd_rank(self._h, _p(out, C.POINTER(C.c_int64))))
+        return out
+
+    def overlap_sets(self, radius: float, cl):
+        """Exact overlap sets the grid yields: (offsets[M+1], ids) with the
+        insertion indices of CL point i's set, ascending, in
+        ids[offsets[i]:offsets[i+1]]."""
+        cl = _d(cl, 3)
+        M = cl.shape[0]
+        offsets = np.zeros(M + 1, dtype=np.uint64)
+        cap = 0
+        ids = np.zeros(1, dtype=np.int32)
+        while True:
+            status = lib().ocl_gb300_overlap_sets(self._h, float(radius), _p(cl), M, _p(offsets, _u64p),
+                                                  _p(ids, _ip), cap)
+            if status == _abi.CAPACITY:
+                cap = int(offsets[-1])
+                ids = np.zeros(max(cap, 1), dtype=np.int32)
+                continue
+            check(status)
+            return offsets.astype(np.int64), ids[:int(offsets[-1])]
+
+    def certificate(self, cutter, cl) -> dict:
+        """FP64 contacts of every exact-overlap pair against the FP32 bounds
+        the mixed path uses to leave work out (ocl_gb300_certificate_check)."""
+        cl = _d(cl, 3)
+        out = _abi.Cert()
+        desc = cutter.desc()
+        check(lib().ocl_gb300_certificate_check(self._h, C.byref(desc), _p(cl), cl.shape[0], C.byref(out)))
+        return out.as_dict()

@@ -68,6 +68,38 @@ class Point:
     def __eq__(self, o):
         return isinstance(o, Point) and self.x == o.x and self.y == o.y and self.z == o.z
 
+    # rotations about the x, y, z axes (src/geo/point.cpp:105-134)
+    def xRotate(self, theta):
+        self.x, self.y, self.z = _rotate3(_rx(theta), self.x, self.y, self.z)
+
+    def yRotate(self, theta):
+        self.x, self.y, self.z = _rotate3(_ry(theta), self.x, self.y, self.z)
+
+    def zRotate(self, theta):
+        self.x, self.y, self.z = _rotate3(_rz(theta), self.x, self.y, self.z)
+
+
+def _rx(t):
+    c, s = math.cos(t), math.sin(t)
+    return (1.0, 0.0, 0.0, 0.0, c, -s, 0.0, s, c)
+
+
+def _ry(t):
+    c, s = math.cos(t), math.sin(t)
+    return (c, 0.0, s, 0.0, 1.0, 0.0, -s, 0.0, c)
+
+
+def _rz(t):
+    c, s = math.cos(t), math.sin(t)
+    return (c, -s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0)
+
+
+def _rotate3(m, x, y, z):
+    """Point::matrixRotate: each row of the matrix times (x, y, z), summed
+    left to right (scalars or numpy arrays; no fused multiply-add)."""
+    a, b, c, d, e, f, g, h, i = m
+    return a * x + b * y + c * z, d * x + e * y + f * z, g * x + h * y + i * z
+
 
 class CCPoint(Point):
     __slots__ = ("type",)
@@ -119,6 +151,13 @@ class Triangle:
     def getPoints(self):
         return list(self.p)
 
+    def rotate(self, xr, yr, zr):
+        """Triangle::rotate (src/geo/triangle.cpp:130-138)."""
+        for q in self.p:
+            q.xRotate(xr)
+            q.yRotate(yr)
+            q.zRotate(zr)
+
     def array(self):
         return [c for q in self.p for c in (q.x, q.y, q.z)]
 
@@ -159,6 +198,17 @@ class STLSurf:
 
     def size(self):
         return int(self.array().shape[0])
+
+    def rotate(self, xr, yr, zr):
+        """STLSurf::rotate (src/geo/stlsurf.cpp:44-55): every vertex rotated
+        about x, then y, then z; the device copy is made again on next use."""
+        a = self.array().reshape(-1, 3).copy()
+        x, y, z = a[:, 0], a[:, 1], a[:, 2]
+        for m in (_rx(xr), _ry(yr), _rz(zr)):
+            x, y, z = _rotate3(m, x, y, z)
+        self._arr = np.stack([x, y, z], axis=1).reshape(-1, 9)
+        self._rows = []
+        self._dev = {}
 
     def getTriangles(self):
         a = self.array()

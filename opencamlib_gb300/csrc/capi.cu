@@ -3,6 +3,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "drop.cuh"
@@ -16,6 +17,43 @@ static thread_local std::string tl_error;
 std::string& last_error_ref() { return tl_error; }
 void set_error(const std::string& msg) { tl_error = msg; }
 
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points
+// (no link against the driver library).
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+uint64_t context_key() {
+    static std::once_flag once;
+    static CtxGetCurrentFn get_cur = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+        return 0;
+    }
+    if (get_cur && get_id) {
+        void* ctx = nullptr;
+        unsigned long long id = 0;
+        // the runtime makes the device's primary context current lazily;
+        // cudaSetDevice does it now
+        if (get_cur(&ctx) == 0 && !ctx && cudaSetDevice(dev) == cudaSuccess) get_cur(&ctx);
+        if (ctx && get_id(ctx, &id) == 0) return (uint64_t)id | (1ull << 63);
+    }
+    return (uint64_t)dev + 1;
+}
+
 int mesh_create(const double* tris, uint64_t n, unsigned bucket, Mesh** out);
 void mesh_destroy(Mesh* m);
 int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t F, uint64_t* offsets, double* ival,
@@ -25,6 +63,11 @@ int path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, d
 int adaptive_path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, double sampling,
                            double min_sampling, double cos_limit, double* xyz, double* cc, int32_t* type,
                            uint64_t cap, uint64_t* count, ocl_gb300_stats* stats);
+int mesh_kd_order(Mesh& m, int dims, int64_t* order);
+int mesh_kd_rank(Mesh& m, int64_t* rank);
+int overlap_sets(Mesh& m, double radius, const double* cl, uint64_t M, uint64_t* offsets, int32_t* ids,
+                 uint64_t cap);
+int certificate_check(Mesh& m, const CutterP& cp, const double* cl, uint64_t M, ocl_gb300_cert* out);
 
 // Constructors of the basic cutters (cylcutter.cpp:39-46, ballcutter.cpp:38-45,
 // bullcutter.cpp:38-47, conecutter.cpp:39-49); compiled with
@@ -390,6 +433,47 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
     if (stats)
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return st;
+}
+
+int ocl_gb300_mesh_kd_order(ocl_gb300_mesh mesh, int dims, int64_t* order) {
+    if (!mesh || (!order && mesh->m->n)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    return mesh_kd_order(*mesh->m, dims, order);
+}
+
+int ocl_gb300_mesh_kd_rank(ocl_gb300_mesh mesh, int64_t* rank) {
+    if (!mesh || (!rank && mesh->m->n)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    return mesh_kd_rank(*mesh->m, rank);
+}
+
+int ocl_gb300_overlap_sets(ocl_gb300_mesh mesh, double radius, const double* cl_xyz, uint64_t M, uint64_t* offsets,
+                           int32_t* ids, uint64_t cap) {
+    if (!mesh || !offsets || (M > 0 && !cl_xyz) || (cap > 0 && !ids)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    return overlap_sets(*mesh->m, radius, cl_xyz, M, offsets, ids, cap);
+}
+
+int ocl_gb300_certificate_check(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* cl_xyz,
+                                uint64_t M, ocl_gb300_cert* out) {
+    if (!mesh || !out || (M > 0 && !cl_xyz)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    CutterP cp;
+    int st = cutter_or_error(cutter, cp);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(mesh->m->mu);
+    return certificate_check(*mesh->m, cp, cl_xyz, M, out);
 }
 
 }  // extern "C"

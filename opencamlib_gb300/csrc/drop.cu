@@ -21,7 +21,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <set>
 #include <string>
 
 #include <cub/cub.cuh>
@@ -757,7 +759,20 @@ struct DropWork {
     }
 };
 
+// One workspace per (host thread, CUDA context): its buffers, events and
+// launch context belong to the device that was current when they were made.
+// tl_work is the calling thread's workspace for its current context.
+static thread_local std::map<uint64_t, DropWork*> tl_works;
 static thread_local DropWork* tl_work = nullptr;
+
+static DropWork* work_for_current_context() {
+    const uint64_t key = context_key();
+    if (!key) return nullptr;
+    DropWork*& w = tl_works[key];
+    if (!w) w = new DropWork();
+    tl_work = w;
+    return w;
+}
 
 // The dense screen kernel over all warps, then the sparse one over the warps
 // whose points it found spread out (a fixed grid striding over the list).
@@ -788,18 +803,26 @@ static void launch_screen(const DropCtx& h, const CutterP& cp, unsigned blocks, 
 // k_drop_exact over the handed-back points (count on the device).
 static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
                         uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(k_drop_exact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)EXACT_SMEM);
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(k_drop_exact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)EXACT_SMEM);
-    });
-    if (attr_err != cudaSuccess) {
-        set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(attr_err));
-        return OCL_GB300_DEVICE_ERROR;
+    // the shared-memory opt-in is a property of the kernel in one context:
+    // set once per context (device), not once per process
+    static std::mutex mu;
+    static std::set<uint64_t> done;
+    const uint64_t key = context_key();
+    if (!key) return OCL_GB300_DEVICE_ERROR;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!done.count(key)) {
+            cudaError_t e = cudaFuncSetAttribute(k_drop_exact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)EXACT_SMEM);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_drop_exact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)EXACT_SMEM);
+            if (e != cudaSuccess) {
+                set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+                return OCL_GB300_DEVICE_ERROR;
+            }
+            done.insert(key);
+        }
     }
     if (blocks == 0) blocks = 1;
     if (composite)
@@ -809,6 +832,30 @@ static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, 
     return OCL_GB300_OK;
 }
 
+void init_drop_ctx(const Mesh& m, const CutterP& cp, DropCtx& h) {
+    std::memset(&h, 0, sizeof(DropCtx));
+    h.cp = cp;
+    h.g = m.grid;
+    h.cells = m.d_cells;
+    h.entries = m.d_entries;
+    h.t64 = m.d_t64;
+    h.t32 = m.d_t32;
+    h.kd_nodes = m.drop_kd.d_nodes;
+    h.kd_order = m.drop_kd.d_order;
+    h.seeded = true;
+    bool composite = false;
+    fill_prof(cp, h.prof, h.hlb, composite);
+    h.composite_screen = composite;
+    fill_comp(cp, h.comp);
+    // FP32 position error budget of the local frame (coordinates up to half
+    // the mesh extent plus the cutter radius from the origin) and the margin
+    // of every bound test
+    const double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
+    const double maxabs = half + cp.radius + 1.0;
+    h.E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
+    h.guard = 4.0f * h.E + 1e-5f * (float)cp.radius;
+}
+
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats) {
     if (M == 0) return OCL_GB300_OK;
@@ -816,8 +863,9 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         set_error("too many CL points");
         return OCL_GB300_BAD_ARG;
     }
-    if (!tl_work) tl_work = new DropWork();
-    DropWork& w = *tl_work;
+    DropWork* wp = work_for_current_context();
+    if (!wp) return OCL_GB300_DEVICE_ERROR;
+    DropWork& w = *wp;
     size_t sort_bytes = 0;
     CK(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, w.keys.p, w.keys2.p, w.perm0.p, w.perm.p, (int64_t)M, 0,
                                        32, stream));
@@ -826,13 +874,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
 
     if (!w.host_ctx) w.host_ctx = new DropCtx();
     DropCtx* h = w.host_ctx;  // passed by value as the kernels' __grid_constant__ parameter
-    std::memset(h, 0, sizeof(DropCtx));
-    h->cp = cp;
-    h->g = m.grid;
-    h->cells = m.d_cells;
-    h->entries = m.d_entries;
-    h->t64 = m.d_t64;
-    h->t32 = m.d_t32;
+    init_drop_ctx(m, cp, *h);
+    const bool composite = h->composite_screen;
     h->cl = w.cls.p;
     h->perm = w.perm.p;
     h->M = (int)M;
@@ -846,19 +889,8 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     h->ncand = w.ncand.p;
     h->blo = w.blo.p;
     h->sparse_list = w.sparse.p;
-    h->seeded = true;
     h->sparse_n = w.counters.p + C_SPARSE;
     h->counters = w.counters.p;
-    h->kd_nodes = m.drop_kd.d_nodes;
-    h->kd_order = m.drop_kd.d_order;
-    bool composite = false;
-    fill_prof(cp, h->prof, h->hlb, composite);
-    h->composite_screen = composite;
-    fill_comp(cp, h->comp);
-    double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
-    double maxabs = half + cp.radius + 1.0;
-    h->E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
-    h->guard = 4.0f * h->E + 1e-5f * (float)cp.radius;
 
     cudaEvent_t* ev = w.ring[w.ring_pos];
     if (!ev[0]) {
@@ -1011,26 +1043,25 @@ __global__ void k_noalloc_identity(uint32_t* perm, int M) {
 
 // Device address of the scratch array, looked up once per device with that
 // device current (the host-side name is only a stand-in for the symbol).
+// The cache is keyed by the CUDA context, so a context made after a device
+// reset (which reloads the module) gets its own lookup.
 static int noalloc_scratch(NoAllocScratch** out) {
     static std::mutex mu;
-    static NoAllocScratch* addr[256] = {};
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) {
-        set_error("device ordinal out of range");
-        return OCL_GB300_DEVICE_ERROR;
-    }
+    static std::map<uint64_t, NoAllocScratch*> addr;
+    const uint64_t key = context_key();
+    if (!key) return OCL_GB300_DEVICE_ERROR;
     std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
+    NoAllocScratch*& a = addr[key];
+    if (!a) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             set_error(std::string("cudaGetSymbolAddress(no-alloc scratch): ") + cudaGetErrorString(e));
             return OCL_GB300_DEVICE_ERROR;
         }
-        addr[dev] = static_cast<NoAllocScratch*>(p);
+        a = static_cast<NoAllocScratch*>(p);
     }
-    *out = addr[dev];
+    *out = a;
     return OCL_GB300_OK;
 }
 
@@ -1046,15 +1077,8 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     int st = noalloc_scratch(&sc);
     if (st) return st;
     DropCtx h;
-    std::memset(&h, 0, sizeof(h));
-    h.cp = cp;
-    h.g = m.grid;
-    h.cells = m.d_cells;
-    h.entries = m.d_entries;
-    h.t64 = m.d_t64;
-    h.t32 = m.d_t32;
-    h.kd_nodes = m.drop_kd.d_nodes;
-    h.kd_order = m.drop_kd.d_order;
+    init_drop_ctx(m, cp, h);
+    const bool composite = h.composite_screen;
     h.cl = d_cl;  // caller's order
     h.perm = sc->perm;
     h.M = (int)M;
@@ -1068,17 +1092,8 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
     h.ncand = sc->ncand;
     h.blo = sc->blo;
     h.sparse_list = sc->sparse;
-    h.seeded = true;
     h.sparse_n = sc->counters + C_SPARSE;
     h.counters = sc->counters;
-    bool composite = false;
-    fill_prof(cp, h.prof, h.hlb, composite);
-    h.composite_screen = composite;
-    fill_comp(cp, h.comp);
-    double half = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4]));
-    double maxabs = half + cp.radius + 1.0;
-    h.E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, cp.radius));
-    h.guard = 4.0f * h.E + 1e-5f * (float)cp.radius;
     // the array keeps the previous call's contents: clear what must start at zero
     CK(cudaMemsetAsync(sc->counters, 0, sizeof(sc->counters), stream));
     const int TB = 256;

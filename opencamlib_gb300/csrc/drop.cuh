@@ -73,6 +73,9 @@ struct DropCtx {
 };
 
 struct DropWork;
+// The per-call context fields that depend only on the mesh and the cutter:
+// mesh arrays, grid, KD tree, FP32 profiles, the error budget E and guard.
+void init_drop_ctx(const Mesh& m, const CutterP& cp, DropCtx& h);
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats);
 

@@ -67,6 +67,8 @@ struct Mesh {
 };
 
 int upload_kd(Mesh& M, const KDTreeD& kd, PushIndex& out);
+// The YZ (X-fibers) or XZ (Y-fibers) tree of the push-cutter, built on first use.
+int ensure_push_index(Mesh& m, int dir);
 std::string& last_error_ref();
 void set_error(const std::string& msg);
 

@@ -44,9 +44,17 @@ static int probe_rate(int iters, double& tflops) {
     const unsigned blocks = (unsigned)sms * (unsigned)std::max(1, per_sm / PROBE_THREADS);
     DevBuf<T> out((size_t)blocks * PROBE_THREADS);
     if (!out.ok()) return OCL_GB300_OOM;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    // destroyed on every way out of the function
+    struct Events {
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } ev;
+    CK(cudaEventCreate(&ev.e[0]));
+    CK(cudaEventCreate(&ev.e[1]));
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1];
     float best = 0.0f;
     for (int rep = 0; rep < 4; ++rep) {
         CK(cudaEventRecord(e0));
@@ -58,8 +66,6 @@ static int probe_rate(int iters, double& tflops) {
         CK(cudaEventElapsedTime(&ms, e0, e1));
         if (rep > 0 && (best == 0.0f || ms < best)) best = ms;  // rep 0 warms up
     }
-    CK(cudaEventDestroy(e0));
-    CK(cudaEventDestroy(e1));
     const double flops = 2.0 * PROBE_CHAINS * (double)iters * (double)blocks * PROBE_THREADS;
     tflops = best > 0.0f ? flops / (best * 1e-3) / 1e12 : 0.0;
     return OCL_GB300_OK;

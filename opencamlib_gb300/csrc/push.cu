@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     }
 }
 
-static int ensure_push_index(Mesh& m, int dir) {
+int ensure_push_index(Mesh& m, int dir) {
     PushIndex& pi = m.push[dir];
     if (pi.built) return OCL_GB300_OK;
     KDTreeD kd;

@@ -11,6 +11,13 @@ namespace oclg {
 
 void set_error(const std::string& msg);
 
+// Key of the calling thread's current CUDA context: the driver's context id
+// (unique for the life of the process, so a context created after a device
+// reset gets a new key), or device ordinal + 1 where the driver does not
+// report ids.  Caches of device state (workspaces, function attributes,
+// symbol addresses) are keyed by it.  Returns 0 and sets the error on failure.
+uint64_t context_key();
+
 // Evaluate a CUDA call; on failure record the message and return DEVICE_ERROR
 // (or OOM for allocation failures) from the enclosing function.
 #define CK(call)                                                                         \

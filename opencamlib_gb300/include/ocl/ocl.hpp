@@ -72,6 +72,23 @@ class Point {
     const Point operator*(const double& a) const { return Point(*this) *= a; }
     bool operator==(const Point& p) const { return x == p.x && y == p.y && z == p.z; }
     bool operator!=(const Point& p) const { return !(*this == p); }
+    // rotations about the x, y, z axes (src/geo/point.cpp:105-134): the
+    // point times a rotation matrix, each row summed left to right
+    void xRotate(double theta) {
+        matrixRotate(1, 0, 0, 0, std::cos(theta), -std::sin(theta), 0, std::sin(theta), std::cos(theta));
+    }
+    void yRotate(double theta) {
+        matrixRotate(std::cos(theta), 0, std::sin(theta), 0, 1, 0, -std::sin(theta), 0, std::cos(theta));
+    }
+    void zRotate(double theta) {
+        matrixRotate(std::cos(theta), -std::sin(theta), 0, std::sin(theta), std::cos(theta), 0, 0, 0, 1);
+    }
+    void matrixRotate(double a, double b, double c, double d, double e, double f, double g, double h, double i) {
+        const double xr = a * x + b * y + c * z;
+        const double yr = d * x + e * y + f * z;
+        const double zr = g * x + h * y + i * z;
+        x = xr; y = yr; z = zr;
+    }
     std::string str() const {
         std::ostringstream o;
         o << "(" << x << ", " << y << ", " << z << ")";
@@ -165,6 +182,15 @@ class Triangle {
     Point n;
     Bbox bb;
     Point upNormal() const { return (n.z < 0) ? -1.0 * n : n; }
+    // Triangle::rotate (src/geo/triangle.cpp:130-138)
+    void rotate(double xr, double yr, double zr) {
+        for (int k = 0; k < 3; ++k) {
+            p[k].xRotate(xr);
+            p[k].yRotate(yr);
+            p[k].zRotate(zr);
+        }
+        calc();
+    }
 
    private:
     void calc() {
@@ -187,6 +213,18 @@ class STLSurf {
         bb.addPoint(t.p[0]);
         bb.addPoint(t.p[1]);
         bb.addPoint(t.p[2]);
+        ++version_;
+    }
+    // STLSurf::rotate (src/geo/stlsurf.cpp:44-55): every triangle rotated,
+    // the bounding box rebuilt; the device copy is made again on next use
+    void rotate(double xr, double yr, double zr) {
+        bb.clear();
+        for (Triangle& t : tris) {
+            t.rotate(xr, yr, zr);
+            bb.addPoint(t.p[0]);
+            bb.addPoint(t.p[1]);
+            bb.addPoint(t.p[2]);
+        }
         ++version_;
     }
     unsigned int size() const { return static_cast<unsigned int>(tris.size()); }

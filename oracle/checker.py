@@ -69,6 +69,8 @@ def _lib(which: str):
     if which == "port":
         L.oracle_overlap_pairs.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long, C.c_int]
         L.oracle_overlap_pairs.restype = C.c_long
+        L.oracle_overlap_sets.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long, C.c_int, _i64p, _ip, C.c_long]
+        L.oracle_overlap_sets.restype = C.c_long
         L.oracle_cutter_fields.argtypes = [cd, _dp]
         L.oracle_cutter_fields.restype = C.c_int
         L.oracle_last_loop_seconds.restype = C.c_double
@@ -79,6 +81,8 @@ def _lib(which: str):
         L.ref_stl_read.restype = C.c_long
         L.ref_line_filter.argtypes = [_dp, C.c_long, C.c_double, _dp, C.c_long]
         L.ref_line_filter.restype = C.c_long
+        L.ref_rotate.argtypes = [_dp, C.c_long, C.c_double, C.c_double, C.c_double, _dp, _dp]
+        L.ref_rotate.restype = C.c_int
     _libs[which] = L
     return L
 
@@ -204,6 +208,27 @@ def overlap_pairs(tris, radius, cl, nthreads=0):
     return L.oracle_overlap_pairs(_ptr(tris), tris.shape[0], radius, _ptr(cl), cl.shape[0], nthreads)
 
 
+def overlap_sets(tris, radius, cl, nthreads=0):
+    """Exact overlap sets S(cl) as the reference forms them (KD search, then
+    MillingCutter::overlaps): (offsets[M+1], ids) with ascending insertion
+    indices of point i in ids[offsets[i]:offsets[i+1]]."""
+    L = _lib("port")
+    tris = _d(tris).reshape(-1, 9)
+    cl = _d(cl).reshape(-1, 3)
+    M = cl.shape[0]
+    counts = np.zeros(M, dtype=np.int64)
+    total = L.oracle_overlap_sets(_ptr(tris), tris.shape[0], radius, _ptr(cl), M, nthreads, _ptr(counts, _i64p),
+                                  None, 0)
+    if total < 0:
+        raise RuntimeError("overlap_sets failed")
+    ids = np.zeros(max(total, 1), dtype=np.int32)
+    L.oracle_overlap_sets(_ptr(tris), tris.shape[0], radius, _ptr(cl), M, nthreads, _ptr(counts, _i64p),
+                          _ptr(ids, _ip), total)
+    offsets = np.zeros(M + 1, dtype=np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    return offsets, ids[:total]
+
+
 def cutter_fields(cutter):
     L = _lib("port")
     out = np.zeros(4 + 9 * _abi.MAX_SUB)
@@ -240,6 +265,16 @@ def ref_line_filter(xyz, tol) -> np.ndarray:
     out = np.zeros((max(len(a), 1), 3), dtype=np.float64)
     k = L.ref_line_filter(_ptr(a), len(a), float(tol), _ptr(out), len(out))
     return out[:k]
+
+
+def ref_rotate(tris, xr, yr, zr):
+    """The reference's STLSurf::rotate: (rotated (n, 9) triangles, bbox[6])."""
+    L = _lib("ref")
+    t = _d(tris).reshape(-1, 9)
+    out = np.zeros_like(t)
+    bb = np.zeros(6)
+    L.ref_rotate(_ptr(t), t.shape[0], float(xr), float(yr), float(zr), _ptr(out), _ptr(bb))
+    return out, bb
 
 
 def last_loop_seconds() -> float:

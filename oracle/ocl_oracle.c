@@ -967,6 +967,87 @@ long oracle_overlap_pairs(const double* tris, long ntri, double radius, const do
     return total;
 }
 
+/* The exact overlap set S(cl) of BatchDropCutter::dropCutter5
+ * (batchdropcutter.cpp:208-222): KD candidates of the cutter's bbox
+ * (KDTree::search_cutter_overlap kdtree.hpp:130-135) filtered by
+ * MillingCutter::overlaps, as ascending insertion indices.  counts[i] gets
+ * |S(cl_i)|; ids (may be NULL) receives the sets back to back while they fit
+ * in cap.  Returns the total. */
+static int cmp_long(const void* a, const void* b) {
+    long x = *(const long*)a, y = *(const long*)b;
+    return (x > y) - (x < y);
+}
+
+long oracle_overlap_sets(const double* tris, long ntri, double radius, const double* cl, long M,
+                         int nthreads, int64_t* counts, int32_t* ids, long cap) {
+    ocl_gb300_cutter cd;
+    memset(&cd, 0, sizeof(cd));
+    cd.kind = OCL_CUTTER_CYL;
+    cd.base.kind = OCL_CUTTER_CYL;
+    cd.base.diameter = 2.0 * radius;
+    cd.base.length = 1.0;
+    Scene S;
+    if (scene_init(&S, tris, ntri, &cd, 1, 0) != 0) return -1;
+    S.cutter.radius = radius;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+    {
+        LVec buf = {0, 0, 0};
+#pragma omp for schedule(dynamic, 16)
+        for (long i = 0; i < M; ++i) {
+            CL p;
+            memset(&p, 0, sizeof(p));
+            p.x = cl[3 * i];
+            p.y = cl[3 * i + 1];
+            p.z = cl[3 * i + 2];
+            double bb[6] = {p.x - radius, p.x + radius, p.y - radius, p.y + radius, p.z, p.z + 1.0};
+            buf.n = 0;
+            if (ntri > 0) kd_search(&S.kd, 0, bb, &buf);
+            long n = 0;
+            for (long k = 0; k < buf.n; ++k)
+                if (overlaps(&S.cutter, &p, &S.tris[buf.v[k]])) ++n;
+            counts[i] = n;
+        }
+        free(buf.v);
+    }
+    long total = 0;
+    for (long i = 0; i < M; ++i) total += counts[i];
+    if (ids && total <= cap) {
+        long* start = (long*)malloc(sizeof(long) * (M > 0 ? M : 1));
+        long acc = 0;
+        for (long i = 0; i < M; ++i) {
+            start[i] = acc;
+            acc += counts[i];
+        }
+#pragma omp parallel
+        {
+            LVec buf = {0, 0, 0};
+#pragma omp for schedule(dynamic, 16)
+            for (long i = 0; i < M; ++i) {
+                CL p;
+                memset(&p, 0, sizeof(p));
+                p.x = cl[3 * i];
+                p.y = cl[3 * i + 1];
+                p.z = cl[3 * i + 2];
+                double bb[6] = {p.x - radius, p.x + radius, p.y - radius, p.y + radius, p.z, p.z + 1.0};
+                buf.n = 0;
+                if (ntri > 0) kd_search(&S.kd, 0, bb, &buf);
+                long n = 0;
+                for (long k = 0; k < buf.n; ++k)
+                    if (overlaps(&S.cutter, &p, &S.tris[buf.v[k]])) buf.v[n++] = buf.v[k];
+                qsort(buf.v, (size_t)n, sizeof(long), cmp_long);
+                for (long k = 0; k < n; ++k) ids[start[i] + k] = (int32_t)buf.v[k];
+            }
+            free(buf.v);
+        }
+        free(start);
+    }
+    scene_free(&S);
+    return total;
+}
+
 int oracle_kd_order(const double* tris, long ntri, unsigned bucket, int dims, int64_t* order) {
     Tri* T = (Tri*)malloc(sizeof(Tri) * (ntri > 0 ? ntri : 1));
     for (long i = 0; i < ntri; ++i) tri_init(&T[i], tris + 9 * i);

@@ -54,10 +54,16 @@ OCL_CHECKER_DECLS(ref_)
 /* Exact-overlap candidate count sum_cl |S(cl)| (MillingCutter::overlaps). */
 long oracle_overlap_pairs(const double* tris, long ntri, double radius,
                           const double* cl, long M, int nthreads);
+/* Exact overlap sets S(cl) (KD search + overlaps, as dropCutter5), ascending
+ * insertion indices per point; returns the total (ids filled if it fits cap). */
+long oracle_overlap_sets(const double* tris, long ntri, double radius, const double* cl, long M,
+                         int nthreads, int64_t* counts, int32_t* ids, long cap);
 
 int oracle_cutter_fields(const ocl_gb300_cutter* c, double* out);
 double oracle_last_loop_seconds(void);
 int ref_preset_fields(int preset, const double* args, double* out);
+/* STLSurf::rotate on a triangle list: rotated triangles and the surface bbox. */
+int ref_rotate(const double* tris, long ntri, double xr, double yr, double zr, double* out, double* bb);
 
 #ifdef __cplusplus
 }

@@ -334,6 +334,30 @@ long ref_line_filter(const double* xyz, long n, double tol, double* out, long ca
     return k;
 }
 
+// STLSurf::rotate(xr, yr, zr) on ntri triangles: the rotated triangles in
+// order (p1 p2 p3) into out (9 ntri) and the surface bbox into bb[6]
+// (Bbox::operator[] order).
+int ref_rotate(const double* tris, long ntri, double xr, double yr, double zr, double* out, double* bb) {
+    ocl::STLSurf surf;
+    for (long i = 0; i < ntri; ++i) {
+        const double* v = tris + 9 * i;
+        surf.addTriangle(ocl::Triangle(ocl::Point(v[0], v[1], v[2]), ocl::Point(v[3], v[4], v[5]),
+                                       ocl::Point(v[6], v[7], v[8])));
+    }
+    surf.rotate(xr, yr, zr);
+    long n = 0;
+    for (const ocl::Triangle& t : surf.tris) {
+        for (int k = 0; k < 3; ++k) {
+            out[9 * n + 3 * k] = t.p[k].x;
+            out[9 * n + 3 * k + 1] = t.p[k].y;
+            out[9 * n + 3 * k + 2] = t.p[k].z;
+        }
+        ++n;
+    }
+    for (unsigned k = 0; k < 6; ++k) bb[k] = surf.bb[k];
+    return 0;
+}
+
 // preset: 1 CompCyl(d,l) 2 CompBall(d,l) 3 CylCone(d1,d2,a) 4 BallCone(d1,d2,a)
 //         5 BullCone(d1,r1,d2,a) 6 ConeCone(d1,a1,d2,a2)
 int ref_preset_fields(int preset, const double* a, double* out) {

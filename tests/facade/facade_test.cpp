@@ -4,6 +4,15 @@
 //   facade_test drop <tris.bin> <cl.bin> <out.bin> <cutter> <args...>
 //   facade_test push <tris.bin> <fibers.bin> <out.bin> <dir 0|1> <cutter> <args...>
 //   facade_test path <tris.bin> <spans.bin> <out.bin> <sampling> <minz> <cutter> <args...>
+//   facade_test apdc <tris.bin> <spans.bin> <out.bin> <sampling> <min_sampling> <cos_limit> <cutter> <args...>
+//   facade_test rotate <tris.bin> <angles.bin> <out.bin>
+//   facade_test stldrop <file.stl> <cl.bin> <out.bin> <cutter> <args...>
+//
+// rotate: STLSurf::rotate(xr, yr, zr); output the triangles, then the bbox (6).
+// stldrop: STLReader -> STLSurf -> BatchDropCutter, three runs on one
+// surface: as read; after addTriangle of a horizontal triangle over the
+// surface's bbox at maxz + 1; after rotate(0, 0, pi/2).  Output: the three
+// runs' points one after the other (the device copy must follow each change).
 //
 // tris.bin: N x 9 doubles; cl.bin: M x 3; fibers.bin: F x 6; spans.bin: S x 11.
 // cutter: cyl d l | ball d l | bull d r l | cone d angle l | ballcone d1 d2 angle
@@ -40,18 +49,80 @@ static std::unique_ptr<ocl::MillingCutter> make_cutter(int argc, char** argv, in
 }
 
 int main(int argc, char** argv) {
-    if (argc < 6) {
-        std::fprintf(stderr, "usage: facade_test drop|push|path ...\n");
+    if (argc < 5) {
+        std::fprintf(stderr, "usage: facade_test drop|push|path|apdc|rotate|stldrop ...\n");
         return 2;
     }
     std::string mode = argv[1];
-    std::vector<double> T = load(argv[2]), P = load(argv[3]);
+    std::vector<double> T = mode == "stldrop" ? std::vector<double>() : load(argv[2]), P = load(argv[3]);
     ocl::STLSurf surf;
     for (size_t i = 0; i + 9 <= T.size(); i += 9)
         surf.addTriangle(ocl::Triangle(ocl::Point(T[i], T[i + 1], T[i + 2]), ocl::Point(T[i + 3], T[i + 4], T[i + 5]),
                                        ocl::Point(T[i + 6], T[i + 7], T[i + 8])));
     std::vector<double> out;
-    if (mode == "drop") {
+    auto put_points = [&out](std::vector<ocl::CLPoint> pts) {
+        for (ocl::CLPoint& p : pts) {
+            ocl::CCPoint cc = p.getCC();
+            double r[7] = {p.x, p.y, p.z, cc.x, cc.y, cc.z, (double)cc.type};
+            out.insert(out.end(), r, r + 7);
+        }
+    };
+    if (mode == "rotate") {
+        if (P.size() < 3) return 2;
+        surf.rotate(P[0], P[1], P[2]);
+        for (const ocl::Triangle& t : surf.tris)
+            for (int k = 0; k < 3; ++k) {
+                out.push_back(t.p[k].x);
+                out.push_back(t.p[k].y);
+                out.push_back(t.p[k].z);
+            }
+        for (unsigned k = 0; k < 6; ++k) out.push_back(surf.bb[k]);
+    } else if (mode == "stldrop") {
+        std::string path = argv[2];
+        std::wstring wp(path.begin(), path.end());
+        ocl::STLReader reader(wp, surf);
+        auto cutter = make_cutter(argc, argv, 5);
+        ocl::BatchDropCutter bdc;
+        bdc.setSTL(surf);
+        bdc.setCutter(cutter.get());
+        for (int run = 0; run < 3; ++run) {
+            if (run == 1) {
+                const double z = surf.bb[5] + 1.0;
+                surf.addTriangle(ocl::Triangle(ocl::Point(surf.bb[0] - 10, surf.bb[2] - 10, z),
+                                               ocl::Point(surf.bb[1] + 30, surf.bb[2] - 10, z),
+                                               ocl::Point(surf.bb[0] - 10, surf.bb[3] + 30, z)));
+            } else if (run == 2) {
+                surf.rotate(0.0, 0.0, 1.5707963267948966);
+            }
+            bdc.clearCLPoints();
+            for (size_t i = 0; i + 3 <= P.size(); i += 3) {
+                ocl::CLPoint p(P[i], P[i + 1], P[i + 2]);
+                bdc.appendPoint(p);
+            }
+            bdc.run();
+            if (!bdc.lastError().empty()) return 1;
+            put_points(bdc.getCLPoints());
+        }
+    } else if (mode == "apdc") {
+        double sampling = std::atof(argv[5]), minsamp = std::atof(argv[6]), coslim = std::atof(argv[7]);
+        auto cutter = make_cutter(argc, argv, 8);
+        ocl::Path path;
+        for (size_t i = 0; i + 11 <= P.size(); i += 11) {
+            ocl::Point p1(P[i + 1], P[i + 2], P[i + 3]), p2(P[i + 4], P[i + 5], P[i + 6]), c(P[i + 7], P[i + 8], P[i + 9]);
+            if (P[i] == 0.0) path.append(ocl::Line(p1, p2));
+            else path.append(ocl::Arc(p1, p2, c, P[i + 10] != 0.0));
+        }
+        ocl::AdaptivePathDropCutter apdc;
+        apdc.setSTL(surf);
+        apdc.setCutter(cutter.get());
+        apdc.setPath(&path);
+        apdc.setSampling(sampling);
+        apdc.setMinSampling(minsamp);
+        apdc.setCosLimit(coslim);
+        apdc.run();
+        if (!apdc.lastError().empty()) return 1;
+        put_points(apdc.getPoints());
+    } else if (mode == "drop") {
         auto cutter = make_cutter(argc, argv, 5);
         ocl::BatchDropCutter bdc;
         bdc.setSTL(surf);

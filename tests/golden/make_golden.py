@@ -6,7 +6,11 @@ cases and stores inputs and outputs as .npz files.  Needs the reference
 source tree (oracle/Makefile REF_SRC); the fixtures are committed so that
 the GPU tests run without it.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--real]
+
+The real-mesh fixtures (real_*.npz) are made from the reference's stl/
+folder next to its sources (REF_SRC, as for oracle/Makefile) when missing or
+with --real.
 """
 from __future__ import annotations
 
@@ -59,6 +63,43 @@ def path_case(name, tris, spans):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
+# Real meshes shipped with the reference (its stl/ folder), read by the
+# reference's own STLReader; the CL raster covers each mesh's bbox widened by
+# 4 mm, starting 10 mm below it.
+REAL_MESHES = ("sphere_on_plate", "30sphere", "mount_rush", "wheel_in_box")
+REAL_CUTTERS = ("cyl", "ball", "bull", "cone", "ballcone")
+
+
+def real_mesh_case(name, stl_dir):
+    tris = ck.ref_stl_read(os.path.join(stl_dir, name + ".stl"))
+    t32 = tris.astype(np.float32)
+    assert np.array_equal(t32.astype(np.float64), tris)  # STL coordinates are float32
+    lo, hi = tris.reshape(-1, 3).min(axis=0), tris.reshape(-1, 3).max(axis=0)
+    n = 32
+    xs = np.linspace(lo[0] - 4.0, hi[0] + 4.0, n) + 0.0123
+    ys = np.linspace(lo[1] - 4.0, hi[1] + 4.0, n) + 0.0071
+    X, Y = np.meshgrid(xs, ys)
+    cl = np.stack([X.ravel(), Y.ravel(), np.full(X.size, lo[2] - 10.0)], axis=1)
+    out = {"tris": t32, "cl": cl}
+    for cname in REAL_CUTTERS:
+        z, cc, ty, _ = ck.drop(tris, CUTTERS[cname](), cl, "ref")
+        out[f"{cname}_z"], out[f"{cname}_cc"], out[f"{cname}_type"] = z, cc, ty
+    if name == "sphere_on_plate":
+        zs = lo[2] + (hi[2] - lo[2]) * np.array([0.15, 0.5, 0.85])
+        fx = np.concatenate([w.fibers(0, z, lo[1] - 2, hi[1] + 2, 25, lo[0] - 8, hi[0] + 8) for z in zs])
+        fy = np.concatenate([w.fibers(1, z, lo[0] - 2, hi[0] + 2, 25, lo[1] - 8, hi[1] + 8) for z in zs])
+        out["fib_x"], out["fib_y"] = fx, fy
+        for cname in ("ball", "bull"):
+            for d, fib in ((0, fx), (1, fy)):
+                res, _ = ck.push(tris, CUTTERS[cname](), d, fib, "ref")
+                flat = [iv for r in res for iv in r]
+                out[f"{cname}_{d}_counts"] = np.array([len(r) for r in res], dtype=np.int32)
+                out[f"{cname}_{d}_ival"] = np.array([[iv[0], iv[1]] for iv in flat]).reshape(-1, 2)
+                out[f"{cname}_{d}_cc"] = np.array([np.concatenate([iv[2], iv[3]]) for iv in flat]).reshape(-1, 6)
+                out[f"{cname}_{d}_type"] = np.array([[iv[4], iv[5]] for iv in flat], dtype=np.int32).reshape(-1, 2)
+    np.savez_compressed(os.path.join(HERE, "real_" + name + ".npz"), **out)
+
+
 def main():
     ck.build(ref=True)
     if not ck.available("ref"):
@@ -75,6 +116,10 @@ def main():
     path_case("path_heightfield", hf, path_spans())
     orders = {f"dims{d}_b{b}": ck.kd_order(hf, "ref", b, d) for d in (0, 1, 2) for b in (1, 3)}
     np.savez_compressed(os.path.join(HERE, "kd_order.npz"), tris=hf, **orders)
+    stl_dir = os.path.join(os.path.dirname(os.environ.get("REF_SRC", "/root/reference/src").rstrip("/")), "stl")
+    if "--real" in sys.argv or not all(os.path.exists(os.path.join(HERE, f"real_{m}.npz")) for m in REAL_MESHES):
+        for m in REAL_MESHES:
+            real_mesh_case(m, stl_dir)
     print("golden fixtures written to", HERE)
 
 

@@ -10,10 +10,11 @@ def golden(name):
     return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
 
 
-def push_records_equal(res, g, prefix, exact=True, sort=False, tol=0.0):
+def push_records_equal(res, g, prefix, exact=True, sort=False, tol=0.0, cc_tol=1e-6):
     """Compare per-fiber interval records with a golden set.  With sort=True
     both sides are ordered by lower t (the GPU returns sorted intervals, the
-    reference keeps insertion order)."""
+    reference keeps insertion order).  exact=False: endpoints within tol (in
+    fiber parameter t), CC points within cc_tol mm, CC types identical."""
     counts = g[prefix + "_counts"]
     ival = g[prefix + "_ival"]
     cc = g[prefix + "_cc"]
@@ -38,3 +39,5 @@ def push_records_equal(res, g, prefix, exact=True, sort=False, tol=0.0):
                 assert a[4] == b[4] and a[5] == b[5]
             else:
                 assert abs(a[0] - b[0]) <= tol and abs(a[1] - b[1]) <= tol, (f, a[:2], b[:2])
+                assert a[4] == b[4] and a[5] == b[5], (f, a[4:], b[4:])
+                assert np.max(np.abs(a[2] - b[2])) <= cc_tol and np.max(np.abs(a[3] - b[3])) <= cc_tol, (f, a, b)

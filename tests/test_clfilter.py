@@ -35,8 +35,9 @@ def check_against_reference(xyz, tol):
     keep = _native.line_filter(xyz, tol)
     assert len(xyz) == 0 or keep[0] == 0
     assert np.all(np.diff(keep) > 0)
-    if checker.available("ref"):
-        np.testing.assert_array_equal(xyz[keep], checker.ref_line_filter(xyz, tol))
+    if not checker.available("ref"):
+        pytest.skip("the reference build (oracle/_ref) needs the reference sources, absent on this machine")
+    np.testing.assert_array_equal(xyz[keep], checker.ref_line_filter(xyz, tol))
     return keep
 
 

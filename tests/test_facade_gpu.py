@@ -50,18 +50,76 @@ def test_facade_push(exe, tmp_path, cname):
     out = _run(exe, tmp_path, "push", g["tris"], g["fib_x"], ["0"] + ARGS[cname])
     counts = g[f"{cname}_0_counts"]
     k = 0
-    ival = g[f"{cname}_0_ival"]
+    ival, cc, ty = g[f"{cname}_0_ival"], g[f"{cname}_0_cc"], g[f"{cname}_0_type"]
     j = 0
     for n in counts:
         assert int(out[k]) == n
         k += 1
         for _ in range(int(n)):
-            assert abs(out[k] - ival[j, 0]) < 1e-9 and abs(out[k + 1] - ival[j, 1]) < 1e-9
+            # lower upper lcc(3) ucc(3) ltype utype, as the reference's Interval
+            assert out[k] == ival[j, 0] and out[k + 1] == ival[j, 1]
+            np.testing.assert_array_equal(out[k + 2:k + 8], cc[j])
+            assert (int(out[k + 8]), int(out[k + 9])) == tuple(ty[j])
             k += 10
             j += 1
+    assert k == len(out)
 
 
 def test_facade_path(exe, tmp_path):
     g = golden("path_heightfield")
     out = _run(exe, tmp_path, "path", g["tris"], g["spans"], ["0.37", "-5.0"] + ARGS["ball"]).reshape(-1, 7)
     assert np.max(np.abs(out[:, :3] - g["ball_pdc_xyz"])) <= 1e-7
+
+
+@pytest.mark.parametrize("cname", ["ball", "cone", "ballcone"])
+def test_facade_adaptive_path(exe, tmp_path, cname):
+    g = golden("path_heightfield")
+    out = _run(exe, tmp_path, "apdc", g["tris"], g["spans"], ["0.8", "0.05", "0.999"] + ARGS[cname]).reshape(-1, 7)
+    assert out.shape[0] == len(g[f"{cname}_apdc_xyz"])  # the reference's points, in its order
+    assert np.max(np.abs(out[:, :3] - g[f"{cname}_apdc_xyz"])) <= 1e-7
+    np.testing.assert_array_equal(out[:, 6].astype(np.int32), g[f"{cname}_apdc_type"])
+
+
+def test_facade_stlreader_surface_cache(exe, oracle_lib, tmp_path):
+    # STLReader -> STLSurf -> BatchDropCutter, then addTriangle, then rotate:
+    # each run must see the surface as it is (the device copy is rebuilt)
+    g = golden("drop_heightfield")
+    t32 = g["tris"].astype(np.float32)
+    stl = tmp_path / "hf.stl"
+    with open(stl, "w") as f:
+        f.write("solid hf\n")
+        for t in t32:
+            f.write("facet normal 0 0 1\nouter loop\n")
+            for k in range(3):
+                f.write("vertex %.9g %.9g %.9g\n" % (t[3 * k], t[3 * k + 1], t[3 * k + 2]))
+            f.write("endloop\nendfacet\n")
+        f.write("endsolid hf\n")
+    cl = g["cl"][::4]
+    c = ARGS["ball"]
+    cl_path = tmp_path / "cl.bin"
+    np.ascontiguousarray(cl).tofile(cl_path)
+    o = tmp_path / "o.bin"
+    import subprocess
+    r = subprocess.run([exe, "stldrop", str(stl), str(cl_path), str(o)] + c, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = np.fromfile(o, dtype=np.float64).reshape(3, len(cl), 7)
+    tris = t32.astype(np.float64)
+    from tests.golden.cases import CUTTERS
+    ball = CUTTERS["ball"]()
+    # run 1: the surface as read
+    assert np.abs(out[0, :, 2] - oracle_lib.drop(tris, ball, cl, "port")[0]).max() <= 1e-5
+    # run 2: plus a horizontal triangle over everything at maxz + 1
+    lo, hi = tris.reshape(-1, 3).min(axis=0), tris.reshape(-1, 3).max(axis=0)
+    z = hi[2] + 1.0
+    extra = np.array([[lo[0] - 10, lo[1] - 10, z, hi[0] + 30, lo[1] - 10, z, lo[0] - 10, hi[1] + 30, z]])
+    t2 = np.concatenate([tris, extra])
+    assert np.abs(out[1, :, 2] - oracle_lib.drop(t2, ball, cl, "port")[0]).max() <= 1e-5
+    # run 3: rotated a quarter turn about z (STLSurf::rotate)
+    if oracle_lib.available("ref"):
+        t3, _ = oracle_lib.ref_rotate(t2, 0.0, 0.0, 1.5707963267948966)
+    else:
+        from opencamlib_gb300 import api
+        s3 = api.STLSurf(t2)
+        s3.rotate(0.0, 0.0, 1.5707963267948966)
+        t3 = s3.array()
+    assert np.abs(out[2, :, 2] - oracle_lib.drop(t3, ball, cl, "port")[0]).max() <= 1e-5

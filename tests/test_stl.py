@@ -58,8 +58,9 @@ def ref_available():
 
 
 def same_as_reference(path):
-    if ref_available():
-        np.testing.assert_array_equal(_native.stl_read(path, strict=False), checker.ref_stl_read(path))
+    if not ref_available():
+        pytest.skip("the reference build (oracle/_ref) needs the reference sources, absent on this machine")
+    np.testing.assert_array_equal(_native.stl_read(path, strict=False), checker.ref_stl_read(path))
 
 
 @pytest.mark.parametrize("fmt", ["ascii", "ascii_crlf", "binary"])
