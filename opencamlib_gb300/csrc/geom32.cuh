@@ -367,10 +367,13 @@ struct BullEdge32 {
     float u1, u2, m, dm, L, A, B, az;
 };
 
-// f'(u) times rho (same sign as f'; no division)
+// f'(u) times rho (same sign as f'; no division).  At rho = 0 -- the CL
+// point on the edge line (dm = 0) and u = 0 -- the product vanishes, but there
+// f' = m (the flat bottom has h' = 0), so m itself is returned: a zero would
+// stop the bisection at u = 0, short of the maximiser on the torus.
 __device__ __forceinline__ float bull_fp32(const Prof32& c, const BullEdge32& b, float u) {
     const float rho = sqrtf(u * u + b.dm * b.dm);
-    return b.m * rho - dh32(c, rho) * u;
+    return rho > 0.0f ? b.m * rho - dh32(c, rho) * u : b.m;
 }
 
 // Edge n of the triangle (local vertices px/py/pz); false: no contact.

@@ -74,6 +74,8 @@ def _lib(which: str):
         L.oracle_cutter_fields.argtypes = [cd, _dp]
         L.oracle_cutter_fields.restype = C.c_int
         L.oracle_last_loop_seconds.restype = C.c_double
+        L.oracle_edge_contact.argtypes = [cd, C.c_double, C.c_double, _dp, _dp, _dp, _dp]
+        L.oracle_edge_contact.restype = C.c_int
     else:
         L.ref_preset_fields.argtypes = [C.c_int, _dp, _dp]
         L.ref_preset_fields.restype = C.c_int
@@ -227,6 +229,18 @@ def overlap_sets(tris, radius, cl, nthreads=0):
     offsets = np.zeros(M + 1, dtype=np.int64)
     np.cumsum(counts, out=offsets[1:])
     return offsets, ids[:total]
+
+
+def edge_contact(cutter, x, y, p1, p2):
+    """singleEdgeDrop of one edge on its own: (status, clz, cc) with status 1
+    when the CC lies on the segment, 0 when not, -1 beyond the radius."""
+    L = _lib("port")
+    a, b = _d(p1).reshape(3), _d(p2).reshape(3)
+    clz = C.c_double(0.0)
+    cc = np.zeros(3)
+    desc = cutter.desc()
+    st = L.oracle_edge_contact(C.byref(desc), float(x), float(y), _ptr(a), _ptr(b), C.byref(clz), _ptr(cc))
+    return st, clz.value, cc
 
 
 def cutter_fields(cutter):

@@ -705,6 +705,33 @@ static int single_edge_drop(const Cutter* c, CL* cl, P3 p1, P3 p2, double d, Ctx
     return 0;
 }
 
+/* One edge's contact (MillingCutter::singleEdgeDrop millingcutter.cpp:100-136)
+ * for a CL point at (x, y) on its own: 1 and clz, cc[3] when the CC lies on
+ * the segment, 0 when it does not, -1 when the line is beyond the radius. */
+int oracle_edge_contact(const ocl_gb300_cutter* cd, double x, double y, const double* a, const double* b,
+                        double* clz, double* cc) {
+    Cutter c;
+    if (cutter_make(&c, cd) != 0) return -2;
+    CL cl;
+    memset(&cl, 0, sizeof(cl));
+    cl.x = x;
+    cl.y = y;
+    cl.z = -1e300;
+    P3 p1 = pt(a[0], a[1], a[2]), p2 = pt(b[0], b[1], b[2]);
+    double d = xy_distance_to_line(clp(&cl), p1, p2);
+    int r = -1;
+    if (d <= c.radius) {
+        Ctx ctx = {0};
+        r = single_edge_drop(&c, &cl, p1, p2, d, &ctx);
+        *clz = cl.z;
+        cc[0] = cl.cc.p.x;
+        cc[1] = cl.cc.p.y;
+        cc[2] = cl.cc.p.z;
+    }
+    cutter_free(&c);
+    return r;
+}
+
 /* MillingCutter::edgeDrop millingcutter.cpp:79-94 */
 static int edge_drop_basic(const Cutter* c, CL* cl, const Tri* t, Ctx* ctx) {
     int result = 0;

@@ -60,6 +60,10 @@ long oracle_overlap_sets(const double* tris, long ntri, double radius, const dou
                          int nthreads, int64_t* counts, int32_t* ids, long cap);
 
 int oracle_cutter_fields(const ocl_gb300_cutter* c, double* out);
+/* One edge's contact for a CL point (singleEdgeDrop): 1 with clz and cc[3]
+ * when the CC lies on the segment, 0 when not, -1 beyond the radius. */
+int oracle_edge_contact(const ocl_gb300_cutter* c, double x, double y, const double* p1, const double* p2,
+                        double* clz, double* cc);
 double oracle_last_loop_seconds(void);
 int ref_preset_fields(int preset, const double* args, double* out);
 /* STLSurf::rotate on a triangle list: rotated triangles and the surface bbox. */
