@@ -54,6 +54,12 @@ def parse():
     ap.add_argument("--block-origin", default="400,300", help="raster column,row of the block's corner")
     ap.add_argument("--stride", type=int, default=0,
                     help="only every S-th raster point along x and y (a small case spanning the whole mesh)")
+    ap.add_argument("--oracle-sample", type=int, default=4000,
+                    help="CL points per cutter compared with the CPU oracle (precision_vs_oracle)")
+    ap.add_argument("--no-fp64-full", action="store_true",
+                    help="skip the plain FP64 run over the whole raster (mixed == FP64 check and speed-up)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run one device step with statistics, print its counters and exit (for ncu)")
     return ap.parse_args()
 
 
@@ -289,6 +295,89 @@ def block_indices(side, i0=400, j0=300):
     return (jj * 1000 + ii).ravel()
 
 
+def mixed_vs_fp64(mesh, cl, cuts):
+    """Per cutter, the mixed path and the plain FP64 kernel (the reference's
+    KD-tree algorithm on the device) over the same points: results compared
+    bit for bit, device times from the library's CUDA events."""
+    out = {}
+    for name, c in cuts:
+        z64, cc64, ty64, s64 = mesh.drop(c, cl, "fp64")
+        zm, ccm, tym, sm = mesh.drop(c, cl, "mixed")
+        dz = np.abs(zm - z64)
+        out[name] = {"points": int(len(cl)), "max_dz_mm": float(dz.max()), "rms_dz_mm": float(np.sqrt(np.mean(dz * dz))),
+                     "cctype_match": float(np.mean(tym == ty64)), "cc_max_diff_mm": float(np.abs(ccm - cc64).max()),
+                     "bit_identical": bool(np.array_equal(zm, z64) and np.array_equal(ccm, cc64)
+                                           and np.array_equal(tym, ty64)),
+                     "fp64_kernel_ms": s64.kernel_ms, "mixed_kernel_ms": sm.kernel_ms,
+                     "speedup": s64.kernel_ms / max(sm.kernel_ms, 1e-9), "exact_pairs": int(s64.pairs),
+                     "violations": int(sm.violations)}
+    return out
+
+
+def precision_vs_oracle(mesh, tris, cl_full, cuts, sample):
+    """Per cutter, the mixed path against the CPU oracle (the C restatement
+    pinned bit for bit to the reference build) on a seeded sample of the
+    raster: max / RMS |dz|, CC type agreement, CC point difference."""
+    from oracle import checker
+    checker.build(ref=False)
+    pts = cl_full[sample_indices(sample, seed=29)]
+    out = {}
+    for name, c in cuts:
+        zm, ccm, tym, _ = mesh.drop(c, pts, "mixed")
+        zr, ccr, tyr, _ = checker.drop(tris, c, pts, "port")
+        dz = np.abs(zm - zr)
+        lifted = tyr != 0
+        out[name] = {"points": int(len(pts)), "max_dz_mm": float(dz.max()), "rms_dz_mm": float(np.sqrt(np.mean(dz * dz))),
+                     "cctype_match": float(np.mean(tym == tyr)),
+                     "cc_max_diff_mm": float(np.abs(ccm[lifted] - ccr[lifted]).max(initial=0.0)),
+                     "oracle": "oracle/ocl_oracle.c (C restatement of BatchDropCutter::dropCutter5, "
+                               "pinned to the reference build), seeded uniform sample of the raster"}
+    return out
+
+
+def roofline_block(tris, M, cuts, breakdown, stage, args, compute):
+    """Compute roofline of the timed step (FP32 screen + FP64 refinement
+    against the device's measured FMA peaks; frozen per-pair operation
+    counts from opencamlib_gb300.roofline), with the HBM view beside it."""
+    from opencamlib_gb300 import roofline as rf
+    names = [n for n, _ in cuts]
+    step_s = float(stage[:, 3].sum()) / args.steps / 1e3
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = tris.shape[0] * 72 + M * (24 + 36)
+    screen_ms = float(stage[:, 0].mean())
+    traffic = None
+    if not (args.block or args.stride) and all(rf.SCREEN_DRAM_BYTES.get(n) for n in names):
+        traffic = sum(rf.SCREEN_DRAM_BYTES[n] for n in names) / len(names)
+    hbm_view = {"bound": "hbm", "kernel": "k_drop_screen (per call)", "achieved": alg_bytes / (screen_ms / 1e3) / 1e9,
+                "peak": hbm, "unit": "GB/s", "frac": alg_bytes / (screen_ms / 1e3) / 1e9 / hbm, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes, "per_launch_ms": screen_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
+    if not rf.measured(names) or not compute or "fp32_tflops" not in compute:
+        hbm_view["note"] = "per-pair operation counts not measured yet: HBM view only (the path is not HBM-bound)"
+        return hbm_view
+    counts = {n: (int(st.screened), int(st.refined)) for n, st in breakdown}
+    p32, p64 = compute["fp32_tflops"] * 1e12, compute["fp64_tflops"] * 1e12
+    r = rf.step_roofline(counts, step_s, p32, p64)
+    screen_f32 = sum(counts[n][0] * rf.FP32_PER_SCREEN[n] for n in names)
+    return {"bound": "fp32+fp64 issue", "kernel": "drop step: k_drop_screen (FP32) + k_drop_refine / k_bull_eval / "
+                                                  "k_drop_exact / k_drop_kd (FP64)",
+            "achieved": r["achieved_flops_fp32_equiv"] / 1e12, "peak": compute["fp32_tflops"],
+            "unit": "TFLOP/s (FP32-equivalent: FP64 operations x P32/P64)", "frac": r["frac"],
+            "traffic": traffic,
+            "fp32_ops_per_step": r["fp32_ops"], "fp64_ops_per_step": r["fp64_ops"],
+            "t_roof_ms": r["t_roof_s"] * 1e3, "t_step_ms": step_s * 1e3,
+            "screen_fp32_tflops": screen_f32 / (float(stage[:, 0].sum()) / args.steps / 1e3) / 1e12,
+            "peak_source": "ocl_gb300_fma_peaks on this GPU (MEASURED_PEAKS.json has no FP32/FP64 figure)",
+            "ops_source": "opencamlib_gb300/roofline.py (ncu instruction counters per screened pair / refined "
+                          "triangle, profiles/compute_ops_drop_block256.md)",
+            "hbm": hbm_view}
+
+
 def run_reference(args):
     rank, world, local, dist = dist_setup(args.gpus)
     if rank != 0:
@@ -358,6 +447,20 @@ def main():
             if stats_out is not None:
                 stats_out.append((name, st))
 
+    if args.profile_step:
+        # one step with statistics: the launches an ncu capture of this
+        # command sees, with the library's own counters for them
+        rec = []
+        step_device(rec)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_step": {n: {"screened": int(st.screened), "refined": int(st.refined),
+                                               "fallback_points": int(st.fallback), "launches": int(st.launches),
+                                               "kernel_ms": st.kernel_ms, "screen_ms": st.screen_ms,
+                                               "refine_ms": st.refine_ms, "fallback_ms": st.fallback_ms}
+                                           for n, st in rec},
+                          "cl_points": int(M), "triangles": int(tris.shape[0])}), flush=True)
+        return
+
     # warm-up + per-kernel breakdown (stats path syncs; not timed)
     breakdown = []
     for _ in range(max(1, args.warmup)):
@@ -425,47 +528,25 @@ def main():
             dist.destroy_process_group()
         return
 
-    # precision: mixed vs plain FP64 (GPU) on a 200x200 block of the raster,
-    # per cutter, and the plain FP64 kernel's rate on the same block
-    prec = {}
-    fp64_rate = {}
-    pts = cl_full[block_indices(200)]
-    for name, c in cuts:
-        z64, cc64, ty64, s64 = mesh.drop(c, pts, "fp64")
-        zm, ccm, tym, sm = mesh.drop(c, pts, "mixed")
-        dz = np.abs(zm - z64)
-        prec[name] = {"max_dz_mm": float(dz.max()), "rms_dz_mm": float(np.sqrt(np.mean(dz * dz))),
-                      "cctype_match": float(np.mean(tym == ty64)), "points": int(len(pts))}
-        fp64_rate[name] = {"fp64_kernel_ms": s64.kernel_ms, "mixed_kernel_ms": sm.kernel_ms,
-                           "speedup": s64.kernel_ms / max(sm.kernel_ms, 1e-9), "points": int(len(pts)),
-                           "exact_pairs": int(s64.pairs)}
+    # mixed vs plain FP64 on the GPU over the whole timed point set (the
+    # results must be bit-identical), and the plain FP64 kernel's time
+    fp64_full = None
+    if not args.no_fp64_full:
+        fp64_full = mixed_vs_fp64(mesh, cl, cuts)
+    # mixed against the CPU oracle (pinned to the reference) on a seeded sample
+    prec_oracle = None
+    if args.oracle_sample > 0:
+        try:
+            prec_oracle = precision_vs_oracle(mesh, tris, cl_full, cuts, args.oracle_sample)
+        except Exception as e:  # reported, never required
+            prec_oracle = {"error": str(e)}
 
-    # dominant kernel and roofline (algorithmic bytes: N*72 mesh + M*(24 in + 36 out)),
-    # from the timed region's stage events
+    # stage times of the timed region (CUDA events of the library on the launching stream)
     agg = {"screen": float(stage[:, 0].sum()) / args.steps, "refine": float(stage[:, 1].sum()) / args.steps,
            "fallback": float(stage[:, 2].sum()) / args.steps}
     launches = 0
     for name, st in breakdown:
         launches += int(st.launches)
-    dom = max(agg, key=agg.get)
-    per_launch_ms = float(stage[:, ("screen", "refine", "fallback").index(dom)].mean())
-    alg_bytes = tris.shape[0] * 72 + M * (24 + 36)
-    traffic = None
-    if dom == "screen" and not (args.block or args.cutters or args.stride):
-        try:  # DRAM bytes per screen launch from the committed ncu capture
-            for ln in open(os.path.join(ROOT, "profiles", "k_drop_screen_dram_full_size.md")):
-                if ln.startswith("traffic_bytes_per_launch:"):
-                    traffic = int(ln.split(":")[1])
-        except OSError:
-            traffic = None
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
-    kname = {"screen": "k_drop_screen", "refine": "k_drop_refine", "fallback": "k_drop_kd"}[dom]
 
     aux = None
     if not args.no_aux and not (args.block or args.cutters or args.stride):
@@ -481,6 +562,8 @@ def main():
                    "source": "ocl_gb300_fma_peaks: 8 FMA chains per thread on a full-occupancy grid, this GPU"}
     except Exception as e:  # reported, never required
         compute = {"error": str(e)}
+    roof = roofline_block(tris, M, cuts, breakdown, stage, args, compute)
+
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -515,17 +598,11 @@ def main():
         "e2e": {"value": e2e, "unit": "CL-points/s", "h2d_bytes_per_step": len(cuts) * M * 24,
                 "d2h_bytes_per_step": len(cuts) * M * (8 + 24 + 4)},
         "gpu_launches": launches * args.steps,
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
-                     "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": alg_bytes,
-                     "note": "algorithmic bytes N*72 + M*60 per launch over the mean launch time of the dominant "
-                             "stage in the timed region; the kernel is FP32-issue and latency bound, not HBM-bound "
-                             "(traffic: ncu DRAM bytes per launch of the full-size workload)"},
+        "roofline": roof,
         "kernel_ms_per_step": agg,
         "compute_peaks": compute,
-        "precision": prec,
-        "fp64_block": fp64_rate,
+        "precision_vs_oracle": prec_oracle,
+        "mixed_vs_fp64": fp64_full,
         "cpu_baseline": cpu,
         "other_operations": aux,
     }
