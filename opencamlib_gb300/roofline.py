@@ -33,10 +33,10 @@ dram__bytes_write.sum) of the screen kernels of one call on the full
 """
 from __future__ import annotations
 
-# cutter -> FP32 operations per screened pair (None: not measured yet)
-FP32_PER_SCREEN = {"cyl": None, "ball": None, "bull": None, "cone": None, "ballcone": None}
+# cutter -> FP32 operations per screened pair
+FP32_PER_SCREEN = {"cyl": 912.6, "ball": 1111.4, "bull": 1491.2, "cone": 1202.4, "ballcone": 1995.2}
 # cutter -> FP64 operations per refined triangle
-FP64_PER_REFINED = {"cyl": None, "ball": None, "bull": None, "cone": None, "ballcone": None}
+FP64_PER_REFINED = {"cyl": 122.1, "ball": 237.4, "bull": 1274.8, "cone": 295.3, "ballcone": 320.6}
 # cutter -> DRAM bytes of the screen kernels per call on the 1,000,000-point raster
 SCREEN_DRAM_BYTES = {"cyl": None, "ball": None, "bull": None, "cone": None, "ballcone": None}
 
