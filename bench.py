@@ -58,6 +58,9 @@ def parse():
                     help="CL points per cutter compared with the CPU oracle (precision_vs_oracle)")
     ap.add_argument("--no-fp64-full", action="store_true",
                     help="skip the plain FP64 run over the whole raster (mixed == FP64 check and speed-up)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batching measurement")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the 64-job batching measurement and print it (for profiling)")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one device step with statistics, print its counters and exit (for ncu)")
     return ap.parse_args()
@@ -295,6 +298,84 @@ def block_indices(side, i0=400, j0=300):
     return (jj * 1000 + ii).ravel()
 
 
+def batch_measurements(steps=2, warmup=1, njobs=64, autotune=True):
+    """The batching workload: 64 seeded jobs (heightfield / sphere /
+    box-with-fillet meshes of 1k-2M triangles, 1k-4M raster points, the five
+    cutter families with diameters 1-20 mm; workloads.batch_jobs(seed=3)),
+    timed as one ocl_gb300_drop_device call per job (a stream of launches per
+    job) and as one batch (persistent work-stealing launches, CUDA graph
+    replay); device outputs compared bit for bit."""
+    import torch
+    from opencamlib_gb300 import _native, workloads as w
+    specs = w.batch_jobs(seed=3, njobs=njobs)
+    t0 = time.time()
+    jobs = []
+    for sp in specs:
+        tris = w.mesh_of_size(sp["mesh"], sp["N"], sp["seed"])
+        c = w.batch_cutter(sp["cutter"], sp["d"])
+        pts = w.batch_points(tris, sp["M"], c.radius)
+        mesh = _native.DeviceMesh(tris)
+        M = len(pts)
+        d_cl = torch.from_numpy(pts).cuda()
+        bufs = [torch.empty(M, dtype=torch.float64, device="cuda"), torch.empty((M, 3), dtype=torch.float64, device="cuda"),
+                torch.empty(M, dtype=torch.int32, device="cuda")]
+        ref = [torch.empty_like(b) for b in bufs]
+        jobs.append({"spec": sp, "tris": int(len(tris)), "mesh": mesh, "cutter": c, "M": M, "cl": d_cl, "out": bufs,
+                     "ref": ref})
+    torch.cuda.synchronize()
+    setup_s = time.time() - t0
+    total = sum(j["M"] for j in jobs)
+    stream = torch.cuda.Stream()
+
+    def per_job(target):
+        for j in jobs:
+            j["mesh"].drop_device(j["cutter"], j["cl"].data_ptr(), j["M"], j[target][0].data_ptr(),
+                                  j[target][1].data_ptr(), j[target][2].data_ptr(), stream=stream.cuda_stream,
+                                  stats=False)
+
+    def timed(fn):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                ev[0].record(stream)
+                fn()
+                ev[1].record(stream)
+            torch.cuda.synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        return ts
+
+    t_single = timed(lambda: per_job("ref"))
+    t1 = time.time()
+    batch = _native.DropBatch([(j["mesh"], j["cutter"], j["cl"].data_ptr(), j["M"], j["out"][0].data_ptr(),
+                                j["out"][1].data_ptr(), j["out"][2].data_ptr()) for j in jobs], autotune=autotune)
+    create_s = time.time() - t1
+    t_batch = timed(lambda: batch.run(stream.cuda_stream))
+    st = batch.run(stream.cuda_stream, stats=True)
+    torch.cuda.synchronize()
+    same = all(torch.equal(j["out"][k], j["ref"][k]) for j in jobs for k in range(3))
+    info = batch.info()
+    out = {"jobs": len(jobs), "points": int(total), "triangles": int(sum(j["tris"] for j in jobs)),
+           "setup_s": setup_s, "batch_create_s": create_s,
+           "one_call_per_job_ms": float(np.median(t_single)), "batch_ms": float(np.median(t_batch)),
+           "one_call_per_job_points_per_s": total / (np.median(t_single) / 1e3),
+           "batch_points_per_s": total / (np.median(t_batch) / 1e3),
+           "speedup": float(np.median(t_single) / np.median(t_batch)), "bit_identical": bool(same),
+           "violations": int(st.violations), "handed_back_points": int(st.fallback), "plain_points": int(st.plain_points),
+           "launches_per_run": info["launches_per_run"], "waves": info["waves"], "chunks": info["chunks"],
+           "workspace_bytes": info["workspace_bytes"], "tuned": info["variants"],
+           "launches_one_call_per_job": "about 15 per job (Morton sort, 9 stage kernels) x 64 jobs",
+           "workload": "workloads.batch_jobs(seed=3): 64 jobs, N ~ logU[1e3, 2e6] triangles (heightfield / sphere / "
+                       "box-with-fillet), M ~ logU[1e3, 4e6] raster points, cutter uniform over 5 families, d ~ U[1, 20] mm"}
+    batch.release()
+    for j in jobs:
+        j["mesh"].release()
+    return out
+
+
 def mixed_vs_fp64(mesh, cl, cuts):
     """Per cutter, the mixed path and the plain FP64 kernel (the reference's
     KD-tree algorithm on the device) over the same points: results compared
@@ -447,6 +528,10 @@ def main():
             if stats_out is not None:
                 stats_out.append((name, st))
 
+    if args.batch_only:
+        print(json.dumps({"batch": batch_measurements()}), flush=True)
+        return
+
     if args.profile_step:
         # one step with statistics: the launches an ncu capture of this
         # command sees, with the library's own counters for them
@@ -563,6 +648,11 @@ def main():
     except Exception as e:  # reported, never required
         compute = {"error": str(e)}
     roof = roofline_block(tris, M, cuts, breakdown, stage, args, compute)
+    if aux is not None and not args.no_batch and "error" not in aux:
+        try:
+            aux["batch"] = batch_measurements()
+        except Exception as e:  # reported, never required
+            aux["batch"] = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline:

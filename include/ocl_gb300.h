@@ -178,6 +178,62 @@ int ocl_gb300_drop_device_noalloc(ocl_gb300_mesh mesh, const ocl_gb300_cutter* c
                                   double* d_z_out, double* d_cc_out, int32_t* d_type_out,
                                   void* stream);
 
+/* ---- batches of drop-cutter jobs ----------------------------------------- */
+/* Many BatchDropCutter runs (each its own mesh, cutter and device point set,
+ * of any size) executed together.  No counterpart in the reference, whose
+ * parallelism is one OpenMP loop over the CL points of one run
+ * (src/dropcutter/batchdropcutter.cpp:207); each job's results equal
+ * ocl_gb300_drop_device's for that job bit for bit.  Jobs are cut into chunks,
+ * chunks packed into waves under a workspace budget; each stage of a wave is
+ * one persistent launch per kernel variant whose blocks take 128-point tiles
+ * of any job through an atomic counter (work stealing); the run is captured
+ * once into a CUDA graph and replayed by every later run.
+ * The batch keeps the job array's pointers: meshes and device buffers must
+ * stay valid (and meshes unchanged) until the batch is released. */
+typedef struct ocl_gb300_drop_job {
+    ocl_gb300_mesh mesh;
+    ocl_gb300_cutter cutter;
+    const double* d_cl_xyz;   /* device, M x 3 */
+    uint64_t M;
+    double* d_z_out;          /* device, M */
+    double* d_cc_out;         /* device, M x 3 */
+    int32_t* d_type_out;      /* device, M */
+} ocl_gb300_drop_job;
+
+typedef struct ocl_gb300_batch_opts {
+    uint64_t workspace_bytes; /* budget of the batch's device workspace (0: 8 GiB) */
+    uint64_t chunk_points;    /* jobs are cut into chunks of at most this many points (0: 1 Mi) */
+    int32_t autotune;         /* 1: pick candidate-list capacity and screen grid size per kernel
+                                 variant by timing a probe of the jobs (writes into the jobs'
+                                 outputs while it runs) */
+    int32_t graph;            /* 1: capture the run into a CUDA graph on the first run, replay after */
+    int32_t list_capacity;    /* candidates kept per CL point when not autotuned (16..256; 0: 256) */
+    int32_t reserved;
+} ocl_gb300_batch_opts;
+
+#define OCL_GB300_BATCH_MAX_VARIANTS 16
+typedef struct ocl_gb300_batch_info {
+    uint64_t jobs, chunks, waves, points;
+    uint64_t launches_per_run;  /* kernel launches of one run (all waves) */
+    uint64_t workspace_bytes;
+    int32_t variants;           /* screen kernel variants in the batch */
+    int32_t variant_kind[OCL_GB300_BATCH_MAX_VARIANTS];  /* OCL_CUTTER_* */
+    int32_t variant_sig[OCL_GB300_BATCH_MAX_VARIANTS];   /* composite make-up, -1 generic */
+    int32_t list_capacity[OCL_GB300_BATCH_MAX_VARIANTS]; /* chosen per variant */
+    int32_t grid_mult[OCL_GB300_BATCH_MAX_VARIANTS];
+} ocl_gb300_batch_info;
+
+typedef struct ocl_gb300_batch_s* ocl_gb300_batch;
+/* opts may be NULL (defaults: 8 GiB, 1 Mi-point chunks, no autotuning, graph on). */
+int ocl_gb300_batch_create(const ocl_gb300_drop_job* jobs, uint64_t njobs, const ocl_gb300_batch_opts* opts,
+                           ocl_gb300_batch* out);
+/* Runs every job on `stream` (cudaStream_t as void*); no host sync unless
+ * stats != NULL (then stats holds the counters summed over all jobs and the
+ * run's device time). */
+int ocl_gb300_batch_run(ocl_gb300_batch batch, void* stream, ocl_gb300_stats* stats);
+int ocl_gb300_batch_info_get(ocl_gb300_batch batch, ocl_gb300_batch_info* out);
+int ocl_gb300_batch_release(ocl_gb300_batch batch);
+
 /* ---- push-cutter ------------------------------------------------------- */
 #define OCL_GB300_XFIBER 0
 #define OCL_GB300_YFIBER 1

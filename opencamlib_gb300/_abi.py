@@ -68,3 +68,32 @@ class Cert(C.Structure):
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class DropJob(C.Structure):
+    """ocl_gb300_drop_job: one BatchDropCutter run of a batch (device buffers)."""
+    _fields_ = [("mesh", C.c_void_p), ("cutter", CutterDesc), ("d_cl_xyz", C.c_void_p), ("M", C.c_uint64),
+                ("d_z_out", C.c_void_p), ("d_cc_out", C.c_void_p), ("d_type_out", C.c_void_p)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("workspace_bytes", C.c_uint64), ("chunk_points", C.c_uint64), ("autotune", C.c_int32),
+                ("graph", C.c_int32), ("list_capacity", C.c_int32), ("reserved", C.c_int32)]
+
+
+BATCH_MAX_VARIANTS = 16
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("jobs", C.c_uint64), ("chunks", C.c_uint64), ("waves", C.c_uint64), ("points", C.c_uint64),
+                ("launches_per_run", C.c_uint64), ("workspace_bytes", C.c_uint64), ("variants", C.c_int32),
+                ("variant_kind", C.c_int32 * BATCH_MAX_VARIANTS), ("variant_sig", C.c_int32 * BATCH_MAX_VARIANTS),
+                ("list_capacity", C.c_int32 * BATCH_MAX_VARIANTS), ("grid_mult", C.c_int32 * BATCH_MAX_VARIANTS)]
+
+    def as_dict(self):
+        n = self.variants
+        return {"jobs": self.jobs, "chunks": self.chunks, "waves": self.waves, "points": self.points,
+                "launches_per_run": self.launches_per_run, "workspace_bytes": self.workspace_bytes,
+                "variants": [{"kind": self.variant_kind[k], "sig": self.variant_sig[k],
+                              "list_capacity": self.list_capacity[k], "grid_mult": self.grid_mult[k]}
+                             for k in range(n)]}

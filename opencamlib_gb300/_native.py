@@ -27,7 +27,8 @@ EXPORTS = [
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available", "ocl_gb300_mesh_kd_order", "ocl_gb300_mesh_kd_rank", "ocl_gb300_overlap_sets",
-    "ocl_gb300_certificate_check",
+    "ocl_gb300_certificate_check", "ocl_gb300_batch_create", "ocl_gb300_batch_run", "ocl_gb300_batch_info_get",
+    "ocl_gb300_batch_release",
 ]
 
 _lib = None
@@ -72,6 +73,11 @@ def lib():
     L.ocl_gb300_mesh_kd_rank.argtypes = [C.c_void_p, _i64p]
     L.ocl_gb300_overlap_sets.argtypes = [C.c_void_p, C.c_double, _dp, C.c_uint64, _u64p, _ip, C.c_uint64]
     L.ocl_gb300_certificate_check.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.POINTER(_abi.Cert)]
+    L.ocl_gb300_batch_create.argtypes = [C.POINTER(_abi.DropJob), C.c_uint64, C.POINTER(_abi.BatchOpts),
+                                         C.POINTER(C.c_void_p)]
+    L.ocl_gb300_batch_run.argtypes = [C.c_void_p, C.c_void_p, st]
+    L.ocl_gb300_batch_info_get.argtypes = [C.c_void_p, C.POINTER(_abi.BatchInfo)]
+    L.ocl_gb300_batch_release.argtypes = [C.c_void_p]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -322,3 +328,48 @@ class DeviceMesh:
         desc = cutter.desc()
         check(lib().ocl_gb300_certificate_check(self._h, C.byref(desc), _p(cl), cl.shape[0], C.byref(out)))
         return out.as_dict()
+
+
+class DropBatch:
+    """Many BatchDropCutter runs executed together (ocl_gb300_batch_*).
+
+    jobs: sequence of (DeviceMesh, cutter, d_cl, M, d_z, d_cc, d_type) with
+    device pointers as ints.  The meshes and buffers must outlive the batch.
+    """
+
+    def __init__(self, jobs, workspace_bytes=0, chunk_points=0, autotune=False, graph=True, list_capacity=0):
+        self._jobs = list(jobs)
+        arr = (_abi.DropJob * max(len(self._jobs), 1))()
+        for k, (mesh, cutter, d_cl, M, d_z, d_cc, d_ty) in enumerate(self._jobs):
+            arr[k].mesh = mesh.handle
+            arr[k].cutter = cutter.desc()
+            arr[k].d_cl_xyz = d_cl
+            arr[k].M = M
+            arr[k].d_z_out = d_z
+            arr[k].d_cc_out = d_cc
+            arr[k].d_type_out = d_ty
+        opts = _abi.BatchOpts(workspace_bytes, chunk_points, 1 if autotune else 0, 1 if graph else 0, list_capacity, 0)
+        h = C.c_void_p()
+        check(lib().ocl_gb300_batch_create(arr, len(self._jobs), C.byref(opts), C.byref(h)))
+        self._h = h
+
+    def run(self, stream=0, stats=False):
+        st = _abi.Stats() if stats else None
+        check(lib().ocl_gb300_batch_run(self._h, C.c_void_p(stream), C.byref(st) if st is not None else None))
+        return st
+
+    def info(self) -> dict:
+        out = _abi.BatchInfo()
+        check(lib().ocl_gb300_batch_info_get(self._h, C.byref(out)))
+        return out.as_dict()
+
+    def release(self):
+        if getattr(self, "_h", None):
+            lib().ocl_gb300_batch_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass

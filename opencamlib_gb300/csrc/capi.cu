@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "drop.cuh"
 #include "geom64.cuh"
@@ -474,6 +475,52 @@ int ocl_gb300_certificate_check(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cut
     if (st) return st;
     std::lock_guard<std::mutex> lk(mesh->m->mu);
     return certificate_check(*mesh->m, cp, cl_xyz, M, out);
+}
+
+struct ocl_gb300_batch_s {
+    Batch* b;
+};
+
+int ocl_gb300_batch_create(const ocl_gb300_drop_job* jobs, uint64_t njobs, const ocl_gb300_batch_opts* opts,
+                           ocl_gb300_batch* out) {
+    if (!out || (njobs > 0 && !jobs)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    *out = nullptr;
+    int st = need_device();
+    if (st) return st;
+    std::vector<Mesh*> meshes(njobs);
+    for (uint64_t k = 0; k < njobs; ++k) meshes[k] = jobs[k].mesh ? jobs[k].mesh->m : nullptr;
+    Batch* b = nullptr;
+    st = batch_create(jobs, meshes.data(), njobs, opts, &b);
+    if (st) return st;
+    *out = new ocl_gb300_batch_s{b};
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_batch_run(ocl_gb300_batch batch, void* stream, ocl_gb300_stats* stats) {
+    if (!batch) {
+        set_error("null batch");
+        return OCL_GB300_BAD_ARG;
+    }
+    return batch_run(*batch->b, (cudaStream_t)stream, stats);
+}
+
+int ocl_gb300_batch_info_get(ocl_gb300_batch batch, ocl_gb300_batch_info* out) {
+    if (!batch || !out) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    batch_info(*batch->b, out);
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_batch_release(ocl_gb300_batch batch) {
+    if (!batch) return OCL_GB300_BAD_ARG;
+    batch_destroy(batch->b);
+    delete batch;
+    return OCL_GB300_OK;
 }
 
 }  // extern "C"

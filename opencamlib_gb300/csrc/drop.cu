@@ -201,6 +201,26 @@ __global__ void __launch_bounds__(128) k_drop_kd(const __grid_constant__ DropCtx
         drop_kd_warp<FAST>(ctx, s_hlb, list, nlist, warp, s_stack[wl], lane);
 }
 
+// Batch: every warp of the persistent grid strides over the points each job
+// handed to the plain kernel (counts on the device), job after job.
+__global__ void __launch_bounds__(128) k_drop_kd_b(const __grid_constant__ BatchView bv) {
+    __shared__ uint2 s_stack[4][KD_STACK];
+    __shared__ float s_hlb[HLB_N];
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned k = 0; k < bv.njobs; ++k) {
+        const DropCtx& ctx = bv.ctxs[bv.jobs[k]];
+        const int n = (int)ctx.counters[C_PLAIN];
+        if (n == 0) continue;
+        __syncthreads();
+        for (int q = threadIdx.x; q < HLB_N; q += blockDim.x) s_hlb[q] = ctx.hlb[q];
+        __syncthreads();
+        for (int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp * 32 < n; warp += nwarps)
+            drop_kd_warp<true>(ctx, s_hlb, ctx.list2, n, warp, s_stack[wl], lane);
+    }
+}
+
 // One step of dropCutter5's fold (batchdropcutter.cpp:187-231): the overlap
 // and below tests, then MillingCutter::dropCutter on the triangle.
 // zfloor (local frame): for the cutters whose fold is a plain maximum
@@ -312,9 +332,10 @@ __device__ __forceinline__ float bull_edge_hi(const DropCtx& ctx, const Tri32& t
     return bull_edge_solve32(c, b, ctx.E).hi;
 }
 
-__global__ void __launch_bounds__(128) k_bull_plan(const __grid_constant__ DropCtx ctx, uint2* __restrict__ queue,
-                                                  unsigned long long* __restrict__ qcount) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// One point's plan; every lane of the warp calls it (one queue reservation
+// per warp).
+__device__ __forceinline__ void bull_plan_point(const DropCtx& ctx, const uint32_t i, uint2* __restrict__ queue,
+                                                unsigned long long* __restrict__ qcount) {
     const int lane = threadIdx.x & 31;
     int cnt = 0;
     if (i < (uint32_t)ctx.M) {
@@ -353,12 +374,25 @@ __global__ void __launch_bounds__(128) k_bull_plan(const __grid_constant__ DropC
     for (int k = 0; k < mine; ++k) queue[base + incl - mine + k] = make_uint2(i, (uint32_t)k);
 }
 
-__global__ void __launch_bounds__(128) k_bull_eval(const __grid_constant__ DropCtx ctx, const uint2* __restrict__ queue,
-                                                  const unsigned long long* __restrict__ qcount) {
-    const unsigned long long nq = *qcount;
-    int capped = 0;
-    for (unsigned long long w = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; w < nq;
-         w += (unsigned long long)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(128) k_bull_plan(const __grid_constant__ DropCtx ctx, uint2* __restrict__ queue,
+                                                  unsigned long long* __restrict__ qcount) {
+    bull_plan_point(ctx, blockIdx.x * blockDim.x + threadIdx.x, queue, qcount);
+}
+
+__global__ void __launch_bounds__(128) k_bull_plan_b(const __grid_constant__ BatchView bv) {
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    while (batch_next_tile(bv, ts, s_ctx, tile))
+        bull_plan_point(s_ctx, tile.y * TILE_POINTS + threadIdx.x, s_ctx.edge_queue, s_ctx.counters + C_EDGEQ);
+}
+
+// Queue entries [w0, nq) with stride `step` of one call's edge queue.
+__device__ __forceinline__ void bull_eval_range(const DropCtx& ctx, const uint2* __restrict__ queue,
+                                                unsigned long long nq, unsigned long long w0, unsigned long long step,
+                                                int& capped) {
+    for (unsigned long long w = w0; w < nq; w += step) {
         const uint2 it = queue[w];
         const uint32_t s = ctx.edge_slots[(size_t)it.x * EDGE_SLOTS + it.y];
         const Tri64& t = ctx.t64[s >> 2];
@@ -376,7 +410,25 @@ __global__ void __launch_bounds__(128) k_bull_eval(const __grid_constant__ DropC
         r.pad = 0;
         ctx.edge_res[(size_t)it.x * EDGE_SLOTS + it.y] = r;
     }
+}
+
+__global__ void __launch_bounds__(128) k_bull_eval(const __grid_constant__ DropCtx ctx, const uint2* __restrict__ queue,
+                                                  const unsigned long long* __restrict__ qcount) {
+    int capped = 0;
+    bull_eval_range(ctx, queue, *qcount, blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x,
+                    (unsigned long long)gridDim.x * blockDim.x, capped);
     if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+}
+
+__global__ void __launch_bounds__(128) k_bull_eval_b(const __grid_constant__ BatchView bv) {
+    for (unsigned k = 0; k < bv.njobs; ++k) {
+        const DropCtx& ctx = bv.ctxs[bv.jobs[k]];
+        int capped = 0;
+        bull_eval_range(ctx, ctx.edge_queue, ctx.counters[C_EDGEQ],
+                        blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x,
+                        (unsigned long long)gridDim.x * blockDim.x, capped);
+        if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+    }
 }
 
 // MillingCutter::dropCutter for a bull, edges from k_bull_eval where planned
@@ -456,9 +508,7 @@ __device__ __forceinline__ void fold_bull(const DropCtx& ctx, CL64& cl, uint32_t
 // BULL_PLAN: the bull with its edges evaluated ahead (fold_bull only); else
 // every other case (fold_one only), so each kernel carries one fold.
 template <bool BULL_PLAN>
-__global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ DropCtx ctx) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (uint32_t)ctx.M) return;
+__device__ __forceinline__ void refine_point(const DropCtx& ctx, const uint32_t i) {
     const int n = ctx.ncand[i];
     if (n == 0xFFFF) return;  // handed to the plain path
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
@@ -503,6 +553,25 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
 }
 
+template <bool BULL_PLAN>
+__global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ DropCtx ctx) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint32_t)ctx.M) return;
+    refine_point<BULL_PLAN>(ctx, i);
+}
+
+template <bool BULL_PLAN>
+__global__ void __launch_bounds__(128) k_drop_refine_b(const __grid_constant__ BatchView bv) {
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    while (batch_next_tile(bv, ts, s_ctx, tile)) {
+        const uint32_t i = tile.y * TILE_POINTS + threadIdx.x;
+        if (i < (uint32_t)s_ctx.M) refine_point<BULL_PLAN>(s_ctx, i);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Exact fold of one handed-back CL point per block.
 // The block gathers every triangle whose certified FP32 upper bound lies above
@@ -515,26 +584,35 @@ constexpr int EXACT_CAP = 4096;
 constexpr int EXACT_THREADS = 256;
 constexpr size_t EXACT_SMEM = (size_t)EXACT_CAP * (8 + 4 + 4 + 4);
 
+// Shared memory of the exact kernel: EXACT_CAP keys (KD rank << 32 | slot),
+// triangles, upper bounds and lowest branch thresholds (+inf: none) in the
+// dynamic part; the profile table and two reduction words beside it.
+struct ExactShared {
+    unsigned long long* key;
+    uint32_t* tri;
+    float* hi;
+    float* qt;
+    float* hlb;
+    int* n;
+    int* red;
+};
+
+// One handed-back point, by the whole block.
 template <bool COMP>
-__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_constant__ DropCtx ctx,
-                                                              const uint32_t* __restrict__ list,
-                                                              const unsigned long long* __restrict__ nlist_dev,
-                                                              uint32_t* __restrict__ list2,
-                                                              unsigned long long* __restrict__ nlist2) {
-    extern __shared__ unsigned long long s_key[];  // EXACT_CAP keys (KD rank << 32 | slot)
-    uint32_t* s_tri = reinterpret_cast<uint32_t*>(s_key + EXACT_CAP);
-    float* s_hi = reinterpret_cast<float*>(s_tri + EXACT_CAP);
-    float* s_qt = s_hi + EXACT_CAP;  // lowest branch threshold (+inf: none)
-    __shared__ float s_hlb[HLB_N];
-    __shared__ int s_n, s_red;
-    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
+__device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
+                                            uint32_t* __restrict__ list2, unsigned long long* __restrict__ nlist2) {
+    unsigned long long* s_key = S.key;
+    uint32_t* s_tri = S.tri;
+    float* s_hi = S.hi;
+    float* s_qt = S.qt;
+    const float* s_hlb = S.hlb;
+    int& s_n = *S.n;
+    int& s_red = *S.red;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int nlist = (int)*nlist_dev;
     const GridP& g = ctx.g;
     const float R = ctx.prof.R, gd = ctx.guard, Rg = R + gd, inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    for (int p = blockIdx.x; p < nlist; p += gridDim.x) {
-        const uint32_t i = list[p];
+    {
         const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
         const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
         const float z0l = __double2float_rd(z0 - g.oz);
@@ -582,7 +660,7 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
         if (n > EXACT_CAP) {
             if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
             __syncthreads();
-            continue;
+            return;
         }
         // Only triangles whose upper bound reaches T are folded, T at most
         // blo - guard (the final height lies above it) and at most every
@@ -700,6 +778,47 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
     }
 }
 
+#define OCLG_EXACT_SHARED                                                                    \
+    extern __shared__ unsigned long long s_key[];                                            \
+    __shared__ float s_hlb[HLB_N];                                                           \
+    __shared__ int s_n, s_red;                                                               \
+    ExactShared S;                                                                           \
+    S.key = s_key;                                                                           \
+    S.tri = reinterpret_cast<uint32_t*>(s_key + EXACT_CAP);                                  \
+    S.hi = reinterpret_cast<float*>(S.tri + EXACT_CAP);                                      \
+    S.qt = S.hi + EXACT_CAP;                                                                 \
+    S.hlb = s_hlb;                                                                           \
+    S.n = &s_n;                                                                              \
+    S.red = &s_red;
+
+template <bool COMP>
+__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_constant__ DropCtx ctx,
+                                                              const uint32_t* __restrict__ list,
+                                                              const unsigned long long* __restrict__ nlist_dev,
+                                                              uint32_t* __restrict__ list2,
+                                                              unsigned long long* __restrict__ nlist2) {
+    OCLG_EXACT_SHARED
+    for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
+    const int nlist = (int)*nlist_dev;
+    for (int p = blockIdx.x; p < nlist; p += gridDim.x) exact_point<COMP>(ctx, list[p], S, list2, nlist2);
+}
+
+// Batch: every block strides over the handed-back points of each job in turn.
+template <bool COMP>
+__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact_b(const __grid_constant__ BatchView bv) {
+    OCLG_EXACT_SHARED
+    for (unsigned k = 0; k < bv.njobs; ++k) {
+        const DropCtx& ctx = bv.ctxs[bv.jobs[k]];
+        const int nlist = (int)ctx.counters[C_FALLBACK];
+        if (nlist == 0) continue;
+        __syncthreads();
+        for (int q = threadIdx.x; q < HLB_N; q += blockDim.x) s_hlb[q] = ctx.hlb[q];
+        for (int p = blockIdx.x; p < nlist; p += gridDim.x)
+            exact_point<COMP>(ctx, ctx.list[p], S, ctx.list2, ctx.counters + C_PLAIN);
+    }
+}
+#undef OCLG_EXACT_SHARED
+
 __global__ void k_collect_overflow(const uint16_t* ncand, int M, uint32_t* list, unsigned long long* counter) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M) return;
@@ -707,6 +826,62 @@ __global__ void k_collect_overflow(const uint16_t* ncand, int M, uint32_t* list,
         unsigned long long slot = atomicAdd(counter, 1ull);
         list[slot] = (uint32_t)i;
     }
+}
+
+__global__ void __launch_bounds__(128) k_collect_overflow_b(const __grid_constant__ BatchView bv) {
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    while (batch_next_tile(bv, ts, s_ctx, tile)) {
+        const uint32_t i = tile.y * TILE_POINTS + threadIdx.x;
+        if (i < (uint32_t)s_ctx.M && s_ctx.ncand[i] == 0xFFFF)
+            s_ctx.list[atomicAdd(&s_ctx.counters[C_FALLBACK], 1ull)] = i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batch ordering: Morton keys of every job's points in the job's own frame,
+// prefixed by the job index, so one radix sort orders the whole wave job by
+// job (each job's points stay a contiguous segment) and along the curve
+// within a job.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t batch_job_of(const BatchIn* __restrict__ in, uint32_t njobs, uint64_t g) {
+    uint32_t lo = 0, hi = njobs - 1;  // last job with off <= g
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (in[mid].off <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_batch_morton(const BatchIn* __restrict__ in, uint32_t njobs, uint64_t Mtot,
+                               unsigned long long* __restrict__ keys, uint32_t* __restrict__ idx) {
+    const uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (g >= Mtot) return;
+    const uint32_t j = batch_job_of(in, njobs, g);
+    const BatchIn b = in[j];
+    const uint64_t i = g - b.off;
+    const double fx = (b.cl[3 * i] - b.x0) * b.sx, fy = (b.cl[3 * i + 1] - b.y0) * b.sy;
+    const uint32_t qx = (uint32_t)fmin(fmax(fx, 0.0), 65535.0);
+    const uint32_t qy = (uint32_t)fmin(fmax(fy, 0.0), 65535.0);
+    keys[g] = ((unsigned long long)j << 32) | (spread16(qx) | (spread16(qy) << 1));
+    idx[g] = (uint32_t)g;
+}
+
+__global__ void k_batch_gather(const BatchIn* __restrict__ in, const unsigned long long* __restrict__ keys,
+                               const uint32_t* __restrict__ idx, uint64_t Mtot, double* __restrict__ cls,
+                               uint32_t* __restrict__ perm) {
+    const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= Mtot) return;
+    const uint32_t j = (uint32_t)(keys[p] >> 32);
+    const BatchIn& b = in[j];
+    const uint64_t i = idx[p] - b.off;
+    cls[3 * p] = b.cl[3 * i];
+    cls[3 * p + 1] = b.cl[3 * i + 1];
+    cls[3 * p + 2] = b.cl[3 * i + 2];
+    perm[p] = (uint32_t)i;  // the job-local caller index
 }
 
 // ---------------------------------------------------------------------------
@@ -800,30 +975,34 @@ static void launch_screen(const DropCtx& h, const CutterP& cp, unsigned blocks, 
     }
 }
 
-// k_drop_exact over the handed-back points (count on the device).
-static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
-                        uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
-    // the shared-memory opt-in is a property of the kernel in one context:
-    // set once per context (device), not once per process
+// The exact kernels' dynamic shared memory (above the 48 KB default) is a
+// property of each kernel in one context: opted in once per context
+// (device), not once per process.
+int ensure_exact_smem() {
     static std::mutex mu;
     static std::set<uint64_t> done;
     const uint64_t key = context_key();
     if (!key) return OCL_GB300_DEVICE_ERROR;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (!done.count(key)) {
-            cudaError_t e = cudaFuncSetAttribute(k_drop_exact<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)EXACT_SMEM);
-            if (e == cudaSuccess)
-                e = cudaFuncSetAttribute(k_drop_exact<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)EXACT_SMEM);
-            if (e != cudaSuccess) {
-                set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-                return OCL_GB300_DEVICE_ERROR;
-            }
-            done.insert(key);
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(key)) return OCL_GB300_OK;
+    const void* kernels[4] = {(const void*)k_drop_exact<false>, (const void*)k_drop_exact<true>,
+                              (const void*)k_drop_exact_b<false>, (const void*)k_drop_exact_b<true>};
+    for (const void* k : kernels) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EXACT_SMEM);
+        if (e != cudaSuccess) {
+            set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+            return OCL_GB300_DEVICE_ERROR;
         }
     }
+    done.insert(key);
+    return OCL_GB300_OK;
+}
+
+// k_drop_exact over the handed-back points (count on the device).
+static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
+                        uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
+    int st = ensure_exact_smem();
+    if (st) return st;
     if (blocks == 0) blocks = 1;
     if (composite)
         k_drop_exact<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2);
@@ -983,6 +1162,57 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     return OCL_GB300_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Batch launchers (ocl_gb300_drop_batch, batch.cu)
+// ---------------------------------------------------------------------------
+size_t batch_sort_bytes(uint64_t Mtot, int end_bit) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)Mtot, 0, end_bit);
+    return b;
+}
+
+void batch_launch_order(const BatchIn* d_in, uint32_t njobs, uint64_t Mtot, unsigned long long* keys, uint32_t* idx,
+                        unsigned long long* keys2, uint32_t* idx2, void* sort_tmp, size_t sort_bytes, int end_bit,
+                        double* cls, uint32_t* perm, cudaStream_t stream, int* status) {
+    const unsigned nb = (unsigned)((Mtot + 255) / 256);
+    k_batch_morton<<<nb, 256, 0, stream>>>(d_in, njobs, Mtot, keys, idx);
+    const cudaError_t e = cub::DeviceRadixSort::SortPairs(sort_tmp, sort_bytes, keys, keys2, idx, idx2, (int64_t)Mtot,
+                                                          0, end_bit, stream);
+    if (e != cudaSuccess) {
+        set_error(std::string("batch sort: ") + cudaGetErrorString(e));
+        *status = OCL_GB300_DEVICE_ERROR;
+        return;
+    }
+    k_batch_gather<<<nb, 256, 0, stream>>>(d_in, keys2, idx2, Mtot, cls, perm);
+}
+
+void batch_launch_bull(const BatchView& plan, const BatchView& eval, unsigned blocks, cudaStream_t stream) {
+    k_bull_plan_b<<<blocks, TILE_POINTS, 0, stream>>>(plan);
+    k_bull_eval_b<<<blocks, 128, 0, stream>>>(eval);
+}
+
+void batch_launch_refine(const BatchView& bv, bool bull_plan, unsigned blocks, cudaStream_t stream) {
+    if (bull_plan) k_drop_refine_b<true><<<blocks, TILE_POINTS, 0, stream>>>(bv);
+    else k_drop_refine_b<false><<<blocks, TILE_POINTS, 0, stream>>>(bv);
+}
+
+void batch_launch_collect(const BatchView& bv, unsigned blocks, cudaStream_t stream) {
+    k_collect_overflow_b<<<blocks, TILE_POINTS, 0, stream>>>(bv);
+}
+
+int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream) {
+    int st = ensure_exact_smem();
+    if (st) return st;
+    if (composite) k_drop_exact_b<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv);
+    else k_drop_exact_b<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv);
+    return OCL_GB300_OK;
+}
+
+void batch_launch_plain(const BatchView& bv, unsigned blocks, cudaStream_t stream) {
+    k_drop_kd_b<<<blocks, 128, 0, stream>>>(bv);
+}
 
 int drop_stage_times(uint64_t count, double* out) {
     if (!tl_work) return count == 0 ? OCL_GB300_OK : OCL_GB300_BAD_ARG;

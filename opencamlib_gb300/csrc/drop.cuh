@@ -65,12 +65,63 @@ struct DropCtx {
     uint8_t* edge_n;        // per CL: planned edges (may exceed EDGE_SLOTS)
     struct EdgeRes* edge_res;  // M x EDGE_SLOTS results
     unsigned long long* counters;
+    // hand-back lists and the bull edge queue of this call (read from here by
+    // the batch kernels; the single-call kernels take them as arguments)
+    uint32_t* list;
+    uint32_t* list2;
+    uint2* edge_queue;
     float E;                // FP32 position error budget
     float guard;            // margin for the bound tests
     bool composite_screen;  // composite cutter: screen_composite with comp
     Comp32 comp;
     float hlb[HLB_N];       // lower bound of height(r) on [k R / HLB_N, R]
 };
+
+// A launch over many jobs (ocl_gb300_drop_batch).  Each job has its own
+// context (mesh, cutter, its slice of the batch's arrays).  Work tiles are
+// (job, 128-point block of the job); persistent blocks take them in turn
+// through an atomic counter (work stealing), so jobs of very different sizes
+// share the GPU without a launch per job.  Stages whose work is counted on
+// the device (scattered warps, handed-back points, bull edge queues) stride
+// over the device-side lists of the jobs named in `jobs`.
+constexpr int TILE_POINTS = 128;  // points per work tile (4 screen warps = one refinement block)
+struct BatchView {
+    const DropCtx* ctxs;
+    const uint2* tiles;   // (job, block of the job)
+    unsigned ntiles;
+    unsigned* next;       // tile counter of this launch (zeroed before it)
+    const uint32_t* jobs; // jobs of this launch
+    unsigned njobs;
+};
+
+// Per job of a batch wave: the caller's points and the Morton frame of the
+// job's mesh (x0, y0 origin; sx, sy scale to 16-bit cells).
+struct BatchIn {
+    const double* cl;
+    uint64_t off;  // first point of the job in the wave
+    uint64_t M;
+    double x0, y0, sx, sy;
+};
+
+// Launchers of the batch kernels (drop.cu); `blocks` is the persistent grid.
+void batch_launch_order(const BatchIn* d_in, uint32_t njobs, uint64_t Mtot, unsigned long long* keys,
+                        uint32_t* idx, unsigned long long* keys2, uint32_t* idx2, void* sort_tmp, size_t sort_bytes,
+                        int end_bit, double* cls, uint32_t* perm, cudaStream_t stream, int* status);
+size_t batch_sort_bytes(uint64_t Mtot, int end_bit);
+void batch_launch_bull(const BatchView& plan, const BatchView& eval, unsigned blocks, cudaStream_t stream);
+void batch_launch_refine(const BatchView& bv, bool bull_plan, unsigned blocks, cudaStream_t stream);
+void batch_launch_collect(const BatchView& bv, unsigned blocks, cudaStream_t stream);
+int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream);
+void batch_launch_plain(const BatchView& bv, unsigned blocks, cudaStream_t stream);
+// Opt the exact kernels into their dynamic shared memory in the current context.
+int ensure_exact_smem();
+
+struct Batch;
+int batch_create(const ocl_gb300_drop_job* jobs, Mesh* const* meshes, uint64_t njobs, const ocl_gb300_batch_opts* opts,
+                 Batch** out);
+int batch_run(Batch& b, cudaStream_t stream, ocl_gb300_stats* stats);
+void batch_info(const Batch& b, ocl_gb300_batch_info* out);
+void batch_destroy(Batch* b);
 
 struct DropWork;
 // The per-call context fields that depend only on the mesh and the cutter:

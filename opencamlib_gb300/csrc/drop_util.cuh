@@ -54,6 +54,42 @@ __device__ __forceinline__ bool warp_rect(const GridP& g, int L, double xmin, do
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Batch tiles (BatchView): one persistent block takes (job, block) tiles in
+// turn; the job's context lives in shared memory while the block works on it.
+// ---------------------------------------------------------------------------
+struct TileState {
+    uint2 tile;    // the block's current tile
+    uint32_t job;  // job whose context is in shared memory (~0u: none yet)
+};
+static_assert(sizeof(DropCtx) % 8 == 0, "DropCtx is copied in 8-byte words");
+
+__device__ __forceinline__ void batch_copy_ctx(const DropCtx* __restrict__ src, DropCtx& dst) {
+    const unsigned long long* s = reinterpret_cast<const unsigned long long*>(src);
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(&dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(DropCtx) / 8); k += blockDim.x) d[k] = s[k];
+}
+
+// Next tile of a persistent block; every thread of the block calls it.
+// Returns 0 when the launch's tiles are used up, 1 for a tile of the job
+// already in `ctx`, 2 for a tile of another job (its context copied in).
+// `ts.job` must be set to ~0u by one thread before the first call.
+__device__ __forceinline__ int batch_next_tile(const BatchView& bv, TileState& ts, DropCtx& ctx, uint2& tile) {
+    __syncthreads();  // the block is done with the previous tile
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(bv.next, 1u);
+        ts.tile = t < bv.ntiles ? bv.tiles[t] : make_uint2(0xFFFFFFFFu, 0u);
+    }
+    __syncthreads();
+    tile = ts.tile;
+    if (tile.x == 0xFFFFFFFFu) return 0;
+    if (tile.x == ts.job) return 1;
+    batch_copy_ctx(bv.ctxs + tile.x, ctx);
+    __syncthreads();
+    if (threadIdx.x == 0) ts.job = tile.x;  // read again only after the next call's first barrier
+    return 2;
+}
+
 __device__ __forceinline__ float hlb_at(const float* hlb, float d, float inv_step) {
     int k = (int)(fmaxf(d, 0.0f) * inv_step);
     k = min(k, HLB_N - 1);

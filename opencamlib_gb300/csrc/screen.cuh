@@ -46,6 +46,18 @@ bool screen_launch_comp_a_sparse(const DropCtx& h, int sig, unsigned blocks, cud
 bool screen_launch_comp_b_sparse(const DropCtx& h, int sig, unsigned blocks, cudaStream_t stream, int stage);
 void screen_launch_comp_any_sparse(const DropCtx& h, unsigned blocks, cudaStream_t stream, int stage);
 
+// Batch launchers: *_dense_b in the dense units, *_b (stage 0 seeding,
+// stage 2 sparse screen) in the sparse units; `blocks` is the persistent
+// grid.  The composite ones return false when the make-up is not theirs.
+void screen_launch_basic_dense_b(const BatchView& bv, int kind, unsigned blocks, cudaStream_t stream);
+void screen_launch_basic_b(const BatchView& bv, int kind, unsigned blocks, cudaStream_t stream, int stage);
+bool screen_launch_comp_a_dense_b(const BatchView& bv, int sig, unsigned blocks, cudaStream_t stream);
+bool screen_launch_comp_a_b(const BatchView& bv, int sig, unsigned blocks, cudaStream_t stream, int stage);
+bool screen_launch_comp_b_dense_b(const BatchView& bv, int sig, unsigned blocks, cudaStream_t stream);
+bool screen_launch_comp_b_b(const BatchView& bv, int sig, unsigned blocks, cudaStream_t stream, int stage);
+void screen_launch_comp_any_dense_b(const BatchView& bv, unsigned blocks, cudaStream_t stream);
+void screen_launch_comp_any_b(const BatchView& bv, unsigned blocks, cudaStream_t stream, int stage);
+
 // Float <-> int keys whose integer order is the float order (for atomicMax /
 // atomicMin on floats held in shared memory).
 __device__ __forceinline__ int f2o(float f) {
@@ -507,8 +519,7 @@ __device__ __forceinline__ float seed_blo(const DropCtx& ctx, double x, double y
 // One warp per 32 sorted points: seeds the bounds of spread-out warps into
 // ctx.blo (the screen starts from them); other warps get the start height.
 template <int KIND, int CK>
-__global__ void __launch_bounds__(128) k_drop_seed(const __grid_constant__ DropCtx ctx) {
-    const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+__device__ __forceinline__ void seed_warp(const DropCtx& ctx, const int base) {
     if (base >= ctx.M) return;
     const int lane = threadIdx.x & 31;
     const bool active = base + lane < ctx.M;
@@ -520,6 +531,22 @@ __global__ void __launch_bounds__(128) k_drop_seed(const __grid_constant__ DropC
     float blo = z0l;
     if ((xmax - xmin) + (ymax - ymin) > ctx.cp.radius) blo = seed_blo<KIND, CK>(ctx, x, y, active, z0l);
     if (active) ctx.blo[i] = blo;
+}
+
+template <int KIND, int CK>
+__global__ void __launch_bounds__(128) k_drop_seed(const __grid_constant__ DropCtx ctx) {
+    seed_warp<KIND, CK>(ctx, ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32);
+}
+
+// The same over the tiles of a batch (persistent blocks, work stealing).
+template <int KIND, int CK>
+__global__ void __launch_bounds__(128) k_drop_seed_b(const __grid_constant__ BatchView bv) {
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    while (batch_next_tile(bv, ts, s_ctx, tile))
+        seed_warp<KIND, CK>(s_ctx, (int)(tile.y * TILE_POINTS) + (int)(threadIdx.x >> 5) * 32);
 }
 
 template <int KIND, int CK, bool SPARSE>
@@ -746,6 +773,47 @@ __global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK)
     const unsigned long long n = *ctx.sparse_n;
     for (unsigned long long w = blockIdx.x * SCREEN_WARPS + wl; w < n; w += (unsigned long long)gridDim.x * SCREEN_WARPS)
         screen_warp<KIND, CK, SPARSE>(ctx, sh, (int)(ctx.sparse_list[w] << 5));
+}
+
+// Batch versions.  Dense: persistent blocks over the launch's tiles (one
+// tile = the 4 warps of one block of a job), the job's context and profile
+// table in shared memory.  Sparse: every block strides over the scattered
+// warps of each job of the launch in turn (counts on the device).
+template <int KIND, int CK>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
+    k_drop_screen_b(const __grid_constant__ BatchView bv) {
+    __shared__ ScanShared sh;
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    int r;
+    while ((r = batch_next_tile(bv, ts, s_ctx, tile)) != 0) {
+        if (r == 2) {
+            for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) sh.hlb[k] = s_ctx.hlb[k];
+            __syncthreads();
+        }
+        const int base = (int)(tile.y * SCREEN_WARPS + (threadIdx.x >> 5)) * 32;
+        if (base < s_ctx.M) screen_warp<KIND, CK, false>(s_ctx, sh, base);
+    }
+}
+
+template <int KIND, int CK>
+__global__ void __launch_bounds__(SCREEN_WARPS * 32, screen_min_blocks(KIND, CK))
+    k_drop_screen_sparse_b(const __grid_constant__ BatchView bv) {
+    __shared__ ScanShared sh;
+    const int wl = threadIdx.x >> 5;
+    for (unsigned k = 0; k < bv.njobs; ++k) {
+        const DropCtx& ctx = bv.ctxs[bv.jobs[k]];
+        const unsigned long long n = *ctx.sparse_n;
+        if (n == 0) continue;
+        __syncthreads();
+        for (int q = threadIdx.x; q < HLB_N; q += blockDim.x) sh.hlb[q] = ctx.hlb[q];
+        __syncthreads();
+        for (unsigned long long w = blockIdx.x * SCREEN_WARPS + wl; w < n;
+             w += (unsigned long long)gridDim.x * SCREEN_WARPS)
+            screen_warp<KIND, CK, true>(ctx, sh, (int)(ctx.sparse_list[w] << 5));
+    }
 }
 
 

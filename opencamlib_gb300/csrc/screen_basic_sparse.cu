@@ -25,4 +25,27 @@ void screen_launch_basic_sparse(const DropCtx& h, int kind, unsigned blocks, cud
     }
 }
 
+
+void screen_launch_basic_b(const BatchView& bv, int kind, unsigned blocks, cudaStream_t stream, int stage) {
+    const dim3 tb(SCREEN_WARPS * 32);
+    switch (kind) {
+    case OCL_CUTTER_CONE:
+        if (stage == 0) k_drop_seed_b<1, OCL_CUTTER_CONE><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<1, OCL_CUTTER_CONE><<<blocks, tb, 0, stream>>>(bv);
+        break;
+    case OCL_CUTTER_CYL:
+        if (stage == 0) k_drop_seed_b<0, OCL_CUTTER_CYL><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<0, OCL_CUTTER_CYL><<<blocks, tb, 0, stream>>>(bv);
+        break;
+    case OCL_CUTTER_BALL:
+        if (stage == 0) k_drop_seed_b<0, OCL_CUTTER_BALL><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<0, OCL_CUTTER_BALL><<<blocks, tb, 0, stream>>>(bv);
+        break;
+    default:
+        if (stage == 0) k_drop_seed_b<0, OCL_CUTTER_BULL><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<0, OCL_CUTTER_BULL><<<blocks, tb, 0, stream>>>(bv);
+        break;
+    }
+}
+
 }  // namespace oclg

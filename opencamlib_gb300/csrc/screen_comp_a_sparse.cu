@@ -17,4 +17,19 @@ bool screen_launch_comp_a_sparse(const DropCtx& h, int sig, unsigned blocks, cud
     return true;
 }
 
+
+bool screen_launch_comp_a_b(const BatchView& bv, int sig, unsigned blocks, cudaStream_t stream, int stage) {
+    const dim3 tb(SCREEN_WARPS * 32);
+    if (sig == SIG_BALLCONE) {
+        if (stage == 0) k_drop_seed_b<2, SIG_BALLCONE><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<2, SIG_BALLCONE><<<blocks, tb, 0, stream>>>(bv);
+    } else if (sig == SIG_BULLCONE) {
+        if (stage == 0) k_drop_seed_b<2, SIG_BULLCONE><<<blocks, tb, 0, stream>>>(bv);
+        else k_drop_screen_sparse_b<2, SIG_BULLCONE><<<blocks, tb, 0, stream>>>(bv);
+    } else {
+        return false;
+    }
+    return true;
+}
+
 }  // namespace oclg

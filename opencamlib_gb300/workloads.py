@@ -12,6 +12,9 @@ Workloads (sizes as used by the tests and the benchmark):
                    plate -> exactly 1,048,576 triangles
   raster           CL points on a regular xy raster at a given start z
   sphere_torus     sphere-on-plate + torus (R=25, r=8) for the push-cutter
+  batch_jobs       64 drop-cutter jobs of uneven mesh and point counts
+                   (heightfield / sphere / box-with-fillet meshes, all five
+                   cutter families, diameters 1-20 mm)
 """
 from __future__ import annotations
 
@@ -181,27 +184,24 @@ def torus(cx, cy, cz, R, r, nu, nv) -> np.ndarray:
 
 
 def sphere(cx, cy, cz, r, naz, nrings) -> np.ndarray:
-    """Full UV sphere: two pole fans and nrings-2 bands."""
-    tris = []
+    """Full UV sphere: a north pole fan, nrings-2 bands of two triangles per
+    quad, a south pole fan (vertex (k, m) at polar angle k pi / nrings and
+    azimuth 2 pi m / naz)."""
     th = np.arange(nrings + 1) * math.pi / nrings
     ph = 2.0 * math.pi * np.arange(naz) / naz
     ct, st = np.cos(th), np.sin(th)
     cp, sp = np.cos(ph), np.sin(ph)
-
-    def v(k, m):
-        m = m % naz
-        return (cx + r * st[k] * cp[m], cy + r * st[k] * sp[m], cz + r * ct[k])
-
-    for m in range(naz):
-        tris.append((cx, cy, cz + r) + v(1, m) + v(1, m + 1))
-    for k in range(1, nrings - 1):
-        for m in range(naz):
-            a, b, c, d = v(k, m), v(k, m + 1), v(k + 1, m + 1), v(k + 1, m)
-            tris.append(a + d + c)
-            tris.append(a + c + b)
-    for m in range(naz):
-        tris.append((cx, cy, cz - r) + v(nrings - 1, m + 1) + v(nrings - 1, m))
-    return np.array(tris, dtype=np.float64)
+    V = np.stack([cx + r * st[:, None] * cp[None, :], cy + r * st[:, None] * sp[None, :],
+                  np.broadcast_to(cz + r * ct[:, None], (nrings + 1, naz))], axis=-1)  # [k, m, xyz]
+    Vn = np.roll(V, -1, axis=1)  # vertex (k, m + 1)
+    north = np.broadcast_to(np.array([cx, cy, cz + r]), (naz, 3))
+    south = np.broadcast_to(np.array([cx, cy, cz - r]), (naz, 3))
+    fan_n = np.concatenate([north, V[1], Vn[1]], axis=1)
+    a, b = V[1:nrings - 1], Vn[1:nrings - 1]
+    c, d = Vn[2:nrings], V[2:nrings]
+    band = np.stack([np.concatenate([a, d, c], axis=-1), np.concatenate([a, c, b], axis=-1)], axis=2)
+    fan_s = np.concatenate([south, Vn[nrings - 1], V[nrings - 1]], axis=1)
+    return np.concatenate([fan_n, band.reshape(-1, 9), fan_s], axis=0)
 
 
 def sphere_torus(scale: int = 1) -> np.ndarray:
@@ -235,3 +235,76 @@ def fibers(direction: int, z: float, lo: float, hi: float, n: int, ext_lo: float
     f[:, 2] = z
     f[:, 5] = z
     return f
+
+
+def box_fillet(nx: int, ny: int, size: float = 100.0, h: float = 20.0, r: float = 5.0) -> np.ndarray:
+    """A box with rounded top edges standing on a plate, as an nx x ny
+    heightfield over [0,size]^2: flat top of height h over the middle of the
+    square (60% x 40% of it), quarter-circle fillets of radius r along its top
+    edges, then a vertical drop to the plate at z = 0 (one grid cell wide)."""
+    xs = np.linspace(0.0, size, nx)
+    ys = np.linspace(0.0, size, ny)
+    X, Y = np.meshgrid(xs, ys)
+    x0, x1 = 0.2 * size + r, 0.8 * size - r
+    y0, y1 = 0.3 * size + r, 0.7 * size - r
+    dx = np.maximum(np.maximum(x0 - X, X - x1), 0.0)
+    dy = np.maximum(np.maximum(y0 - Y, Y - y1), 0.0)
+    q = np.sqrt(dx * dx + dy * dy)
+    Z = np.where(q <= 0.0, h, np.where(q < r, h - r + np.sqrt(np.maximum(r * r - q * q, 0.0)), 0.0))
+    return grid_triangles(X, Y, Z)
+
+
+def mesh_of_size(kind: str, n: int, seed: int) -> np.ndarray:
+    """About n triangles from one of the batch generators: 'heightfield' (a
+    bump field), 'sphere' (a UV sphere r=40 on nothing), 'box' (box_fillet)."""
+    if kind == "sphere":
+        # 2 naz (nrings - 1) triangles with naz = 2 nrings
+        nr = max(3, int(round(math.sqrt(n / 4.0))))
+        return sphere(50.0, 50.0, 0.0, 40.0, 2 * nr, nr)
+    side = max(3, int(round(math.sqrt(n / 2.0))) + 1)
+    if kind == "box":
+        return box_fillet(side, side)
+    return heightfield(side, side, seed=seed)
+
+
+def batch_jobs(seed: int = 3, njobs: int = 64, n_range=(1e3, 2e6), m_range=(1e3, 4e6), d_range=(1.0, 20.0)):
+    """Seeded job specs of the batching workload: per job a mesh generator
+    (uniform over heightfield, sphere, box), a triangle count N ~
+    log-uniform(n_range), a CL point count M ~ log-uniform(m_range) on a
+    raster over the mesh's bbox, a cutter family uniform over the five
+    (cyl, ball, bull, cone, ball-cone) and a diameter d ~ U(d_range) (bull
+    corner d/6, cones 45 deg, ball-cone d/3 inside d).  Returns a list of
+    dicts; build_batch_job() makes the mesh and points."""
+    u = uniform(seed, 6 * njobs).reshape(njobs, 6)
+    kinds = ("heightfield", "sphere", "box")
+    cutters_ = ("cyl", "ball", "bull", "cone", "ballcone")
+    out = []
+    for k in range(njobs):
+        N = int(round(math.exp(math.log(n_range[0]) + u[k, 0] * (math.log(n_range[1]) - math.log(n_range[0])))))
+        M = int(round(math.exp(math.log(m_range[0]) + u[k, 1] * (math.log(m_range[1]) - math.log(m_range[0])))))
+        out.append({"job": k, "mesh": kinds[min(int(u[k, 2] * 3), 2)], "N": N, "M": M,
+                    "cutter": cutters_[min(int(u[k, 3] * 5), 4)],
+                    "d": d_range[0] + (d_range[1] - d_range[0]) * u[k, 4], "seed": seed * 1000 + k})
+    return out
+
+
+def batch_cutter(name: str, d: float):
+    from . import cutters as cu
+    L = max(20.0, 2.0 * d)
+    return {"cyl": lambda: cu.CylCutter(d, L), "ball": lambda: cu.BallCutter(d, L),
+            "bull": lambda: cu.BullCutter(d, d / 6.0, L), "cone": lambda: cu.ConeCutter(d, math.pi / 4, L),
+            "ballcone": lambda: cu.BallConeCutter(d / 3.0, d, math.pi / 4)}[name]()
+
+
+def batch_points(tris: np.ndarray, M: int, margin: float) -> np.ndarray:
+    """About M points on a raster over the mesh bbox widened by margin,
+    starting 10 mm below the mesh."""
+    p = tris.reshape(-1, 3)
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    w, h = hi[0] - lo[0] + 2 * margin, hi[1] - lo[1] + 2 * margin
+    nx = max(1, int(round(math.sqrt(M * w / h))))
+    ny = max(1, int(round(M / nx)))
+    xs = lo[0] - margin + (np.arange(nx) + 0.5) * (w / nx)
+    ys = lo[1] - margin + (np.arange(ny) + 0.5) * (h / ny)
+    X, Y = np.meshgrid(xs, ys)
+    return np.stack([X.ravel(), Y.ravel(), np.full(X.size, lo[2] - 10.0)], axis=1)
