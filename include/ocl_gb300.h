@@ -46,6 +46,8 @@ extern "C" {
 #define OCL_GB300_ITER_LIMIT         5  /* a capped device loop ran out (Brent, candidate lists) */
 #define OCL_GB300_NO_DEVICE          6
 #define OCL_GB300_CAPACITY           7  /* caller buffer too small; needed size reported */
+#define OCL_GB300_PENDING            8  /* server request not finished yet (wait timed out) */
+#define OCL_GB300_CANCELLED          9  /* server request cancelled before it finished */
 
 /* ---- CC types: numeric values of ocl::CCType (src/geo/ccpoint.hpp:33-39) */
 enum ocl_gb300_cctype {
@@ -233,6 +235,72 @@ int ocl_gb300_batch_create(const ocl_gb300_drop_job* jobs, uint64_t njobs, const
 int ocl_gb300_batch_run(ocl_gb300_batch batch, void* stream, ocl_gb300_stats* stats);
 int ocl_gb300_batch_info_get(ocl_gb300_batch batch, ocl_gb300_batch_info* out);
 int ocl_gb300_batch_release(ocl_gb300_batch batch);
+
+/* ---- serving: a request loop over device-resident meshes ---------------- */
+/* No counterpart in the reference (which runs one operation per run() call).
+ * Clients on any thread submit BatchDropCutter and AdaptivePathDropCutter
+ * requests with host buffers; a scheduler thread keeps up to `slots` batches
+ * on the GPU at once (batches as in ocl_gb300_batch_*), admits queued
+ * requests into the next batch while its CL points fit the slot's share of
+ * the device-memory budget, and sends an adaptive request's bisection levels
+ * through successive batches (each level rejoins the head of the queue).
+ * Results are those of ocl_gb300_drop / ocl_gb300_adaptive_path_drop for the
+ * same request, whatever else is in the mix.  Meshes added to a server must
+ * outlive it; request buffers must stay valid until ocl_gb300_server_wait
+ * returns for the request (call it exactly once per request). */
+typedef struct ocl_gb300_server_opts {
+    uint64_t hbm_budget_bytes;  /* device memory for in-flight batches (0: 16 GiB; at least 64 MiB) */
+    int32_t slots;              /* batches on the GPU at once (0: 2; at most 16) */
+    int32_t max_batch_requests; /* requests per batch (0: 64) */
+    int32_t list_capacity;      /* candidates kept per CL point (16..256; 0: 256) */
+    int32_t reserved;
+} ocl_gb300_server_opts;
+
+typedef struct ocl_gb300_request_info {
+    int32_t status;             /* OCL_GB300_OK, _CANCELLED, _CAPACITY (adaptive output too small), ... */
+    int32_t batches;            /* batches the request took part in */
+    uint64_t points;            /* CL points dropped for it */
+    double queue_ms;            /* submission to its first batch */
+    double latency_ms;          /* submission to the end of its last batch */
+    char message[160];          /* why it failed */
+} ocl_gb300_request_info;
+
+typedef struct ocl_gb300_server_stats {
+    uint64_t submitted, completed, failed, cancelled, rejected, batches, points, pending;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* latency of completed requests */
+    double elapsed_s;           /* first submission to the latest completion */
+} ocl_gb300_server_stats;
+
+typedef struct ocl_gb300_server_s* ocl_gb300_server;
+int ocl_gb300_server_create(const ocl_gb300_server_opts* opts, ocl_gb300_server* out);
+/* Makes `mesh` available to requests as *mesh_id. */
+int ocl_gb300_server_add_mesh(ocl_gb300_server server, ocl_gb300_mesh mesh, int32_t* mesh_id);
+/* BatchDropCutter request: host cl_xyz (M x 3) in; z_out (M), cc_out (M x 3),
+ * type_out (M) written when the request completes.  Rejected at once
+ * (BAD_ARG: unknown mesh or bad cutter; OOM: more points than one batch may
+ * hold under the budget). */
+int ocl_gb300_server_submit_drop(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
+                                 const double* cl_xyz, uint64_t M, double* z_out, double* cc_out,
+                                 int32_t* type_out, uint64_t* request_id);
+/* AdaptivePathDropCutter request over S spans (as ocl_gb300_adaptive_path_drop);
+ * *count receives the number of points; status CAPACITY if cap is too small. */
+int ocl_gb300_server_submit_adaptive(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
+                                     const double* spans, uint64_t S, double sampling, double min_sampling,
+                                     double cos_limit, double* xyz_out, double* cc_out, int32_t* type_out,
+                                     uint64_t cap, uint64_t* count, uint64_t* request_id);
+/* Waits (timeout_s < 0: without limit) for a request; OCL_GB300_PENDING on
+ * timeout (the request stays), else OCL_GB300_OK with info filled and the
+ * request forgotten. */
+int ocl_gb300_server_wait(ocl_gb300_server server, uint64_t request_id, double timeout_s,
+                          ocl_gb300_request_info* info);
+/* A queued request ends as CANCELLED; one on the GPU finishes its batch
+ * (an adaptive request ends as CANCELLED after it). */
+int ocl_gb300_server_cancel(ocl_gb300_server server, uint64_t request_id);
+int ocl_gb300_server_stats_get(ocl_gb300_server server, ocl_gb300_server_stats* out);
+/* paused != 0: no new batch starts (those on the GPU finish); 0: admission resumes. */
+int ocl_gb300_server_pause(ocl_gb300_server server, int32_t paused);
+/* Finishes the batches on the GPU; queued requests end as CANCELLED. */
+int ocl_gb300_server_destroy(ocl_gb300_server server);
 
 /* ---- push-cutter ------------------------------------------------------- */
 #define OCL_GB300_XFIBER 0

@@ -12,9 +12,12 @@ ITER_LIMIT = 5
 NO_DEVICE = 6
 CAPACITY = 7
 
+PENDING = 8
+CANCELLED = 9
+
 STATUS_NAMES = {OK: "OK", BAD_ARG: "BAD_ARG", UNSUPPORTED_CUTTER: "UNSUPPORTED_CUTTER", OOM: "OOM",
                 DEVICE_ERROR: "DEVICE_ERROR", ITER_LIMIT: "ITER_LIMIT", NO_DEVICE: "NO_DEVICE",
-                CAPACITY: "CAPACITY"}
+                CAPACITY: "CAPACITY", PENDING: "PENDING", CANCELLED: "CANCELLED"}
 
 CUTTER_CYL = 1
 CUTTER_BALL = 2
@@ -97,3 +100,23 @@ class BatchInfo(C.Structure):
                 "variants": [{"kind": self.variant_kind[k], "sig": self.variant_sig[k],
                               "list_capacity": self.list_capacity[k], "grid_mult": self.grid_mult[k]}
                              for k in range(n)]}
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("slots", C.c_int32), ("max_batch_requests", C.c_int32),
+                ("list_capacity", C.c_int32), ("reserved", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batches", C.c_int32), ("points", C.c_uint64), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("message", C.c_char * 160)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("rejected", C.c_uint64), ("batches", C.c_uint64), ("points", C.c_uint64),
+                ("pending", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double), ("elapsed_s", C.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

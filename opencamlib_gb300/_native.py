@@ -28,7 +28,9 @@ EXPORTS = [
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available", "ocl_gb300_mesh_kd_order", "ocl_gb300_mesh_kd_rank", "ocl_gb300_overlap_sets",
     "ocl_gb300_certificate_check", "ocl_gb300_batch_create", "ocl_gb300_batch_run", "ocl_gb300_batch_info_get",
-    "ocl_gb300_batch_release",
+    "ocl_gb300_batch_release", "ocl_gb300_server_create", "ocl_gb300_server_add_mesh",
+    "ocl_gb300_server_submit_drop", "ocl_gb300_server_submit_adaptive", "ocl_gb300_server_wait",
+    "ocl_gb300_server_cancel", "ocl_gb300_server_stats_get", "ocl_gb300_server_pause", "ocl_gb300_server_destroy",
 ]
 
 _lib = None
@@ -78,6 +80,16 @@ def lib():
     L.ocl_gb300_batch_run.argtypes = [C.c_void_p, C.c_void_p, st]
     L.ocl_gb300_batch_info_get.argtypes = [C.c_void_p, C.POINTER(_abi.BatchInfo)]
     L.ocl_gb300_batch_release.argtypes = [C.c_void_p]
+    L.ocl_gb300_server_create.argtypes = [C.POINTER(_abi.ServerOpts), C.POINTER(C.c_void_p)]
+    L.ocl_gb300_server_add_mesh.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]
+    L.ocl_gb300_server_submit_drop.argtypes = [C.c_void_p, C.c_int32, cd, _dp, C.c_uint64, _dp, _dp, _ip, _u64p]
+    L.ocl_gb300_server_submit_adaptive.argtypes = [C.c_void_p, C.c_int32, cd, _dp, C.c_uint64, C.c_double,
+                                                   C.c_double, C.c_double, _dp, _dp, _ip, C.c_uint64, _u64p, _u64p]
+    L.ocl_gb300_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_double, C.POINTER(_abi.RequestInfo)]
+    L.ocl_gb300_server_cancel.argtypes = [C.c_void_p, C.c_uint64]
+    L.ocl_gb300_server_stats_get.argtypes = [C.c_void_p, C.POINTER(_abi.ServerStats)]
+    L.ocl_gb300_server_pause.argtypes = [C.c_void_p, C.c_int32]
+    L.ocl_gb300_server_destroy.argtypes = [C.c_void_p]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -371,5 +383,104 @@ class DropBatch:
     def __del__(self):
         try:
             self.release()
+        except Exception:
+            pass
+
+
+class ServerRequest:
+    """A submitted request: its id and the arrays the results go to (kept
+    alive until the request is waited for)."""
+
+    def __init__(self, rid, kind, arrays):
+        self.id = rid
+        self.kind = kind
+        self.arrays = arrays
+        self.info = None
+
+
+class Server:
+    """Request loop over device-resident meshes (ocl_gb300_server_*):
+    submit_drop / submit_adaptive from any thread, wait() for results."""
+
+    def __init__(self, hbm_budget_bytes=0, slots=0, max_batch_requests=0, list_capacity=0):
+        opts = _abi.ServerOpts(hbm_budget_bytes, slots, max_batch_requests, list_capacity, 0)
+        h = C.c_void_p()
+        check(lib().ocl_gb300_server_create(C.byref(opts), C.byref(h)))
+        self._h = h
+        self._meshes = []
+
+    def add_mesh(self, mesh) -> int:
+        mid = C.c_int32(0)
+        check(lib().ocl_gb300_server_add_mesh(self._h, mesh.handle, C.byref(mid)))
+        self._meshes.append(mesh)
+        return mid.value
+
+    def submit_drop(self, mesh_id, cutter, cl) -> ServerRequest:
+        cl = _d(cl, 3)
+        M = cl.shape[0]
+        z = np.empty(M)
+        cc = np.empty((M, 3))
+        ty = np.empty(M, dtype=np.int32)
+        rid = C.c_uint64(0)
+        desc = cutter.desc()
+        check(lib().ocl_gb300_server_submit_drop(self._h, mesh_id, C.byref(desc), _p(cl), M, _p(z), _p(cc),
+                                                 _p(ty, _ip), C.byref(rid)))
+        return ServerRequest(rid.value, "drop", (cl, z, cc, ty))
+
+    def submit_adaptive(self, mesh_id, cutter, spans, sampling, min_sampling, cos_limit=0.999, cap=None):
+        spans = _d(spans, _abi.SPAN_DOUBLES)
+        if cap is None:  # bisection ends at min_sampling: about two points per min_sampling of length
+            length = float(np.sum(np.hypot(spans[:, 4] - spans[:, 1], spans[:, 5] - spans[:, 2]))) + 1.0
+            cap = int(2 * length / min_sampling + 2 * len(spans) + 64)
+            if (spans[:, 0] != 0).any():
+                cap *= 8  # arcs are longer than their chords
+        xyz = np.empty((cap, 3))
+        cc = np.empty((cap, 3))
+        ty = np.empty(cap, dtype=np.int32)
+        n = C.c_uint64(0)
+        rid = C.c_uint64(0)
+        desc = cutter.desc()
+        check(lib().ocl_gb300_server_submit_adaptive(self._h, mesh_id, C.byref(desc), _p(spans), spans.shape[0],
+                                                     sampling, min_sampling, cos_limit, _p(xyz), _p(cc),
+                                                     _p(ty, _ip), cap, C.byref(n), C.byref(rid)))
+        return ServerRequest(rid.value, "adaptive", (spans, xyz, cc, ty, n))
+
+    def wait(self, req: ServerRequest, timeout=-1.0):
+        """Waits for the request; returns (status, results, info) with results
+        (z, cc, type) for a drop and (xyz, cc, type) for an adaptive path."""
+        info = _abi.RequestInfo()
+        st = lib().ocl_gb300_server_wait(self._h, req.id, float(timeout), C.byref(info))
+        if st == _abi.PENDING:
+            return _abi.PENDING, None, None
+        check(st)
+        d = {"status": info.status, "batches": info.batches, "points": info.points, "queue_ms": info.queue_ms,
+             "latency_ms": info.latency_ms, "message": info.message.decode(errors="replace")}
+        req.info = d
+        if req.kind == "drop":
+            _, z, cc, ty = req.arrays
+            return info.status, (z, cc, ty), d
+        _, xyz, cc, ty, n = req.arrays
+        k = min(int(n.value), len(ty))
+        return info.status, (xyz[:k], cc[:k], ty[:k]), d
+
+    def cancel(self, req: ServerRequest):
+        check(lib().ocl_gb300_server_cancel(self._h, req.id))
+
+    def pause(self, paused=True):
+        check(lib().ocl_gb300_server_pause(self._h, 1 if paused else 0))
+
+    def stats(self) -> dict:
+        out = _abi.ServerStats()
+        check(lib().ocl_gb300_server_stats_get(self._h, C.byref(out)))
+        return out.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ocl_gb300_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass

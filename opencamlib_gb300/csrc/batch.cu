@@ -87,10 +87,9 @@ struct Wave {
     uint64_t points = 0;
     int end_bit = 32;
     size_t sort_bytes = 0;
-    DevBuf<DropCtx> ctxs;
-    DevBuf<BatchIn> in;
-    DevBuf<uint2> tiles;
-    DevBuf<uint32_t> joblist;
+    // byte offsets of the wave's tables in the batch's arena: job contexts,
+    // inputs, tiles and job lists of the launches
+    size_t off_ctx = 0, off_in = 0, off_tiles = 0, off_jobs = 0;
     std::vector<Launch> launches;
     std::vector<std::vector<size_t>> chains;  // screen variant chains (indices into launches)
     int ncounters = 0;
@@ -122,6 +121,8 @@ struct Batch {
     DevBuf<EdgeRes> edge_res;
     DevBuf<uint2> edge_queue;
     DevBuf<unsigned> tile_counters;
+    DevBuf<unsigned char> arena;       // every wave's tables (grow-only)
+    std::vector<unsigned char> blob;   // host image of the arena
     size_t max_counters = 0;
     std::vector<cudaStream_t> side;
     cudaEvent_t fork = nullptr;
@@ -357,13 +358,17 @@ int build_wave(Batch& b, Wave& w) {
     w.ncounters = counter;
     w.end_bit = 32 + (int)bits_for(J);
     w.sort_bytes = batch_sort_bytes(w.points, w.end_bit);
-    if (!w.ctxs.alloc(J) || !w.in.alloc(J) || !w.tiles.alloc(std::max<size_t>(tiles.size(), 1)) ||
-        !w.joblist.alloc(std::max<size_t>(jl.size(), 1)))
-        return OCL_GB300_OOM;
-    CK(cudaMemcpy(w.ctxs.p, ctx.data(), J * sizeof(DropCtx), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(w.in.p, in.data(), J * sizeof(BatchIn), cudaMemcpyHostToDevice));
-    if (!tiles.empty()) CK(cudaMemcpy(w.tiles.p, tiles.data(), tiles.size() * sizeof(uint2), cudaMemcpyHostToDevice));
-    if (!jl.empty()) CK(cudaMemcpy(w.joblist.p, jl.data(), jl.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    // the tables go into the host image of the arena (256-byte aligned parts)
+    auto put = [&](const void* src, size_t bytes) {
+        const size_t off = (b.blob.size() + 255) & ~(size_t)255;
+        b.blob.resize(off + std::max<size_t>(bytes, 1));
+        if (bytes) std::memcpy(b.blob.data() + off, src, bytes);
+        return off;
+    };
+    w.off_ctx = put(ctx.data(), J * sizeof(DropCtx));
+    w.off_in = put(in.data(), J * sizeof(BatchIn));
+    w.off_tiles = put(tiles.data(), tiles.size() * sizeof(uint2));
+    w.off_jobs = put(jl.data(), jl.size() * sizeof(uint32_t));
     return OCL_GB300_OK;
 }
 
@@ -383,14 +388,15 @@ int alloc_workspace(Batch& b) {
         sortb = std::max<uint64_t>(sortb, batch_sort_bytes(w.points, end_bit));
     }
     ncnt = 2 * 16 + 8;
-    if (!b.keys.alloc(P) || !b.keys2.alloc(P) || !b.idx.alloc(P) || !b.idx2.alloc(P) || !b.cls.alloc(3 * P) ||
-        !b.perm.alloc(P) || !b.cand.alloc(C) || !b.cand_hi.alloc(C) || !b.cand_lo.alloc(C) || !b.ncand.alloc(P) ||
-        !b.blo.alloc(P) || !b.list.alloc(P) || !b.list2.alloc(P) || !b.sparse.alloc(std::max<uint64_t>(S, 1)) ||
-        !b.counters.alloc(b.subs.size() * (C_NCOUNTERS + 1)) || !b.sort_tmp.alloc(std::max<uint64_t>(sortb, 1)) ||
-        !b.tile_counters.alloc(ncnt))
+    if (!b.keys.reserve(P) || !b.keys2.reserve(P) || !b.idx.reserve(P) || !b.idx2.reserve(P) ||
+        !b.cls.reserve(3 * P) || !b.perm.reserve(P) || !b.cand.reserve(C) || !b.cand_hi.reserve(C) ||
+        !b.cand_lo.reserve(C) || !b.ncand.reserve(P) || !b.blo.reserve(P) || !b.list.reserve(P) ||
+        !b.list2.reserve(P) || !b.sparse.reserve(std::max<uint64_t>(S, 1)) ||
+        !b.counters.reserve(b.subs.size() * (C_NCOUNTERS + 1)) || !b.sort_tmp.reserve(std::max<uint64_t>(sortb, 1)) ||
+        !b.tile_counters.reserve(ncnt))
         return OCL_GB300_OOM;
-    if (Bp && (!b.edge_slots.alloc(Bp * EDGE_SLOTS) || !b.edge_n.alloc(Bp) || !b.edge_res.alloc(Bp * EDGE_SLOTS) ||
-               !b.edge_queue.alloc(Bp * EDGE_SLOTS)))
+    if (Bp && (!b.edge_slots.reserve(Bp * EDGE_SLOTS) || !b.edge_n.reserve(Bp) ||
+               !b.edge_res.reserve(Bp * EDGE_SLOTS) || !b.edge_queue.reserve(Bp * EDGE_SLOTS)))
         return OCL_GB300_OOM;
     b.max_counters = (size_t)ncnt;
     b.workspace_bytes = P * (2 * 8 + 2 * 4 + 24 + 4 + 2 + 4 + 2 * 4) + C * 12 + S * 4 + sortb +
@@ -400,11 +406,11 @@ int alloc_workspace(Batch& b) {
 
 BatchView view_of(const Batch& b, const Wave& w, const Launch& L) {
     BatchView v;
-    v.ctxs = w.ctxs.p;
-    v.tiles = w.tiles.p + L.tile0;
+    v.ctxs = reinterpret_cast<const DropCtx*>(b.arena.p + w.off_ctx);
+    v.tiles = reinterpret_cast<const uint2*>(b.arena.p + w.off_tiles) + L.tile0;
     v.ntiles = (unsigned)L.ntiles;
     v.next = L.counter >= 0 ? b.tile_counters.p + L.counter : nullptr;
-    v.jobs = w.joblist.p + L.job0;
+    v.jobs = reinterpret_cast<const uint32_t*>(b.arena.p + w.off_jobs) + L.job0;
     v.njobs = (unsigned)L.njobs;
     return v;
 }
@@ -434,7 +440,7 @@ int enqueue(Batch& b, cudaStream_t stream, uint64_t* launches) {
                            w.sub.size() * (C_NCOUNTERS + 1) * sizeof(unsigned long long), stream));
         CK(cudaMemsetAsync(b.tile_counters.p, 0, (size_t)w.ncounters * sizeof(unsigned), stream));
         int st = OCL_GB300_OK;
-        batch_launch_order(w.in.p, (uint32_t)w.sub.size(), w.points, b.keys.p, b.idx.p, b.keys2.p, b.idx2.p,
+        batch_launch_order(reinterpret_cast<const BatchIn*>(b.arena.p + w.off_in), (uint32_t)w.sub.size(), w.points, b.keys.p, b.idx.p, b.keys2.p, b.idx2.p,
                            b.sort_tmp.p, b.sort_tmp.n, w.end_bit, b.cls.p, b.perm.p, stream, &st);
         if (st) return st;
         n += 2 + 4;  // Morton, gather, the sort's passes
@@ -536,15 +542,20 @@ int make_subjobs(Batch& b, const ocl_gb300_drop_job* jobs, Mesh* const* meshes, 
     return OCL_GB300_OK;
 }
 
-int prepare(Batch& b) {
+// Waves, workspace (grown only) and the arena's tables, copied on `stream`
+// (ordered before the run that uses them; no device-wide synchronisation).
+int prepare(Batch& b, cudaStream_t stream) {
     int st = plan_waves(b);
     if (st) return st;
     st = alloc_workspace(b);
     if (st) return st;
+    b.blob.clear();
     for (Wave& w : b.waves) {
         st = build_wave(b, w);
         if (st) return st;
     }
+    if (!b.arena.reserve(b.blob.size())) return OCL_GB300_OOM;
+    CK(cudaMemcpyAsync(b.arena.p, b.blob.data(), b.blob.size(), cudaMemcpyHostToDevice, stream));
     return OCL_GB300_OK;
 }
 
@@ -575,7 +586,7 @@ int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
         for (int cap : caps)
             for (int mult : mults) {
                 probe.conf[v] = VariantConf{cap, mult};
-                status = prepare(probe);
+                status = prepare(probe, stream);
                 if (status) break;
                 float t = 0.0f;
                 for (int rep = 0; rep < 3 && !status; ++rep) {
@@ -636,7 +647,10 @@ int batch_create(const ocl_gb300_drop_job* jobs, Mesh* const* meshes, uint64_t n
             cudaStreamDestroy(s);
         }
     }
-    if (!st) st = prepare(*b);
+    if (!st) {
+        st = prepare(*b, 0);
+        if (!st && cudaStreamSynchronize(0) != cudaSuccess) st = OCL_GB300_DEVICE_ERROR;
+    }
     if (!st) {
         for (int k = 0; k < 4; ++k) {
             cudaStream_t s;
@@ -757,5 +771,33 @@ void batch_info(const Batch& b, ocl_gb300_batch_info* out) {
 }
 
 void batch_destroy(Batch* b) { delete b; }
+
+Batch* batch_new(uint64_t workspace_bytes, uint64_t chunk_points, int list_capacity) {
+    Batch* b = new Batch();
+    if (workspace_bytes) b->budget = workspace_bytes;
+    if (chunk_points) b->chunk = chunk_points;
+    b->use_graph = false;
+    b->context = context_key();
+    (void)list_capacity;
+    return b;
+}
+
+// New jobs on an existing batch: planned on the host, the workspace grown
+// only where it is too small, the tables copied on `stream`.  The batch must
+// not be running (its previous run on `stream` is ordered before).
+int batch_reset(Batch& b, const ocl_gb300_drop_job* jobs, Mesh* const* meshes, uint64_t njobs, int list_capacity,
+                cudaStream_t stream) {
+    if (b.exec) {
+        cudaGraphExecDestroy(b.exec);
+        b.exec = nullptr;
+    }
+    b.use_graph = false;
+    int st = make_subjobs(b, jobs, meshes, njobs);
+    if (st) return st;
+    for (auto& kv : b.conf) kv.second.cap = list_capacity > 0 ? list_capacity : CAND_K;
+    st = ensure_exact_smem();
+    if (st) return st;
+    return prepare(b, stream);
+}
 
 }  // namespace oclg

@@ -523,4 +523,94 @@ int ocl_gb300_batch_release(ocl_gb300_batch batch) {
     return OCL_GB300_OK;
 }
 
+struct ocl_gb300_server_s {
+    Server* s;
+};
+
+int ocl_gb300_server_create(const ocl_gb300_server_opts* opts, ocl_gb300_server* out) {
+    if (!out) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    *out = nullptr;
+    int st = need_device();
+    if (st) return st;
+    Server* s = nullptr;
+    st = server_create(opts, &s);
+    if (st) return st;
+    *out = new ocl_gb300_server_s{s};
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_server_add_mesh(ocl_gb300_server server, ocl_gb300_mesh mesh, int32_t* mesh_id) {
+    if (!server || !mesh || !mesh_id) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_add_mesh(*server->s, mesh->m, mesh_id);
+}
+
+int ocl_gb300_server_submit_drop(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
+                                 const double* cl_xyz, uint64_t M, double* z_out, double* cc_out, int32_t* type_out,
+                                 uint64_t* request_id) {
+    if (!server || !cutter || !request_id || (M > 0 && (!cl_xyz || !z_out || !cc_out || !type_out))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_submit_drop(*server->s, mesh_id, *cutter, cl_xyz, M, z_out, cc_out, type_out, request_id);
+}
+
+int ocl_gb300_server_submit_adaptive(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
+                                     const double* spans, uint64_t S, double sampling, double min_sampling,
+                                     double cos_limit, double* xyz_out, double* cc_out, int32_t* type_out,
+                                     uint64_t cap, uint64_t* count, uint64_t* request_id) {
+    if (!server || !cutter || !request_id || !count || (S > 0 && !spans) ||
+        (cap > 0 && (!xyz_out || !cc_out || !type_out))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_submit_adaptive(*server->s, mesh_id, *cutter, spans, S, sampling, min_sampling, cos_limit, xyz_out,
+                                  cc_out, type_out, cap, count, request_id);
+}
+
+int ocl_gb300_server_wait(ocl_gb300_server server, uint64_t request_id, double timeout_s,
+                          ocl_gb300_request_info* info) {
+    if (!server) {
+        set_error("null server");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_wait(*server->s, request_id, timeout_s, info);
+}
+
+int ocl_gb300_server_cancel(ocl_gb300_server server, uint64_t request_id) {
+    if (!server) {
+        set_error("null server");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_cancel(*server->s, request_id);
+}
+
+int ocl_gb300_server_stats_get(ocl_gb300_server server, ocl_gb300_server_stats* out) {
+    if (!server || !out) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_stats(*server->s, out);
+}
+
+int ocl_gb300_server_pause(ocl_gb300_server server, int32_t paused) {
+    if (!server) {
+        set_error("null server");
+        return OCL_GB300_BAD_ARG;
+    }
+    return server_pause(*server->s, paused != 0);
+}
+
+int ocl_gb300_server_destroy(ocl_gb300_server server) {
+    if (!server) return OCL_GB300_BAD_ARG;
+    server_destroy(server->s);
+    delete server;
+    return OCL_GB300_OK;
+}
+
 }  // extern "C"

@@ -122,6 +122,24 @@ int batch_create(const ocl_gb300_drop_job* jobs, Mesh* const* meshes, uint64_t n
 int batch_run(Batch& b, cudaStream_t stream, ocl_gb300_stats* stats);
 void batch_info(const Batch& b, ocl_gb300_batch_info* out);
 void batch_destroy(Batch* b);
+// A batch without jobs (for repeated use), and new jobs on an existing one.
+Batch* batch_new(uint64_t workspace_bytes, uint64_t chunk_points, int list_capacity);
+int batch_reset(Batch& b, const ocl_gb300_drop_job* jobs, Mesh* const* meshes, uint64_t njobs, int list_capacity,
+                cudaStream_t stream);
+
+struct Server;
+int server_create(const ocl_gb300_server_opts* opts, Server** out);
+void server_destroy(Server* s);
+int server_add_mesh(Server& s, Mesh* m, int32_t* id);
+int server_submit_drop(Server& s, int32_t mesh_id, const ocl_gb300_cutter& c, const double* cl, uint64_t M,
+                       double* z, double* cc, int32_t* ty, uint64_t* id);
+int server_submit_adaptive(Server& s, int32_t mesh_id, const ocl_gb300_cutter& c, const double* spans, uint64_t S,
+                           double sampling, double min_sampling, double cos_limit, double* xyz, double* cc,
+                           int32_t* ty, uint64_t cap, uint64_t* count, uint64_t* id);
+int server_wait(Server& s, uint64_t id, double timeout_s, ocl_gb300_request_info* info);
+int server_cancel(Server& s, uint64_t id);
+int server_stats(Server& s, ocl_gb300_server_stats* out);
+int server_pause(Server& s, bool paused);
 
 struct DropWork;
 // The per-call context fields that depend only on the mesh and the cutter:

@@ -11,18 +11,12 @@
 #include <vector>
 
 #include "drop.cuh"
+#include "paths.cuh"
 #include "util.cuh"
 
 namespace oclg {
 
 static const double PI_REF = 3.1415926535897932;  // common/numeric.hpp:38
-
-struct SpanH {
-    int type;
-    double p1[3], p2[3], c[3];
-    bool dir;
-    double radius, length;
-};
 
 // Arc::xyIncludedAngle (geo/arc.cpp:73-94)
 static double xy_included_angle(const double* v1, const double* v2, bool dir) {
@@ -219,12 +213,6 @@ int path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, d
     return OCL_GB300_OK;
 }
 
-struct APoint {
-    double p[3];
-    double cc[3];
-    int32_t type;
-};
-
 // AdaptivePathDropCutter::flat (adaptivepathdropcutter.cpp:88-94)
 static bool flat_h(const APoint& s, const APoint& m, const APoint& e, double cos_limit) {
     double v1[3], v2[3];
@@ -239,93 +227,101 @@ static bool flat_h(const APoint& s, const APoint& m, const APoint& e, double cos
     return (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) > cos_limit;
 }
 
-int adaptive_path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, double sampling,
-                           double min_sampling, double cos_limit, double* xyz, double* cc, int32_t* type,
-                           uint64_t cap, uint64_t* count, ocl_gb300_stats* stats) {
+int ApdcRun::init(const double* spans, uint64_t S, double sampling, double min_sampling, double cos_limit) {
     if (!(sampling > 0.0) || !(min_sampling > 0.0)) {
         set_error("sampling and min_sampling must be > 0");
         return OCL_GB300_BAD_ARG;
     }
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    std::vector<SpanH> sp(S);
+    S_ = S;
+    sampling_ = sampling;
+    min_sampling_ = min_sampling;
+    cos_limit_ = cos_limit;
+    sp_.assign(S, SpanH());
     for (uint64_t k = 0; k < S; ++k)
-        if (!span_init(sp[k], spans + OCL_GB300_SPAN_DOUBLES * k)) {
+        if (!span_init(sp_[k], spans + OCL_GB300_SPAN_DOUBLES * k)) {
             set_error("invalid span " + std::to_string(k));
             return OCL_GB300_BAD_ARG;
         }
-    // span end points (AdaptivePathDropCutter::adaptive_sampling_run, :57-70)
-    std::vector<double> cl;
+    // span end points first (AdaptivePathDropCutter::adaptive_sampling_run, :57-70)
+    cl_.clear();
     for (uint64_t k = 0; k < S; ++k) {
         double a[3], b[3];
-        span_point(sp[k], 0.0, a);
-        span_point(sp[k], 1.0, b);
-        cl.insert(cl.end(), a, a + 3);
-        cl.insert(cl.end(), b, b + 3);
+        span_point(sp_[k], 0.0, a);
+        span_point(sp_[k], 1.0, b);
+        cl_.insert(cl_.end(), a, a + 3);
+        cl_.insert(cl_.end(), b, b + 3);
     }
-    std::vector<double> z, ccv;
-    std::vector<int32_t> ty;
-    int st = drop_host(m, cp, cl, z, ccv, ty, stats);
-    if (st) return st;
+    ends_ = true;
+    depth_ = 0;
+    done_ = S == 0;
+    starts_.clear();
+    level_.clear();
+    leaves_.clear();
+    return OCL_GB300_OK;
+}
+
+// adaptive_sample (:72-86): every midpoint of the current level
+void ApdcRun::next_level() {
+    cl_.clear();
+    mt_.assign(level_.size(), 0.0);
+    for (size_t j = 0; j < level_.size(); ++j) {
+        const Iv& iv = level_[j];
+        mt_[j] = iv.t0 + (iv.t1 - iv.t0) / 2.0;
+        double p[3];
+        span_point(sp_[iv.span], mt_[j], p);
+        cl_.insert(cl_.end(), p, p + 3);
+    }
+}
+
+void ApdcRun::consume(const double* z, const double* ccv, const int32_t* ty) {
     auto mk = [&](size_t i) {
         APoint p;
-        p.p[0] = cl[3 * i];
-        p.p[1] = cl[3 * i + 1];
+        p.p[0] = cl_[3 * i];
+        p.p[1] = cl_[3 * i + 1];
         p.p[2] = z[i];
-        std::memcpy(p.cc, &ccv[3 * i], 3 * sizeof(double));
+        std::memcpy(p.cc, ccv + 3 * i, 3 * sizeof(double));
         p.type = ty[i];
         return p;
     };
-    struct Iv {
-        uint64_t span;
-        double t0, t1;
-        APoint a, b;
-    };
-    struct Leaf {
-        uint64_t span;
-        double t1;
-        APoint p;
-    };
-    std::vector<APoint> starts(S);
-    std::vector<Iv> level;
-    for (uint64_t k = 0; k < S; ++k) {
-        starts[k] = mk(2 * k);
-        level.push_back({k, 0.0, 1.0, mk(2 * k), mk(2 * k + 1)});
-    }
-    std::vector<Leaf> leaves;
-    for (int depth = 0; !level.empty(); ++depth) {
-        // adaptive_sample (:72-86): drop every midpoint of this level
-        std::vector<double> mc;
-        std::vector<double> mt(level.size());
-        for (size_t j = 0; j < level.size(); ++j) {
-            const Iv& iv = level[j];
-            mt[j] = iv.t0 + (iv.t1 - iv.t0) / 2.0;
-            double p[3];
-            span_point(sp[iv.span], mt[j], p);
-            mc.insert(mc.end(), p, p + 3);
+    if (ends_) {
+        ends_ = false;
+        starts_.resize(S_);
+        for (uint64_t k = 0; k < S_; ++k) {
+            starts_[k] = mk(2 * k);
+            level_.push_back({k, 0.0, 1.0, mk(2 * k), mk(2 * k + 1)});
         }
-        cl.swap(mc);
-        st = drop_host(m, cp, cl, z, ccv, ty, stats);
-        if (st) return st;
-        std::vector<Iv> next;
-        for (size_t j = 0; j < level.size(); ++j) {
-            const Iv& iv = level[j];
-            APoint mid = mk(j);
-            double dx = iv.b.p[0] - iv.a.p[0], dy = iv.b.p[1] - iv.a.p[1];
-            double fw_step = std::sqrt(dx * dx + dy * dy);
-            bool split = (fw_step > sampling) || ((!flat_h(iv.a, mid, iv.b, cos_limit)) && (fw_step > min_sampling));
-            if (split && depth < 60) {
-                next.push_back({iv.span, iv.t0, mt[j], iv.a, mid});
-                next.push_back({iv.span, mt[j], iv.t1, mid, iv.b});
-            } else {
-                leaves.push_back({iv.span, iv.t1, iv.b});
-            }
-        }
-        level.swap(next);
+        next_level();
+        return;
     }
-    std::stable_sort(leaves.begin(), leaves.end(), [](const Leaf& a, const Leaf& b) {
-        return a.span != b.span ? a.span < b.span : a.t1 < b.t1;
-    });
-    const uint64_t n = S + leaves.size();
+    std::vector<Iv> next;
+    for (size_t j = 0; j < level_.size(); ++j) {
+        const Iv& iv = level_[j];
+        APoint mid = mk(j);
+        double dx = iv.b.p[0] - iv.a.p[0], dy = iv.b.p[1] - iv.a.p[1];
+        double fw_step = std::sqrt(dx * dx + dy * dy);
+        bool split = (fw_step > sampling_) || ((!flat_h(iv.a, mid, iv.b, cos_limit_)) && (fw_step > min_sampling_));
+        if (split && depth_ < 60) {
+            next.push_back({iv.span, iv.t0, mt_[j], iv.a, mid});
+            next.push_back({iv.span, mt_[j], iv.t1, mid, iv.b});
+        } else {
+            leaves_.push_back({iv.span, iv.t1, iv.b});
+        }
+    }
+    level_.swap(next);
+    ++depth_;
+    if (level_.empty()) {
+        std::stable_sort(leaves_.begin(), leaves_.end(), [](const Leaf& a, const Leaf& b) {
+            return a.span != b.span ? a.span < b.span : a.t1 < b.t1;
+        });
+        cl_.clear();
+        done_ = true;
+    } else {
+        next_level();
+    }
+}
+
+int ApdcRun::write(double* xyz, double* cc, int32_t* type, uint64_t cap, uint64_t* count) const {
+    const uint64_t n = S_ + leaves_.size();
     *count = n;
     if (n > cap) {
         set_error("output buffer too small");
@@ -333,17 +329,34 @@ int adaptive_path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint
     }
     uint64_t w = 0;
     size_t li = 0;
-    for (uint64_t k = 0; k < S; ++k) {
+    for (uint64_t k = 0; k < S_; ++k) {
         auto put = [&](const APoint& p) {
             std::memcpy(xyz + 3 * w, p.p, 3 * sizeof(double));
             std::memcpy(cc + 3 * w, p.cc, 3 * sizeof(double));
             type[w] = p.type;
             ++w;
         };
-        put(starts[k]);
-        while (li < leaves.size() && leaves[li].span == k) put(leaves[li++].p);
+        put(starts_[k]);
+        while (li < leaves_.size() && leaves_[li].span == k) put(leaves_[li++].p);
     }
     return OCL_GB300_OK;
+}
+
+int adaptive_path_drop_run(Mesh& m, const CutterP& cp, const double* spans, uint64_t S, double sampling,
+                           double min_sampling, double cos_limit, double* xyz, double* cc, int32_t* type,
+                           uint64_t cap, uint64_t* count, ocl_gb300_stats* stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    ApdcRun run;
+    int st = run.init(spans, S, sampling, min_sampling, cos_limit);
+    if (st) return st;
+    std::vector<double> z, ccv;
+    std::vector<int32_t> ty;
+    while (!run.done()) {
+        st = drop_host(m, cp, run.points(), z, ccv, ty, stats);
+        if (st) return st;
+        run.consume(z.data(), ccv.data(), ty.data());
+    }
+    return run.write(xyz, cc, type, cap, count);
 }
 
 }  // namespace oclg

@@ -46,6 +46,12 @@ struct DevBuf {
         }
         return true;
     }
+    // Grow-only: keeps the buffer (and its contents) when it already holds
+    // `count` elements; reallocating frees, and a free synchronises the device.
+    bool reserve(size_t count) {
+        if (count <= n && (p || count == 0)) return true;
+        return alloc(count);
+    }
     bool ok() const { return n == 0 || p != nullptr; }
     void release() {
         if (p) cudaFree(p);
