@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--no-fp64-full", action="store_true",
                     help="skip the plain FP64 run over the whole raster (mixed == FP64 check and speed-up)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-job batching measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop measurement")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the request-loop measurement and print it")
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the 64-job batching measurement and print it (for profiling)")
     ap.add_argument("--profile-step", action="store_true",
@@ -376,6 +379,87 @@ def batch_measurements(steps=2, warmup=1, njobs=64, autotune=True):
     return out
 
 
+def serving_measurements(nreq=200, serial_sample=20):
+    """The serving workload (workloads.serving_requests(seed=5)): 8 resident
+    meshes, 200 requests with Poisson arrivals at 200/s, drops and adaptive
+    paths 1:1, through ocl_gb300_server (admission under a 32 GiB budget,
+    2 batches in flight).  Reports p50/p99 latency from submission to
+    completion and CL points per second over the run, and beside it the same
+    requests run alone one after another on a sample (mixed precision) and
+    the drops of that sample alone in plain FP64."""
+    import threading
+    from opencamlib_gb300 import _abi, _native, workloads as w
+    t0 = time.time()
+    mesh_tris = w.serving_meshes(5, 8)
+    meshes = [_native.DeviceMesh(t) for t in mesh_tris]
+    reqs = w.serving_requests(5, nreq)
+    payload = [w.serving_payload(r, mesh_tris[r["mesh"]]) for r in reqs]
+    cutter = [w.batch_cutter(r["cutter"], r["d"]) for r in reqs]
+    setup_s = time.time() - t0
+    srv = _native.Server(hbm_budget_bytes=32 << 30, slots=2, max_batch_requests=64)
+    ids = [srv.add_mesh(m) for m in meshes]
+    handles = [None] * nreq
+
+    def client():
+        start = time.perf_counter()
+        for k, r in enumerate(reqs):
+            delay = r["t"] - (time.perf_counter() - start)
+            if delay > 0:
+                time.sleep(delay)
+            if r["kind"] == "drop":
+                handles[k] = srv.submit_drop(ids[r["mesh"]], cutter[k], payload[k])
+            else:
+                handles[k] = srv.submit_adaptive(ids[r["mesh"]], cutter[k], payload[k], r["sampling"],
+                                                 r["min_sampling"])
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    lat = {"drop": [], "adaptive": []}
+    bad = 0
+    for k, h in enumerate(handles):
+        st, res, info = srv.wait(h)
+        if st != _abi.OK:
+            bad += 1
+            continue
+        lat[reqs[k]["kind"]].append(info["latency_ms"])
+    stats = srv.stats()
+    srv.close()
+    # the same requests alone, one after another (a sample)
+    sample = list(range(0, nreq, max(1, nreq // serial_sample)))[:serial_sample]
+    pts_serial, t_serial, pts_fp64, t_fp64 = 0, 0.0, 0, 0.0
+    for k in sample:
+        r = reqs[k]
+        m = meshes[r["mesh"]]
+        t1 = time.perf_counter()
+        if r["kind"] == "drop":
+            m.drop(cutter[k], payload[k], "mixed")
+            pts_serial += len(payload[k])
+        else:
+            xyz, _, _, st = m.adaptive_path_drop(cutter[k], payload[k], r["sampling"], r["min_sampling"])
+            pts_serial += len(xyz)
+        t_serial += time.perf_counter() - t1
+        if r["kind"] == "drop" and len(payload[k]) <= 200000:
+            t1 = time.perf_counter()
+            m.drop(cutter[k], payload[k], "fp64")
+            t_fp64 += time.perf_counter() - t1
+            pts_fp64 += len(payload[k])
+    for m in meshes:
+        m.release()
+    pct = lambda v, q: float(np.percentile(v, q)) if v else None
+    return {"requests": nreq, "failed": bad, "setup_s": setup_s,
+            "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"], "mean_ms": stats["mean_ms"], "max_ms": stats["max_ms"],
+            "drop_p50_ms": pct(lat["drop"], 50), "drop_p99_ms": pct(lat["drop"], 99),
+            "adaptive_p50_ms": pct(lat["adaptive"], 50), "adaptive_p99_ms": pct(lat["adaptive"], 99),
+            "cl_points": stats["points"], "elapsed_s": stats["elapsed_s"],
+            "cl_points_per_s": stats["points"] / max(stats["elapsed_s"], 1e-9), "batches": stats["batches"],
+            "serial_sample_requests": len(sample),
+            "serial_mixed_points_per_s": pts_serial / max(t_serial, 1e-9),
+            "serial_fp64_drop_points_per_s": (pts_fp64 / t_fp64) if t_fp64 else None,
+            "arrivals": "Poisson 200/s (seeded), 1:1 drops (100-1e6 points) and adaptive paths (10-500 mm, "
+                        "sampling 0.1-1, min 0.01), 8 meshes 1e4-2e6 triangles, 5 cutter families d 2-12 mm"}
+
+
 def mixed_vs_fp64(mesh, cl, cuts):
     """Per cutter, the mixed path and the plain FP64 kernel (the reference's
     KD-tree algorithm on the device) over the same points: results compared
@@ -528,6 +612,10 @@ def main():
             if stats_out is not None:
                 stats_out.append((name, st))
 
+    if args.serve_only:
+        print(json.dumps({"serving": serving_measurements()}), flush=True)
+        return
+
     if args.batch_only:
         print(json.dumps({"batch": batch_measurements()}), flush=True)
         return
@@ -648,6 +736,11 @@ def main():
     except Exception as e:  # reported, never required
         compute = {"error": str(e)}
     roof = roofline_block(tris, M, cuts, breakdown, stage, args, compute)
+    if aux is not None and not args.no_serve and "error" not in aux:
+        try:
+            aux["serving"] = serving_measurements()
+        except Exception as e:  # reported, never required
+            aux["serving"] = {"error": str(e)}
     if aux is not None and not args.no_batch and "error" not in aux:
         try:
             aux["batch"] = batch_measurements()

@@ -560,7 +560,8 @@ int prepare(Batch& b, cudaStream_t stream) {
 }
 
 // Candidate-list capacity and screen grid size per variant, timed on a
-// probe: each job of the variant cut to its first probe_points points.
+// probe: the first 4,096 points of up to 32 chunks of the variant, each
+// configuration run twice (the second run timed).
 int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
     const int caps[3] = {64, 128, 256};
     const int mults[2] = {1, 2};
@@ -575,10 +576,11 @@ int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
         Batch probe;
         probe.budget = b.budget;
         probe.chunk = b.chunk;
+        // the first 4,096 points of at most 32 chunks of the variant
         for (const SubJob& s : all)
-            if (s.v == v) {
+            if (s.v == v && probe.subs.size() < 32) {
                 SubJob q = s;
-                q.M = std::min<uint64_t>(q.M, 16384);
+                q.M = std::min<uint64_t>(q.M, 4096);
                 probe.subs.push_back(q);
             }
         float best = 1e30f;
@@ -589,7 +591,7 @@ int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
                 status = prepare(probe, stream);
                 if (status) break;
                 float t = 0.0f;
-                for (int rep = 0; rep < 3 && !status; ++rep) {
+                for (int rep = 0; rep < 2 && !status; ++rep) {
                     if (cudaEventRecord(e0, stream) != cudaSuccess) status = OCL_GB300_DEVICE_ERROR;
                     if (!status) status = enqueue(probe, stream, nullptr);
                     if (!status && cudaEventRecord(e1, stream) != cudaSuccess) status = OCL_GB300_DEVICE_ERROR;

@@ -308,3 +308,61 @@ def batch_points(tris: np.ndarray, M: int, margin: float) -> np.ndarray:
     ys = lo[1] - margin + (np.arange(ny) + 0.5) * (h / ny)
     X, Y = np.meshgrid(xs, ys)
     return np.stack([X.ravel(), Y.ravel(), np.full(X.size, lo[2] - 10.0)], axis=1)
+
+
+def serving_requests(seed: int = 5, n: int = 200, rate: float = 200.0, nmeshes: int = 8):
+    """Seeded request stream of the serving workload: Poisson arrivals at
+    `rate` per second; BatchDropCutter and AdaptivePathDropCutter requests
+    1:1; a mesh uniform over `nmeshes`; a cutter family uniform over the five
+    with diameter U[2, 12] mm; drops with log-uniform 100 .. 1,000,000 raster
+    points over the mesh bbox; adaptive paths of total length U[10, 500] mm
+    (a zig-zag of line spans across the mesh), sampling U[0.1, 1] mm,
+    minimum sampling 0.01 mm.  Returns dicts; points and spans are made by
+    serving_payload() against the mesh's bbox."""
+    u = uniform(seed, 8 * n).reshape(n, 8)
+    t = np.cumsum(-np.log(1.0 - u[:, 0]) / rate)
+    cutters_ = ("cyl", "ball", "bull", "cone", "ballcone")
+    out = []
+    for k in range(n):
+        r = {"t": float(t[k]), "kind": "drop" if u[k, 1] < 0.5 else "adaptive", "mesh": int(u[k, 2] * nmeshes),
+             "cutter": cutters_[min(int(u[k, 3] * 5), 4)], "d": 2.0 + 10.0 * u[k, 4], "u": u[k, 5:].copy()}
+        if r["kind"] == "drop":
+            r["M"] = int(round(math.exp(math.log(100) + u[k, 5] * (math.log(1e6) - math.log(100)))))
+        else:
+            r["length"] = 10.0 + 490.0 * u[k, 5]
+            r["sampling"] = 0.1 + 0.9 * u[k, 6]
+            r["min_sampling"] = 0.01
+        out.append(r)
+    return out
+
+
+def serving_meshes(seed: int = 5, n: int = 8):
+    """The resident meshes of the serving workload: generator cycling over
+    heightfield / sphere / box, N ~ log-uniform 10,000 .. 2,000,000."""
+    u = uniform(seed + 1, n)
+    kinds = ("heightfield", "sphere", "box")
+    return [mesh_of_size(kinds[k % 3], int(round(math.exp(math.log(1e4) + u[k] * (math.log(2e6) - math.log(1e4))))),
+                         seed * 100 + k) for k in range(n)]
+
+
+def serving_payload(req, tris):
+    """CL points (drop) or spans (adaptive path) of a request over a mesh."""
+    p = tris.reshape(-1, 3)
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    z0 = lo[2] - 10.0
+    if req["kind"] == "drop":
+        pts = batch_points(tris, req["M"], 0.0)
+        pts[:, 2] = z0
+        return pts
+    w, h = hi[0] - lo[0], hi[1] - lo[1]
+    L = req["length"]
+    nlines = max(1, int(math.ceil(L / max(w, 1e-3))))
+    spans = []
+    left = L
+    for j in range(nlines):
+        seg = min(w, left)
+        left -= seg
+        y = lo[1] + h * (j + 0.5) / nlines
+        a, b = (lo[0], lo[0] + seg) if j % 2 == 0 else (hi[0], hi[0] - seg)
+        spans.append([0, a, y, z0, b, y, z0, 0, 0, 0, 0])
+    return np.array(spans, dtype=np.float64)
