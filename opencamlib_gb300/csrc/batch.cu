@@ -122,6 +122,7 @@ struct Batch {
     DevBuf<uint2> edge_queue;
     DevBuf<unsigned> tile_counters;
     DevBuf<unsigned char> arena;       // every wave's tables (grow-only)
+    DevBuf<unsigned char> exact_scratch;  // handed-back points with many candidates
     std::vector<unsigned char> blob;   // host image of the arena
     size_t max_counters = 0;
     std::vector<cudaStream_t> side;
@@ -395,11 +396,15 @@ int alloc_workspace(Batch& b) {
         !b.counters.reserve(b.subs.size() * (C_NCOUNTERS + 1)) || !b.sort_tmp.reserve(std::max<uint64_t>(sortb, 1)) ||
         !b.tile_counters.reserve(ncnt))
         return OCL_GB300_OOM;
+    // the exact kernel's scratch only when it is a small part of the budget
+    // (without it, points with very many candidates take the plain kernel)
+    if (b.budget >= 4 * batch_exact_scratch_bytes() && !b.exact_scratch.reserve(batch_exact_scratch_bytes()))
+        return OCL_GB300_OOM;
     if (Bp && (!b.edge_slots.reserve(Bp * EDGE_SLOTS) || !b.edge_n.reserve(Bp) ||
                !b.edge_res.reserve(Bp * EDGE_SLOTS) || !b.edge_queue.reserve(Bp * EDGE_SLOTS)))
         return OCL_GB300_OOM;
     b.max_counters = (size_t)ncnt;
-    b.workspace_bytes = P * (2 * 8 + 2 * 4 + 24 + 4 + 2 + 4 + 2 * 4) + C * 12 + S * 4 + sortb +
+    b.workspace_bytes = P * (2 * 8 + 2 * 4 + 24 + 4 + 2 + 4 + 2 * 4) + C * 12 + S * 4 + sortb + b.exact_scratch.n +
                         Bp * EDGE_SLOTS * (4 + sizeof(EdgeRes) + sizeof(uint2)) + Bp;
     return OCL_GB300_OK;
 }
@@ -482,7 +487,7 @@ int enqueue(Batch& b, cudaStream_t stream, uint64_t* launches) {
                 ++n;
                 break;
             case L_EXACT: {
-                int st2 = batch_launch_exact(v, L.flag, L.blocks, stream);
+                int st2 = batch_launch_exact(v, L.flag, L.blocks, stream, b.exact_scratch.p);
                 if (st2) return st2;
                 ++n;
                 break;

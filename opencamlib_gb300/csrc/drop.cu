@@ -597,185 +597,316 @@ struct ExactShared {
     int* red;
 };
 
-// One handed-back point, by the whole block.
+// Per-block global scratch of the exact kernel for points with more than
+// EXACT_CAP candidates (key == nullptr: none; such points go to the plain
+// kernel).  Block b uses entries [b * cap, (b + 1) * cap).
+struct ExactGlobal {
+    unsigned long long* key;
+    uint32_t* tri;
+    float* hi;
+    float* qt;
+    int cap;
+};
+constexpr int EXACT_GCAP = 1 << 16;       // candidates per point the global scratch holds
+constexpr int EXACT_GBLOCKS = 152 * 2;    // exact-kernel blocks (two resident per SM)
+constexpr size_t EXACT_GBYTES = (size_t)EXACT_GBLOCKS * EXACT_GCAP * (8 + 4 + 4 + 4);
+constexpr int EXACT_BINS = 1024;          // rank histogram of the large path's windows
+
+// (Out of line: one copy serves the shared-memory and the global path.)
+// Gather every triangle whose certified FP32 upper bound lies above the start
+// height into (key, tri, hi, qt)[slot] for slot < cap (one thread per grid
+// cell under the cutter, all levels); returns the number found (may exceed cap).
 template <bool COMP>
-__device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
-                                            uint32_t* __restrict__ list2, unsigned long long* __restrict__ nlist2) {
-    unsigned long long* s_key = S.key;
-    uint32_t* s_tri = S.tri;
-    float* s_hi = S.hi;
-    float* s_qt = S.qt;
-    const float* s_hlb = S.hlb;
-    int& s_n = *S.n;
-    int& s_red = *S.red;
-    const int tid = threadIdx.x, lane = tid & 31;
+__device__ __noinline__ int exact_gather(const DropCtx& ctx, double x, double y, float cx, float cy, float z0l,
+                                            const float* s_hlb, int& s_n, unsigned long long* key, uint32_t* tri,
+                                            float* hiv, float* qtv, int cap) {
+    const int tid = threadIdx.x;
     const GridP& g = ctx.g;
     const float R = ctx.prof.R, gd = ctx.guard, Rg = R + gd, inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    {
-        const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
-        const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
-        const float z0l = __double2float_rd(z0 - g.oz);
-        if (tid == 0) s_n = 0;
-        __syncthreads();
-        // gather: one thread per grid cell under the cutter, all levels
-        for (int L = g.nlev - 1; L >= 0; --L) {
-            int c0, c1, r0, r1;
-            if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
-            const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
-            const Cell* cells = ctx.cells + g.cell_off[L];
-            for (int k = tid; k < ncells; k += blockDim.x) {
-                const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
-                if (cell.count == 0) continue;
-                float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
-                float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
-                float d = sqrtf(dx * dx + dy * dy);
-                if (!(d <= Rg && cell.maxz - hlb_at(s_hlb, d - gd, inv_step) > z0l - gd)) continue;
-                for (uint32_t j = 0; j < cell.count; ++j) {
-                    const Entry e = ctx.entries[cell.start + j];
-                    float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
-                    float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
-                    float de = sqrtf(ex * ex + ey * ey);
-                    float ub = e.maxz - hlb_at(s_hlb, de - gd, inv_step);
-                    if (!(de <= Rg && ub > z0l - gd)) continue;
-                    const Tri32 t = ctx.t32[e.tri];
-                    float qt, qth;
-                    Iv v = COMP ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth)
-                                : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
-                    if (!(v.hi > NEG_INF32)) continue;
-                    const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
-                    if (!(hi > z0l - gd)) continue;
-                    const int slot = atomicAdd(&s_n, 1);
-                    if (slot < EXACT_CAP) {
-                        s_key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
-                        s_tri[slot] = (uint32_t)e.tri;
-                        s_hi[slot] = hi;
-                        s_qt[slot] = qt < 3.0e38f ? qt + t.v0[2] - ctx.E : 3.0e38f;
-                    }
+    if (tid == 0) s_n = 0;
+    __syncthreads();
+    for (int L = g.nlev - 1; L >= 0; --L) {
+        int c0, c1, r0, r1;
+        if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
+        const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
+        const Cell* cells = ctx.cells + g.cell_off[L];
+        for (int k = tid; k < ncells; k += blockDim.x) {
+            const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
+            if (cell.count == 0) continue;
+            float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
+            float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
+            float d = sqrtf(dx * dx + dy * dy);
+            if (!(d <= Rg && cell.maxz - hlb_at(s_hlb, d - gd, inv_step) > z0l - gd)) continue;
+            for (uint32_t j = 0; j < cell.count; ++j) {
+                const Entry e = ctx.entries[cell.start + j];
+                float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                float de = sqrtf(ex * ex + ey * ey);
+                float ub = e.maxz - hlb_at(s_hlb, de - gd, inv_step);
+                if (!(de <= Rg && ub > z0l - gd)) continue;
+                const Tri32 t = ctx.t32[e.tri];
+                float qt, qth;
+                Iv v = COMP ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth)
+                            : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
+                if (!(v.hi > NEG_INF32)) continue;
+                const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
+                if (!(hi > z0l - gd)) continue;
+                const int slot = atomicAdd(&s_n, 1);
+                if (slot < cap) {
+                    key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
+                    tri[slot] = (uint32_t)e.tri;
+                    hiv[slot] = hi;
+                    qtv[slot] = qt < 3.0e38f ? qt + t.v0[2] - ctx.E : 3.0e38f;
                 }
             }
         }
+    }
+    __syncthreads();
+    return s_n;
+}
+
+// Only triangles whose upper bound reaches T are folded, T at most
+// blo - guard (the final height lies above it) and at most every branch
+// threshold of the triangles kept.  A triangle left out lifts the running
+// height to below T at most; below its branch points a kept triangle's effect
+// is max(Z, c) with a fixed c and CC; so max(Z, T) is the same in both folds
+// after every triangle, and the final height, above T, is the same with its
+// CC and type.
+__device__ __forceinline__ float exact_threshold(const DropCtx& ctx, uint32_t i, const float* hiv, const float* qtv,
+                                                 int n, int& s_red) {
+    const int tid = threadIdx.x;
+    const float gd = ctx.guard;
+    float T = NEG_INF32;
+    if (ctx.blo[i] > NEG_INF32) T = ctx.blo[i] - gd;
+    for (int it = 0; T > NEG_INF32; ++it) {
+        if (it == 64) {  // not settled: fold everything
+            T = NEG_INF32;
+            break;
+        }
+        if (tid == 0) s_red = f2o(3.0e38f);
         __syncthreads();
-        const int n = s_n;
-        if (n > EXACT_CAP) {
-            if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
-            __syncthreads();
-            return;
-        }
-        // Only triangles whose upper bound reaches T are folded, T at most
-        // blo - guard (the final height lies above it) and at most every
-        // branch threshold of the triangles kept.  A triangle left out lifts
-        // the running height to below T at most; below its branch points a
-        // kept triangle's effect is max(Z, c) with a fixed c and CC; so
-        // max(Z, T) is the same in both folds after every triangle, and the
-        // final height, above T, is the same with its CC and type.
-        float T = NEG_INF32;
-        if (ctx.blo[i] > NEG_INF32) T = ctx.blo[i] - gd;
-        for (int it = 0; T > NEG_INF32; ++it) {
-            if (it == 64) {  // not settled: fold everything
-                T = NEG_INF32;
-                break;
+        float m = 3.0e38f;
+        for (int k = tid; k < n; k += blockDim.x)
+            if (hiv[k] >= T && qtv[k] - gd < T) m = fminf(m, qtv[k] - gd);
+        if (m < 3.0e38f) atomicMin(&s_red, f2o(m));
+        __syncthreads();
+        const float mt = o2f(s_red);
+        __syncthreads();
+        if (!(mt < T)) break;
+        T = mt;
+    }
+    return T;
+}
+
+// Bitonic sort of keys[0, n) in shared memory (padded to a power of two).
+__device__ __forceinline__ void exact_sort(unsigned long long* s_key, int n) {
+    const int tid = threadIdx.x;
+    int np = 1;
+    while (np < n) np <<= 1;
+    for (int k = n + tid; k < np; k += blockDim.x) s_key[k] = ~0ull;
+    __syncthreads();
+    for (int k = 2; k <= np; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int a = tid; a < np; a += blockDim.x) {
+                const int b = a ^ j;
+                if (b > a) {
+                    const unsigned long long ka = s_key[a], kb = s_key[b];
+                    if ((ka > kb) == ((a & k) == 0)) {
+                        s_key[a] = kb;
+                        s_key[b] = ka;
+                    }
+                }
             }
-            if (tid == 0) s_red = f2o(3.0e38f);
             __syncthreads();
-            float m = 3.0e38f;
-            for (int k = tid; k < n; k += blockDim.x)
-                if (s_hi[k] >= T && s_qt[k] - gd < T) m = fminf(m, s_qt[k] - gd);
-            if (m < 3.0e38f) atomicMin(&s_red, f2o(m));
-            __syncthreads();
-            const float mt = o2f(s_red);
-            __syncthreads();
-            if (!(mt < T)) break;
-            T = mt;
         }
+    }
+}
+
+// Fold, in warp 0, the nk triangles whose keys are sorted in s_key (the low
+// word indexes hiv / tri) in KD order, 32 at a time: every lane folds its own
+// triangle from the running height; the first lane that lifts gives the next
+// running height (the triangles before it did not lift from there, so the
+// sequential fold passes them by).  A triangle that does not lift from a
+// height does not lift from any higher one, so for the plain cutters only
+// the later lanes that lifted fold again; a composite sub-cutter's facet can
+// turn from a hidden contact to a lifting one as the height rises, so there
+// every later lane does.
+template <bool COMP>
+__device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsigned long long* s_key, int nk,
+                                           const float* hiv, const uint32_t* tri, float cxl, float cyl, int& capped,
+                                           unsigned& evals) {
+    const int lane = threadIdx.x & 31;
+    const float gd = ctx.guard;
+    for (int q0 = 0; q0 < nk; q0 += 32) {
+        const int q = q0 + lane;
+        const uint32_t slot = q < nk ? (uint32_t)s_key[q] : 0u;
+        const float h = q < nk ? hiv[slot] : NEG_INF32;
+        const uint32_t tr = q < nk ? tri[slot] : 0u;
+        bool pend = q < nk;
+        while (true) {
+            const bool go = pend && h + gd >= __double2float_rd(cl.z - ctx.g.oz);
+            if (!__any_sync(0xffffffffu, go)) break;
+            CL64 mine = cl;
+            if (go) {
+                fold_one(ctx, mine, tr, cxl, cyl, capped);
+                ++evals;
+            }
+            const bool lifted = go && mine.z > cl.z;
+            const unsigned L = __ballot_sync(0xffffffffu, lifted);
+            if (!L) break;
+            const int b = __ffs(L) - 1;
+            cl.z = __shfl_sync(0xffffffffu, mine.z, b);
+            cl.cc.x = __shfl_sync(0xffffffffu, mine.cc.x, b);
+            cl.cc.y = __shfl_sync(0xffffffffu, mine.cc.y, b);
+            cl.cc.z = __shfl_sync(0xffffffffu, mine.cc.z, b);
+            cl.type = __shfl_sync(0xffffffffu, mine.type, b);
+            pend = go && lane > b && (COMP || lifted);
+        }
+    }
+}
+
+// One handed-back point, by the whole block.
+template <bool COMP>
+__device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
+                                            const ExactGlobal& G, uint32_t* __restrict__ list2,
+                                            unsigned long long* __restrict__ nlist2) {
+    unsigned long long* s_key = S.key;
+    int& s_red = *S.red;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const GridP& g = ctx.g;
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
+    const float z0l = __double2float_rd(z0 - g.oz);
+    const int n = exact_gather<COMP>(ctx, x, y, cx, cy, z0l, S.hlb, *S.n, s_key, S.tri, S.hi, S.qt, EXACT_CAP);
+    CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
+    int capped = 0;
+    unsigned evals = 0;
+    if (n <= EXACT_CAP) {
+        const float T = exact_threshold(ctx, i, S.hi, S.qt, n, s_red);
         if (tid == 0) s_red = 0;
         __syncthreads();
-        {
-            int kept = 0;
-            for (int k = tid; k < n; k += blockDim.x) {
-                if (s_hi[k] >= T) ++kept;
-                else s_key[k] = ~0ull;  // sorts after the kept keys
-            }
-            if (kept) atomicAdd(&s_red, kept);
+        int kept = 0;
+        for (int k = tid; k < n; k += blockDim.x) {
+            if (S.hi[k] >= T) ++kept;
+            else s_key[k] = ~0ull;  // sorts after the kept keys
         }
+        if (kept) atomicAdd(&s_red, kept);
         __syncthreads();
         const int nk = s_red;
-        // bitonic sort of the keys (padded to a power of two)
-        int np = 1;
-        while (np < n) np <<= 1;
-        for (int k = n + tid; k < np; k += blockDim.x) s_key[k] = ~0ull;
+        exact_sort(s_key, n);
+        if (tid < 32) exact_fold<COMP>(ctx, cl, s_key, nk, S.hi, S.tri, cx, cy, capped, evals);
+    } else if (G.key && n <= G.cap) {
+        // More candidates than shared memory holds: gathered again into this
+        // block's global scratch and folded in KD order one rank window at a
+        // time (each window's ranks chosen so it fits shared memory), the
+        // running height carried from window to window.
+        const size_t base = (size_t)blockIdx.x * (size_t)G.cap;
+        unsigned long long* gk = G.key + base;
+        uint32_t* gt = G.tri + base;
+        float* gh = G.hi + base;
+        float* gq = G.qt + base;
+        exact_gather<COMP>(ctx, x, y, cx, cy, z0l, S.hlb, *S.n, gk, gt, gh, gq, G.cap);
+        const float T = exact_threshold(ctx, i, gh, gq, n, s_red);
+        constexpr unsigned long long DROPPED = 0xFFFFFFFF00000000ull;
+        for (int k = tid; k < n; k += blockDim.x)
+            if (!(gh[k] >= T)) gk[k] = DROPPED | (unsigned)k;
         __syncthreads();
-        for (int k = 2; k <= np; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int a = tid; a < np; a += blockDim.x) {
-                    const int b = a ^ j;
-                    if (b > a) {
-                        const unsigned long long ka = s_key[a], kb = s_key[b];
-                        if ((ka > kb) == ((a & k) == 0)) {
-                            s_key[a] = kb;
-                            s_key[b] = ka;
+        int* hist = reinterpret_cast<int*>(S.qt);  // the shared thresholds are not used on this path
+        uint64_t cur = 0;
+        for (;;) {
+            // kept entries with rank >= cur: how many, and the largest rank
+            if (tid == 0) {
+                s_red = 0;
+                hist[0] = -1;
+            }
+            __syncthreads();
+            int cnt = 0, rmax = -1;
+            for (int k = tid; k < n; k += blockDim.x) {
+                const uint32_t r = (uint32_t)(gk[k] >> 32);
+                if (r != 0xFFFFFFFFu && r >= cur) {
+                    ++cnt;
+                    rmax = max(rmax, (int)r);
+                }
+            }
+            if (cnt) {
+                atomicAdd(&s_red, cnt);
+                atomicMax(&hist[0], rmax);
+            }
+            __syncthreads();
+            const int total = s_red;
+            uint64_t hi = (uint64_t)hist[0] + 1;
+            __syncthreads();
+            if (total == 0) break;
+            if (total > EXACT_CAP) {
+                // the longest run of histogram bins from `cur` holding at most EXACT_CAP
+                for (;;) {
+                    const uint64_t w = (hi - cur + EXACT_BINS - 1) / EXACT_BINS;
+                    for (int b = tid; b < EXACT_BINS; b += blockDim.x) hist[b] = 0;
+                    __syncthreads();
+                    for (int k = tid; k < n; k += blockDim.x) {
+                        const uint64_t r = gk[k] >> 32;
+                        if (r != 0xFFFFFFFFull && r >= cur && r < hi) atomicAdd(&hist[(r - cur) / w], 1);
+                    }
+                    __syncthreads();
+                    if (tid == 0) {
+                        int acc = 0, j = -1;
+                        for (int b = 0; b < EXACT_BINS; ++b) {
+                            if (acc + hist[b] > EXACT_CAP) break;
+                            acc += hist[b];
+                            j = b;
                         }
+                        s_red = j;
                     }
-                }
-                __syncthreads();
-            }
-        }
-        // fold in KD order (warp 0), 32 triangles at a time: every lane folds
-        // its own triangle from the running height; the first lane that lifts
-        // gives the next running height (the triangles before it did not lift
-        // from there, so the sequential fold passes them by).  A triangle that
-        // does not lift from a height does not lift from any higher one, so
-        // for the plain cutters only the later lanes that lifted fold again;
-        // a composite sub-cutter's facet can turn from a hidden contact to a
-        // lifting one as the height rises, so there every later lane does.
-        if (tid < 32) {
-            CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
-            int capped = 0;
-            unsigned evals = 0;
-            const float cxl = cx, cyl = cy;
-            for (int q0 = 0; q0 < nk; q0 += 32) {
-                const int q = q0 + lane;
-                const uint32_t slot = q < nk ? (uint32_t)s_key[q] : 0u;
-                const float h = q < nk ? s_hi[slot] : NEG_INF32;
-                const uint32_t tr = q < nk ? s_tri[slot] : 0u;
-                bool pend = q < nk;
-                while (true) {
-                    const bool go = pend && h + gd >= __double2float_rd(cl.z - g.oz);
-                    if (!__any_sync(0xffffffffu, go)) break;
-                    CL64 mine = cl;
-                    if (go) {
-                        fold_one(ctx, mine, tr, cxl, cyl, capped);
-                        ++evals;
+                    __syncthreads();
+                    const int j = s_red;
+                    __syncthreads();
+                    if (j >= 0) {
+                        hi = min(hi, cur + (uint64_t)(j + 1) * w);
+                        break;
                     }
-                    const bool lifted = go && mine.z > cl.z;
-                    const unsigned L = __ballot_sync(0xffffffffu, lifted);
-                    if (!L) break;
-                    const int b = __ffs(L) - 1;
-                    cl.z = __shfl_sync(0xffffffffu, mine.z, b);
-                    cl.cc.x = __shfl_sync(0xffffffffu, mine.cc.x, b);
-                    cl.cc.y = __shfl_sync(0xffffffffu, mine.cc.y, b);
-                    cl.cc.z = __shfl_sync(0xffffffffu, mine.cc.z, b);
-                    cl.type = __shfl_sync(0xffffffffu, mine.type, b);
-                    pend = go && lane > b && (COMP || lifted);
+                    hi = cur + w;  // the first bin alone is too full (w > 1: ranks are distinct)
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                evals += __shfl_xor_sync(0xffffffffu, evals, o);
-                capped += __shfl_xor_sync(0xffffffffu, capped, o);
+            // the window's keys into shared memory, sorted, folded
+            if (tid == 0) s_red = 0;
+            __syncthreads();
+            for (int k = tid; k < n; k += blockDim.x) {
+                const uint64_t r = gk[k] >> 32;
+                if (r != 0xFFFFFFFFull && r >= cur && r < hi) {
+                    const int slot = atomicAdd(&s_red, 1);
+                    s_key[slot] = (r << 32) | (unsigned)k;
+                }
             }
-            if (lane == 0) {
-                const uint32_t o = ctx.perm[i];
-                ctx.out_z[o] = cl.z;
-                ctx.out_cc[3 * o] = cl.cc.x;
-                ctx.out_cc[3 * o + 1] = cl.cc.y;
-                ctx.out_cc[3 * o + 2] = cl.cc.z;
-                ctx.out_type[o] = cl.type;
-                if (evals) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)evals);
-                if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
-            }
+            __syncthreads();
+            const int nw = s_red;
+            exact_sort(s_key, nw);
+            if (tid < 32) exact_fold<COMP>(ctx, cl, s_key, nw, gh, gt, cx, cy, capped, evals);
+            __syncthreads();
+            cur = hi;
         }
+    } else {
+        if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
         __syncthreads();
+        return;
     }
+    if (tid < 32) {
+        for (int o = 16; o > 0; o >>= 1) {
+            evals += __shfl_xor_sync(0xffffffffu, evals, o);
+            capped += __shfl_xor_sync(0xffffffffu, capped, o);
+        }
+        if (lane == 0) {
+            const uint32_t o = ctx.perm[i];
+            ctx.out_z[o] = cl.z;
+            ctx.out_cc[3 * o] = cl.cc.x;
+            ctx.out_cc[3 * o + 1] = cl.cc.y;
+            ctx.out_cc[3 * o + 2] = cl.cc.z;
+            ctx.out_type[o] = cl.type;
+            if (evals) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)evals);
+            if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
+        }
+    }
+    __syncthreads();
 }
 
 #define OCLG_EXACT_SHARED                                                                    \
@@ -796,16 +927,18 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_const
                                                               const uint32_t* __restrict__ list,
                                                               const unsigned long long* __restrict__ nlist_dev,
                                                               uint32_t* __restrict__ list2,
-                                                              unsigned long long* __restrict__ nlist2) {
+                                                              unsigned long long* __restrict__ nlist2,
+                                                              const ExactGlobal G) {
     OCLG_EXACT_SHARED
     for (int k = threadIdx.x; k < HLB_N; k += blockDim.x) s_hlb[k] = ctx.hlb[k];
     const int nlist = (int)*nlist_dev;
-    for (int p = blockIdx.x; p < nlist; p += gridDim.x) exact_point<COMP>(ctx, list[p], S, list2, nlist2);
+    for (int p = blockIdx.x; p < nlist; p += gridDim.x) exact_point<COMP>(ctx, list[p], S, G, list2, nlist2);
 }
 
 // Batch: every block strides over the handed-back points of each job in turn.
 template <bool COMP>
-__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact_b(const __grid_constant__ BatchView bv) {
+__global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact_b(const __grid_constant__ BatchView bv,
+                                                                const ExactGlobal G) {
     OCLG_EXACT_SHARED
     for (unsigned k = 0; k < bv.njobs; ++k) {
         const DropCtx& ctx = bv.ctxs[bv.jobs[k]];
@@ -814,7 +947,7 @@ __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact_b(const __grid_con
         __syncthreads();
         for (int q = threadIdx.x; q < HLB_N; q += blockDim.x) s_hlb[q] = ctx.hlb[q];
         for (int p = blockIdx.x; p < nlist; p += gridDim.x)
-            exact_point<COMP>(ctx, ctx.list[p], S, ctx.list2, ctx.counters + C_PLAIN);
+            exact_point<COMP>(ctx, ctx.list[p], S, G, ctx.list2, ctx.counters + C_PLAIN);
     }
 }
 #undef OCLG_EXACT_SHARED
@@ -912,6 +1045,7 @@ struct DropWork {
         return true;
     }
     DevBuf<uint8_t> sort_tmp;
+    DevBuf<unsigned char> exact_scratch;  // handed-back points with many candidates
     DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
     // per-call stage events, a ring over the last STAGE_RING calls (read
     // afterwards by ocl_gb300_stage_times without syncing the calls)
@@ -999,16 +1133,33 @@ int ensure_exact_smem() {
 }
 
 // k_drop_exact over the handed-back points (count on the device).
+// G.key == nullptr: no global scratch (points beyond EXACT_CAP candidates go
+// to the plain kernel).  With scratch the grid is at most EXACT_GBLOCKS (one
+// scratch region per block).
 static int launch_exact(const DropCtx& h, bool composite, const uint32_t* list, const unsigned long long* nlist,
-                        uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream) {
+                        uint32_t* list2, unsigned long long* nlist2, unsigned blocks, cudaStream_t stream,
+                        const ExactGlobal& G) {
     int st = ensure_exact_smem();
     if (st) return st;
     if (blocks == 0) blocks = 1;
+    if (G.key) blocks = std::min<unsigned>(blocks, (unsigned)EXACT_GBLOCKS);
     if (composite)
-        k_drop_exact<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2);
+        k_drop_exact<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2, G);
     else
-        k_drop_exact<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2);
+        k_drop_exact<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(h, list, nlist, list2, nlist2, G);
     return OCL_GB300_OK;
+}
+
+// The exact kernel's global scratch carved from one byte buffer of EXACT_GBYTES.
+static ExactGlobal exact_global_in(unsigned char* p) {
+    ExactGlobal G;
+    const size_t n = (size_t)EXACT_GBLOCKS * EXACT_GCAP;
+    G.key = reinterpret_cast<unsigned long long*>(p);
+    G.tri = reinterpret_cast<uint32_t*>(p + n * 8);
+    G.hi = reinterpret_cast<float*>(p + n * 12);
+    G.qt = reinterpret_cast<float*>(p + n * 16);
+    G.cap = EXACT_GCAP;
+    return G;
 }
 
 void init_drop_ctx(const Mesh& m, const CutterP& cp, DropCtx& h) {
@@ -1123,8 +1274,10 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         CK(cudaEventRecord(ev[3], stream));
         k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
         // the fallback grids stride over however many points were handed back
+        if (!w.exact_scratch.reserve(EXACT_GBYTES)) return OCL_GB300_OOM;
         st = launch_exact(*h, composite, w.list.p, w.counters.p + C_FALLBACK, w.list2.p, w.counters.p + C_PLAIN,
-                          (unsigned)std::min<uint64_t>(M, 152u * 3u), stream);
+                          (unsigned)std::min<uint64_t>(M, (uint64_t)EXACT_GBLOCKS), stream,
+                          exact_global_in(w.exact_scratch.p));
         if (st) return st;
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
         k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list2.p, w.counters.p + C_PLAIN);
@@ -1202,13 +1355,18 @@ void batch_launch_collect(const BatchView& bv, unsigned blocks, cudaStream_t str
     k_collect_overflow_b<<<blocks, TILE_POINTS, 0, stream>>>(bv);
 }
 
-int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream) {
+int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream,
+                       unsigned char* scratch) {
     int st = ensure_exact_smem();
     if (st) return st;
-    if (composite) k_drop_exact_b<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv);
-    else k_drop_exact_b<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv);
+    const ExactGlobal G = scratch ? exact_global_in(scratch) : ExactGlobal{};
+    if (G.key) blocks = std::min<unsigned>(blocks, (unsigned)EXACT_GBLOCKS);
+    if (composite) k_drop_exact_b<true><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv, G);
+    else k_drop_exact_b<false><<<blocks, EXACT_THREADS, EXACT_SMEM, stream>>>(bv, G);
     return OCL_GB300_OK;
 }
+
+size_t batch_exact_scratch_bytes() { return EXACT_GBYTES; }
 
 void batch_launch_plain(const BatchView& bv, unsigned blocks, cudaStream_t stream) {
     k_drop_kd_b<<<blocks, 128, 0, stream>>>(bv);
@@ -1340,7 +1498,7 @@ int drop_run_noalloc(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M,
         k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
         k_collect_overflow<<<nb, TB, 0, stream>>>(sc->ncand, (int)M, sc->list, sc->counters + C_FALLBACK);
         st = launch_exact(h, composite, sc->list, sc->counters + C_FALLBACK, sc->list2, sc->counters + C_PLAIN,
-                          (unsigned)std::min<uint64_t>(M, 152u * 3u), stream);
+                          (unsigned)std::min<uint64_t>(M, 152u * 3u), stream, ExactGlobal{});
         if (st) return st;
         const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
         k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(h, sc->list2, sc->counters + C_PLAIN);

@@ -111,7 +111,10 @@ size_t batch_sort_bytes(uint64_t Mtot, int end_bit);
 void batch_launch_bull(const BatchView& plan, const BatchView& eval, unsigned blocks, cudaStream_t stream);
 void batch_launch_refine(const BatchView& bv, bool bull_plan, unsigned blocks, cudaStream_t stream);
 void batch_launch_collect(const BatchView& bv, unsigned blocks, cudaStream_t stream);
-int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream);
+// scratch: the exact kernel's global scratch (batch_exact_scratch_bytes(); null: none)
+int batch_launch_exact(const BatchView& bv, bool composite, unsigned blocks, cudaStream_t stream,
+                       unsigned char* scratch);
+size_t batch_exact_scratch_bytes();
 void batch_launch_plain(const BatchView& bv, unsigned blocks, cudaStream_t stream);
 // Opt the exact kernels into their dynamic shared memory in the current context.
 int ensure_exact_smem();

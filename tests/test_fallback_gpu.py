@@ -72,11 +72,27 @@ def test_exact_kernel_matches_oracle(ocl, oracle_lib, name):
     _same((z, cc, ty), (z64, cc64, ty64))
 
 
-def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
-    # 160 x 160 cells over 12 mm: ~10,000 triangles under a 6 mm cutter,
-    # more than the exact kernel holds
+@pytest.mark.parametrize("name", ["cyl", "cylcone", "bull"])
+def test_exact_kernel_windows_over_large_lists(ocl, oracle_lib, name):
+    # 160 x 160 cells over 12 mm: ~10,000 triangles under a 6 mm cutter, more
+    # than the exact kernel's shared memory holds: gathered into its global
+    # scratch and folded in KD order one rank window at a time
     tris = flat_plate(161)
     cl = points(64, 6)
+    c = CASES[name][1]()
+    mesh = ocl.DeviceMesh(tris)
+    z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+    assert st.fallback > 0 and st.plain_points == 0
+    assert st.violations == 0
+    _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
+    _same((z, cc, ty), mesh.drop(c, cl, precision="fp64")[:3])
+
+
+def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
+    # 512 x 512 cells over 12 mm: ~100,000 triangles under a 6 mm cutter,
+    # more than the exact kernel's global scratch holds
+    tris = flat_plate(513)
+    cl = points(16, 6)
     c = cu.CylCutter(6.0, 20.0)
     mesh = ocl.DeviceMesh(tris)
     z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
