@@ -565,7 +565,7 @@ int prepare(Batch& b, cudaStream_t stream) {
 }
 
 // Candidate-list capacity and screen grid size per variant, timed on a
-// probe: the first 4,096 points of up to 32 chunks of the variant, each
+// probe: the middle 4,096 points of up to 32 chunks of the variant, each
 // configuration run twice (the second run timed).
 int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
     const int caps[3] = {64, 128, 256};
@@ -581,11 +581,16 @@ int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
         Batch probe;
         probe.budget = b.budget;
         probe.chunk = b.chunk;
-        // the first 4,096 points of at most 32 chunks of the variant
+        // the middle 4,096 points of at most 32 chunks of the variant
         for (const SubJob& s : all)
             if (s.v == v && probe.subs.size() < 32) {
                 SubJob q = s;
                 q.M = std::min<uint64_t>(q.M, 4096);
+                const uint64_t off = (s.M - q.M) / 2;
+                q.d_cl += 3 * off;
+                q.d_z += off;
+                q.d_cc += 3 * off;
+                q.d_type += off;
                 probe.subs.push_back(q);
             }
         float best = 1e30f;
