@@ -607,7 +607,7 @@ struct ExactGlobal {
     float* qt;
     int cap;
 };
-constexpr int EXACT_GCAP = 1 << 16;       // candidates per point the global scratch holds
+constexpr int EXACT_GCAP = 1 << 18;       // candidates per point the global scratch holds
 constexpr int EXACT_GBLOCKS = 152 * 2;    // exact-kernel blocks (two resident per SM)
 constexpr size_t EXACT_GBYTES = (size_t)EXACT_GBLOCKS * EXACT_GCAP * (8 + 4 + 4 + 4);
 constexpr int EXACT_BINS = 1024;          // rank histogram of the large path's windows

@@ -89,9 +89,9 @@ def test_exact_kernel_windows_over_large_lists(ocl, oracle_lib, name):
 
 
 def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
-    # 512 x 512 cells over 12 mm: ~100,000 triangles under a 6 mm cutter,
+    # 1024 x 1024 cells over 12 mm: ~400,000 triangles under a 6 mm cutter,
     # more than the exact kernel's global scratch holds
-    tris = flat_plate(513)
+    tris = flat_plate(1025)
     cl = points(16, 6)
     c = cu.CylCutter(6.0, 20.0)
     mesh = ocl.DeviceMesh(tris)
