@@ -2,7 +2,9 @@
 
 `port` is _build/liboclport.so (the C restatement in ocl_oracle.c, built on
 every machine); `ref` is _ref/liboclref.so (the reference's own sources,
-built only where the reference tree is present).  Only tests/,
+built only where the reference tree is present); `binding` is
+_ref/libgb300binding.so (opencamlib_gb300/integration's reference-side
+binding compiled against the reference's headers, same condition).  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module.
 """
 from __future__ import annotations
@@ -18,6 +20,7 @@ from opencamlib_gb300 import _abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboclport.so")
 REF_SO = os.path.join(HERE, "_ref", "liboclref.so")
+BINDING_SO = os.path.join(HERE, "_ref", "libgb300binding.so")
 
 _libs = {}
 
@@ -28,15 +31,46 @@ _i64p = C.POINTER(C.c_int64)
 
 
 def build(ref: bool = True, quiet: bool = True) -> None:
-    """make port (and ref when the reference tree exists)."""
+    """make port (and ref, plus the binding once the GB300 library is built,
+    when the reference tree exists)."""
     targets = ["port"] + (["ref"] if ref else [])
+    if ref and os.path.exists(os.path.join(HERE, "..", "opencamlib_gb300", "_build", "libocl_gb300.so")):
+        targets.append("binding")
     out = subprocess.run(["make", "-s", "-j8", *targets], cwd=HERE, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
 
 
 def available(which: str) -> bool:
-    return os.path.exists(PORT_SO if which == "port" else REF_SO)
+    return os.path.exists({"port": PORT_SO, "ref": REF_SO, "binding": BINDING_SO}[which])
+
+
+def binding_cutter(kind: int, args):
+    """A reference cutter object (kind 1-4: Cyl, Ball, Bull, Cone; 11-16: the
+    composite presets) through the reference-side binding: (status, the
+    binding's descriptor, the object's own fields in cutter_fields' layout)."""
+    L = _libs.get("binding")
+    if L is None:
+        L = C.CDLL(BINDING_SO)
+        L.binding_cutter.argtypes = [C.c_int, _dp, C.POINTER(_abi.CutterDesc), _dp]
+        L.binding_cutter.restype = C.c_int
+        L.binding_drop.argtypes = [_dp]
+        L.binding_drop.restype = C.c_int
+        _libs["binding"] = L
+    a = _d(list(args) + [0.0] * (4 - len(args)))
+    desc = _abi.CutterDesc()
+    out = np.zeros(4 + 9 * _abi.MAX_SUB)
+    st = L.binding_cutter(kind, _ptr(a), C.byref(desc), _ptr(out))
+    return st, desc, out
+
+
+def binding_drop():
+    """The binding's mesh_create + batch_drop on a two-triangle STLSurf:
+    (status, lifted z of one CL point)."""
+    binding_cutter(1, (1.0, 1.0))  # loads the library
+    z = C.c_double(0.0)
+    st = _libs["binding"].binding_drop(C.byref(z))
+    return st, z.value
 
 
 def _lib(which: str):
@@ -244,9 +278,13 @@ def edge_contact(cutter, x, y, p1, p2):
 
 
 def cutter_fields(cutter):
+    """The oracle's derived cutter fields for a cutter object or a raw
+    descriptor (radius, length, diameter, nsub; then per sub-cutter, or for
+    a basic cutter once: diameter, radius, length, center_height,
+    xy_normal_length, normal_length, radiusvec, heightvec, zoffset)."""
     L = _lib("port")
     out = np.zeros(4 + 9 * _abi.MAX_SUB)
-    desc = cutter.desc()
+    desc = cutter if isinstance(cutter, _abi.CutterDesc) else cutter.desc()
     if L.oracle_cutter_fields(C.byref(desc), _ptr(out)) != 0:
         raise RuntimeError("bad cutter")
     return out

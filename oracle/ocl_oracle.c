@@ -1880,6 +1880,10 @@ int oracle_cutter_fields(const ocl_gb300_cutter* cd, double* out) {
     Cutter c;
     if (cutter_make(&c, cd) != 0) return -1;
     out[0] = c.radius; out[1] = c.length; out[2] = c.diameter; out[3] = c.nsub;
+    if (c.nsub == 0) {  /* a basic cutter: its own derived fields */
+        out[4] = c.diameter; out[5] = c.radius; out[6] = c.length; out[7] = c.center_height;
+        out[8] = c.xy_normal_length; out[9] = c.normal_length;
+    }
     for (int n = 0; n < c.nsub; ++n) {
         double* o = out + 4 + 9 * n;
         const Cutter* s = &c.sub[n];
