@@ -152,51 +152,51 @@ def cpu_baseline(tris, cl, sample, nthreads=0):
 
 def aux_measurements(cl_mesh, cuts, with_cpu):
     """The other operations on the path, measured beside the headline:
-    BatchPushCutter on a waterline-like fiber set (sphere-on-plate + torus,
-    499,202 triangles; 10 z levels x 2,000 X- and 2,000 Y-fibers, extent the
-    mesh bbox +- 2 radii) and PathDropCutter / AdaptivePathDropCutter on a
-    zig-zag of 100 line spans across the 1,048,576-triangle mesh.  Device time
-    from the library's CUDA events; the CPU figures are the oracle port on
-    every 50th fiber / every 10th span (OpenMP on all host cores)."""
-    import ctypes as C
-    from opencamlib_gb300 import _abi, _native, cutters as cu, workloads as w
+    Waterline at the waterline workload's full size (sphere-on-plate + torus,
+    499,202 triangles; 50 heights z = 1..49 mm; X and Y fibers over the mesh
+    bbox +- 2 cutter radii at 0.056 mm, 2,001 per direction per height, so
+    200,100 fibers per cutter; one ocl_gb300_waterline_levels call: both
+    fiber directions pushed on the device, the 50 levels woven on host
+    threads) and PathDropCutter / AdaptivePathDropCutter on a zig-zag of 100
+    line spans across the 1,048,576-triangle mesh.  Device time from the
+    library's CUDA events; the CPU figures are the oracle port's push on
+    every 50th fiber of every 5th level / every 10th span (OpenMP on all
+    host cores)."""
+    from opencamlib_gb300 import _native, cutters as cu, workloads as w
     out = {}
-    L = _native.lib()
     tris = w.sphere_torus(1)
     mesh = _native.DeviceMesh(tris)
-    push = {}
+    zs = np.linspace(1.0, 49.0, 50)
+    wl = {}
     for name, c in (("ball", cu.BallCutter(6.0, 20.0)), ("bull", cu.BullCutter(6.0, 1.0, 20.0))):
-        r = c.radius
-        tot_ms, tot_f, cpu_s, cpu_f = 0.0, 0, 0.0, 0
-        for d in (0, 1):
-            fib = np.ascontiguousarray(np.concatenate(
-                [w.fibers(d, 1.0 + 48.0 * k / 49.0, 0.0, 100.0, 2000, -2 * r, 100.0 + 2 * r) for k in range(0, 50, 5)]))
-            F = fib.shape[0]
-            offsets = np.zeros(F + 1, dtype=np.uint64)
-            cap = 8 * F
-            iv, cc, ty = np.empty(2 * cap), np.empty(6 * cap), np.empty(2 * cap, dtype=np.int32)
-            desc = c.desc()
-            st = _abi.Stats()
-            for _ in range(2):
-                s = L.ocl_gb300_push(mesh.handle, C.byref(desc), d, fib.ctypes.data_as(C.POINTER(C.c_double)), F,
-                                     offsets.ctypes.data_as(C.POINTER(C.c_uint64)),
-                                     iv.ctypes.data_as(C.POINTER(C.c_double)), cc.ctypes.data_as(C.POINTER(C.c_double)),
-                                     ty.ctypes.data_as(C.POINTER(C.c_int32)), cap, C.byref(st))
-                if s != 0:
-                    raise RuntimeError(L.ocl_gb300_last_error().decode())
-            tot_ms += st.kernel_ms
-            tot_f += F
-            if with_cpu:
-                from oracle import checker
-                sub = fib[::50]
-                t0 = time.perf_counter()
-                checker.push(tris, c, d, sub, "port")
-                cpu_s += time.perf_counter() - t0
-                cpu_f += len(sub)
-        push[name] = {"fibers": tot_f, "gpu_ms": tot_ms, "gpu_fibers_per_s": tot_f / (tot_ms / 1e3),
-                      "cpu_fibers_per_s": (cpu_f / cpu_s) if cpu_s else None,
-                      "cpu_sample": f"{cpu_f} fibers (every 50th), KD build included"}
-    out["push"] = push
+        bb = tris.reshape(-1, 3)
+        extent = float(bb[:, 0].max() - bb[:, 0].min()) + 4 * c.radius
+        sampling = extent / 2000.0
+        mesh.waterline_levels(c, zs[:1], sampling)  # builds the push indexes
+        t0 = time.perf_counter()
+        levels, st = mesh.waterline_levels(c, zs, sampling)
+        wall = time.perf_counter() - t0
+        nfib = sum(len(lv.fibers(d)[0]) for lv in levels for d in (0, 1))
+        nint = sum(len(lv.fibers(d)[2]) for lv in levels for d in (0, 1))
+        rec = {"levels": len(zs), "sampling_mm": sampling, "fibers": nfib, "intervals": nint,
+               "loops": sum(len(lv.loops) for lv in levels),
+               "loop_points": int(sum(len(lp) for lv in levels for lp in lv.loops)),
+               "wall_ms": wall * 1e3, "push_device_ms": st.kernel_ms, "weave_and_host_ms": wall * 1e3 - st.kernel_ms,
+               "fibers_per_s": nfib / wall, "push_fibers_per_s": nfib / (st.kernel_ms / 1e3),
+               "pairs": int(st.pairs)}
+        if with_cpu:
+            from oracle import checker
+            sub = [lv.fibers(d)[0][::50] for lv in levels[::5] for d in (0, 1)]
+            t0 = time.perf_counter()
+            nsub = 0
+            for k, fb in enumerate(sub):
+                checker.push(tris, c, k % 2, fb, "port")
+                nsub += len(fb)
+            cpu_s = time.perf_counter() - t0
+            rec["cpu_push_fibers_per_s"] = nsub / cpu_s
+            rec["cpu_sample"] = f"{nsub} fibers (every 50th of every 5th level), oracle port push, KD build included"
+        wl[name] = rec
+    out["waterline"] = wl
     mesh.release()
     # paths: zig-zag of 100 lines across the bump mesh
     m2 = _native.DeviceMesh(cl_mesh)

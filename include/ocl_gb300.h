@@ -338,6 +338,60 @@ int ocl_gb300_adaptive_path_drop(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cu
                                  double* xyz, double* cc, int32_t* type, uint64_t cap,
                                  uint64_t* count, ocl_gb300_stats* stats);
 
+/* ---- waterline ------------------------------------------------------------ */
+/* Waterline loops at one height, kept in a handle until released: the loop
+ * points and the X and Y fibers woven (Waterline::getLoops / getXFibers /
+ * getYFibers, src/algo/waterline.hpp:59-63, src/pythonlib/ocl_algo.cpp:105-119).
+ * Each loop is a cyclic sequence of CL points, as the reference's
+ * Weave::face_traverse walks it (src/algo/weave.cpp:49-73); loops are listed
+ * by their first interval end (X intervals first, in fiber and interval
+ * order, lower end first; then Y intervals), and each starts there. */
+typedef struct ocl_gb300_loops_s* ocl_gb300_loops;
+
+/* Waterline::run (src/algo/waterline.cpp:78-87): X and Y fibers at height z
+ * over the mesh bbox grown by two cutter radii, sampling apart
+ * (init_fibers, :143-178), pushed on the device (BatchPushCutter), woven on
+ * the host (SimpleWeave::build + face_traverse; run2's SmartWeave gives the
+ * same loops). */
+int ocl_gb300_waterline(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, double z, double sampling,
+                        ocl_gb300_loops* out, ocl_gb300_stats* stats);
+
+/* Waterline::run at nz heights in one device pass per fiber direction (the
+ * levels' fibers pushed together, the levels woven in parallel on host
+ * threads); out[k] receives the loops at zs[k]. */
+int ocl_gb300_waterline_levels(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* zs, uint64_t nz,
+                               double sampling, ocl_gb300_loops* out, ocl_gb300_stats* stats);
+
+/* AdaptiveWaterline::run (src/algo/adaptivewaterline.cpp:62-220): fibers
+ * bisected along the bbox diagonal while the step exceeds sampling, or the
+ * fibers are not flat (cos_limit) and the step exceeds min_sampling; each
+ * bisection level's fibers are pushed in one device call per direction.
+ * The reference's defaults: min_sampling = sampling / 10, cos_limit 0.999. */
+int ocl_gb300_adaptive_waterline(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, double z, double sampling,
+                                 double min_sampling, double cos_limit, ocl_gb300_loops* out,
+                                 ocl_gb300_stats* stats);
+
+/* Weave::build + face_traverse on caller fibers (host code only): X fibers
+ * xfib (nx x 6, p1.y == p2.y, p1.z == p2.z), their intervals [xoff[f],
+ * xoff[f+1]) as t-values xival (2 per interval); Y fibers likewise.  The
+ * intervals of one fiber must not overlap (Fiber::addInterval merges
+ * overlapping ones). */
+int ocl_gb300_weave(const double* xfib, uint64_t nx, const uint64_t* xoff, const double* xival,
+                    const double* yfib, uint64_t ny, const uint64_t* yoff, const double* yival,
+                    ocl_gb300_loops* out);
+
+int ocl_gb300_loops_count(ocl_gb300_loops loops, uint64_t* nloops, uint64_t* npoints);
+/* points: npoints x 3; offsets: nloops + 1 (loop k is [offsets[k], offsets[k+1])) */
+int ocl_gb300_loops_get(ocl_gb300_loops loops, double* points, uint64_t* offsets);
+/* The fibers of one direction that were woven.  With fib == NULL only
+ * *nfibers and *nintervals are set; otherwise fib (nfibers x 6), offsets
+ * (nfibers + 1), ival (2 per interval), and, when not NULL, cc (6 per
+ * interval) and cctype (2 per interval) as ocl_gb300_push gives them (zero
+ * for fibers passed to ocl_gb300_weave). */
+int ocl_gb300_loops_fibers(ocl_gb300_loops loops, int dir, uint64_t* nfibers, uint64_t* nintervals, double* fib,
+                           uint64_t* offsets, double* ival, double* cc, int32_t* cctype);
+int ocl_gb300_loops_release(ocl_gb300_loops loops);
+
 /* ---- CL point filter ----------------------------------------------------- */
 /* LineCLFilter::run (src/common/lineclfilter.cpp:40-77) on n points xyz[3 n]:
  * keep[0 .. *nkeep) receives the indices of the points kept, in order (the

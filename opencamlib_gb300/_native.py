@@ -31,6 +31,8 @@ EXPORTS = [
     "ocl_gb300_batch_release", "ocl_gb300_server_create", "ocl_gb300_server_add_mesh",
     "ocl_gb300_server_submit_drop", "ocl_gb300_server_submit_adaptive", "ocl_gb300_server_wait",
     "ocl_gb300_server_cancel", "ocl_gb300_server_stats_get", "ocl_gb300_server_pause", "ocl_gb300_server_destroy",
+    "ocl_gb300_waterline", "ocl_gb300_waterline_levels", "ocl_gb300_adaptive_waterline", "ocl_gb300_weave",
+    "ocl_gb300_loops_count", "ocl_gb300_loops_get", "ocl_gb300_loops_fibers", "ocl_gb300_loops_release",
 ]
 
 _lib = None
@@ -90,6 +92,16 @@ def lib():
     L.ocl_gb300_server_stats_get.argtypes = [C.c_void_p, C.POINTER(_abi.ServerStats)]
     L.ocl_gb300_server_pause.argtypes = [C.c_void_p, C.c_int32]
     L.ocl_gb300_server_destroy.argtypes = [C.c_void_p]
+    vpp = C.POINTER(C.c_void_p)
+    L.ocl_gb300_waterline.argtypes = [C.c_void_p, cd, C.c_double, C.c_double, vpp, st]
+    L.ocl_gb300_waterline_levels.argtypes = [C.c_void_p, cd, _dp, C.c_uint64, C.c_double, vpp, st]
+    L.ocl_gb300_adaptive_waterline.argtypes = [C.c_void_p, cd, C.c_double, C.c_double, C.c_double, C.c_double, vpp,
+                                               st]
+    L.ocl_gb300_weave.argtypes = [_dp, C.c_uint64, _u64p, _dp, _dp, C.c_uint64, _u64p, _dp, vpp]
+    L.ocl_gb300_loops_count.argtypes = [C.c_void_p, _u64p, _u64p]
+    L.ocl_gb300_loops_get.argtypes = [C.c_void_p, _dp, _u64p]
+    L.ocl_gb300_loops_fibers.argtypes = [C.c_void_p, C.c_int, _u64p, _u64p, _dp, _u64p, _dp, _dp, _ip]
+    L.ocl_gb300_loops_release.argtypes = [C.c_void_p]
     L.ocl_gb300_last_error.restype = C.c_char_p
     L.ocl_gb300_version.restype = C.c_char_p
     _lib = L
@@ -137,6 +149,59 @@ def line_filter(xyz, tol: float) -> np.ndarray:
     nk = C.c_uint64(0)
     check(lib().ocl_gb300_line_filter(_p(a), len(a), float(tol), _p(keep, _u64p), C.byref(nk)))
     return keep[:nk.value].astype(np.int64)
+
+
+class Loops:
+    """Waterline loops at one height (an ocl_gb300_loops handle): `loops` is a
+    list of (n, 3) arrays of CL points, each a closed loop; `fibers(dir)` the
+    X (0) or Y (1) fibers woven: (endpoints (F, 6), interval offsets (F+1),
+    [lower, upper] t-values (K, 2), CC points (K, 2, 3), CC types (K, 2))."""
+
+    def __init__(self, handle):
+        self._h = handle
+        try:
+            n, npts = C.c_uint64(0), C.c_uint64(0)
+            check(lib().ocl_gb300_loops_count(handle, C.byref(n), C.byref(npts)))
+            pts = np.zeros((npts.value, 3))
+            off = np.zeros(n.value + 1, dtype=np.uint64)
+            check(lib().ocl_gb300_loops_get(handle, _p(pts), _p(off, _u64p)))
+            self.loops = [pts[int(off[k]):int(off[k + 1])].copy() for k in range(n.value)]
+            self._fibers = [_loops_fibers(handle, d) for d in (0, 1)]
+        finally:
+            lib().ocl_gb300_loops_release(handle)
+            self._h = None
+
+    def fibers(self, direction: int):
+        return self._fibers[direction]
+
+
+def _loops_fibers(handle, d):
+    nf, nk = C.c_uint64(0), C.c_uint64(0)
+    check(lib().ocl_gb300_loops_fibers(handle, d, C.byref(nf), C.byref(nk), None, None, None, None, None))
+    fib = np.zeros((nf.value, 6))
+    off = np.zeros(nf.value + 1, dtype=np.uint64)
+    iv = np.zeros((nk.value, 2))
+    cc = np.zeros((nk.value, 2, 3))
+    ty = np.zeros((nk.value, 2), dtype=np.int32)
+    check(lib().ocl_gb300_loops_fibers(handle, d, C.byref(nf), C.byref(nk), _p(fib), _p(off, _u64p), _p(iv), _p(cc),
+                                       _p(ty, _ip)))
+    return fib, off, iv, cc, ty
+
+
+def weave(xfibers, yfibers) -> "Loops":
+    """Weave::build + face_traverse (host code, no device) on X and Y fibers,
+    each given as (endpoints (F, 6), interval offsets (F+1), t-values (K, 2))."""
+    args = []
+    for fib, off, iv in (xfibers[:3], yfibers[:3]):
+        fib = _d(fib, 6)
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        iv = np.ascontiguousarray(iv, dtype=np.float64).reshape(-1)
+        args.append((fib, off, iv))
+    (xf, xo, xi), (yf, yo, yi) = args
+    h = C.c_void_p()
+    check(lib().ocl_gb300_weave(_p(xf), len(xf), _p(xo, _u64p), _p(xi) if xi.size else None, _p(yf), len(yf),
+                                _p(yo, _u64p), _p(yi) if yi.size else None, C.byref(h)))
+    return Loops(h)
 
 
 def fma_peaks() -> tuple:
@@ -257,6 +322,36 @@ class DeviceMesh:
                             int(ty[2 * k]), int(ty[2 * k + 1])))
             out.append(rec)
         return out, st
+
+    def waterline(self, cutter, z: float, sampling: float):
+        """Waterline::run at height z: a Loops (loops and the fibers woven)
+        and the Stats."""
+        st = _abi.Stats()
+        h = C.c_void_p()
+        check(lib().ocl_gb300_waterline(self._h, C.byref(cutter.desc()), float(z), float(sampling), C.byref(h),
+                                        C.byref(st)))
+        return Loops(h), st
+
+    def waterline_levels(self, cutter, zs, sampling: float):
+        """Waterline::run at every height in zs in one device pass per fiber
+        direction: a list of Loops and the Stats."""
+        z = np.ascontiguousarray(zs, dtype=np.float64).reshape(-1)
+        hs = (C.c_void_p * max(len(z), 1))()
+        st = _abi.Stats()
+        check(lib().ocl_gb300_waterline_levels(self._h, C.byref(cutter.desc()), _p(z), len(z), float(sampling),
+                                               C.cast(hs, C.POINTER(C.c_void_p)), C.byref(st)))
+        return [Loops(C.c_void_p(hs[k])) for k in range(len(z))], st
+
+    def adaptive_waterline(self, cutter, z: float, sampling: float, min_sampling: float = None,
+                           cos_limit: float = 0.999):
+        """AdaptiveWaterline::run at height z (min_sampling defaults to
+        sampling / 10, as setSampling sets it): a Loops and the Stats."""
+        ms = sampling / 10.0 if min_sampling is None else min_sampling
+        st = _abi.Stats()
+        h = C.c_void_p()
+        check(lib().ocl_gb300_adaptive_waterline(self._h, C.byref(cutter.desc()), float(z), float(sampling),
+                                                 float(ms), float(cos_limit), C.byref(h), C.byref(st)))
+        return Loops(h), st
 
     def path_drop(self, cutter, spans, sampling, min_z):
         spans = _d(spans, _abi.SPAN_DOUBLES)

@@ -15,7 +15,7 @@ from ._native import DeviceMesh, line_filter, stl_read
 
 __all__ = ["Point", "CCPoint", "CLPoint", "Triangle", "STLSurf", "STLReader", "Bbox", "Line", "Arc", "Path",
            "Interval", "Fiber", "BatchDropCutter", "PathDropCutter", "AdaptivePathDropCutter", "BatchPushCutter",
-           "LineCLFilter", "CCType"]
+           "LineCLFilter", "CCType", "Waterline", "AdaptiveWaterline"]
 
 
 class CCType:
@@ -532,3 +532,83 @@ class BatchPushCutter(_Operation):
                 out.append(f.lowerCLPoint(n))
                 out.append(f.upperCLPoint(n))
         return out
+
+
+class Waterline(_Operation):
+    """Waterline (src/algo/waterline.hpp:41-88, Python binding
+    src/pythonlib/ocl_algo.cpp:105-119): X and Y fibers at height z pushed on
+    the GPU, woven on the host.  getLoops() gives a list of loops, each a
+    list of Points; run2() gives the same loops as run()."""
+
+    def __init__(self):
+        super().__init__()
+        self.zh = 0.0
+        self.loops = []
+        self.xfibers = []
+        self.yfibers = []
+
+    def setZ(self, z):
+        self.zh = float(z)
+
+    def _weave(self):
+        return self._mesh().waterline(self.cutter, self.zh, self.sampling)
+
+    def run(self):
+        res, st = self._weave()
+        self.stats = st
+        self.nCalls = int(st.pairs)
+        self.loops = [[Point(*p) for p in lp] for lp in res.loops]
+        self.xfibers, self.yfibers = (self._fibers(res, d) for d in (0, 1))
+
+    def run2(self):
+        self.run()
+
+    @staticmethod
+    def _fibers(res, d):
+        fib, off, iv, cc, ty = res.fibers(d)
+        out = []
+        for f in range(len(fib)):
+            g = Fiber(Point(*fib[f, :3]), Point(*fib[f, 3:]))
+            for k in range(int(off[f]), int(off[f + 1])):
+                i = Interval(iv[k, 0], iv[k, 1])
+                i.lower_cc = CCPoint(cc[k, 0, 0], cc[k, 0, 1], cc[k, 0, 2], int(ty[k, 0]))
+                i.upper_cc = CCPoint(cc[k, 1, 0], cc[k, 1, 1], cc[k, 1, 2], int(ty[k, 1]))
+                g.ints.append(i)
+            out.append(g)
+        return out
+
+    def reset(self):
+        self.loops, self.xfibers, self.yfibers = [], [], []
+
+    def getLoops(self):
+        return self.loops
+
+    def getXFibers(self):
+        return self.xfibers
+
+    def getYFibers(self):
+        return self.yfibers
+
+
+class AdaptiveWaterline(Waterline):
+    """AdaptiveWaterline (src/algo/adaptivewaterline.hpp:38-92): fibers
+    bisected where the loops bend (setMinSampling, setCosLimit)."""
+
+    def __init__(self):
+        super().__init__()
+        self.sampling = 1.0
+        self.min_sampling = 0.1
+        self.cosLimit = 0.999
+
+    def setSampling(self, s):
+        self.sampling = float(s)
+        self.min_sampling = self.sampling / 10.0
+
+    def setMinSampling(self, s):
+        self.min_sampling = float(s)
+
+    def setCosLimit(self, c):
+        self.cosLimit = float(c)
+
+    def _weave(self):
+        return self._mesh().adaptive_waterline(self.cutter, self.zh, self.sampling, self.min_sampling, self.cosLimit)

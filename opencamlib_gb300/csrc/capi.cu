@@ -11,6 +11,7 @@
 #include "geom64.cuh"
 #include "mesh.cuh"
 #include "util.cuh"
+#include "waterline.cuh"
 
 namespace oclg {
 
@@ -610,6 +611,175 @@ int ocl_gb300_server_destroy(ocl_gb300_server server) {
     if (!server) return OCL_GB300_BAD_ARG;
     server_destroy(server->s);
     delete server;
+    return OCL_GB300_OK;
+}
+
+// ---- waterline -------------------------------------------------------------
+
+struct ocl_gb300_loops_s {
+    oclg::LoopSet s;
+};
+
+static int waterline_common(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, CutterP& cp) {
+    if (!mesh) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    return cutter_or_error(cutter, cp);
+}
+
+static void total_ms(ocl_gb300_stats* stats, std::chrono::steady_clock::time_point t0) {
+    if (stats)
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int ocl_gb300_waterline_levels(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, const double* zs, uint64_t nz,
+                               double sampling, ocl_gb300_loops* out, ocl_gb300_stats* stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!out || (nz > 0 && !zs)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    for (uint64_t k = 0; k < nz; ++k) out[k] = nullptr;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    CutterP cp;
+    int st = waterline_common(mesh, cutter, cp);
+    if (st) return st;
+    std::vector<oclg::LoopSet> sets;
+    {
+        std::lock_guard<std::mutex> lk(mesh->m->mu);
+        st = oclg::waterline_run(*mesh->m, cp, zs, nz, sampling, sets, stats);
+    }
+    if (st) return st;
+    for (uint64_t k = 0; k < nz; ++k) {
+        out[k] = new ocl_gb300_loops_s();
+        out[k]->s = std::move(sets[k]);
+    }
+    total_ms(stats, t0);
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_waterline(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, double z, double sampling,
+                        ocl_gb300_loops* out, ocl_gb300_stats* stats) {
+    return ocl_gb300_waterline_levels(mesh, cutter, &z, 1, sampling, out, stats);
+}
+
+int ocl_gb300_adaptive_waterline(ocl_gb300_mesh mesh, const ocl_gb300_cutter* cutter, double z, double sampling,
+                                 double min_sampling, double cos_limit, ocl_gb300_loops* out,
+                                 ocl_gb300_stats* stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!out) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    *out = nullptr;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    CutterP cp;
+    int st = waterline_common(mesh, cutter, cp);
+    if (st) return st;
+    auto* h = new ocl_gb300_loops_s();
+    {
+        std::lock_guard<std::mutex> lk(mesh->m->mu);
+        st = oclg::adaptive_waterline_run(*mesh->m, cp, z, sampling, min_sampling, cos_limit, h->s, stats);
+    }
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    total_ms(stats, t0);
+    return OCL_GB300_OK;
+}
+
+static int fibers_in(const double* fib, uint64_t F, const uint64_t* off, const double* iv, int dir,
+                     oclg::FiberSet& fs) {
+    if (F > 0 && (!fib || !off || (off[F] > 0 && !iv))) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    fs.fib.assign(fib, fib + 6 * F);
+    fs.off.assign(1, 0);
+    for (uint64_t f = 0; f < F; ++f) {
+        const double* p = fib + 6 * f;
+        const bool ok = dir == OCL_GB300_XFIBER ? (p[1] == p[4] && p[2] == p[5]) : (p[0] == p[3] && p[2] == p[5]);
+        if (!ok || off[f + 1] < off[f]) {
+            set_error("weave: fiber " + std::to_string(f) + " is not an axis-parallel fiber of its direction");
+            return OCL_GB300_BAD_ARG;
+        }
+        fs.off.push_back(off[f + 1] - off[0]);
+    }
+    const uint64_t K = F ? off[F] - off[0] : 0;
+    fs.ival.assign(iv ? iv + 2 * off[0] : iv, iv ? iv + 2 * (off[0] + K) : iv);
+    fs.cc.assign(6 * K, 0.0);
+    fs.type.assign(2 * K, 0);
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_weave(const double* xfib, uint64_t nx, const uint64_t* xoff, const double* xival, const double* yfib,
+                    uint64_t ny, const uint64_t* yoff, const double* yival, ocl_gb300_loops* out) {
+    if (!out) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    *out = nullptr;
+    auto* h = new ocl_gb300_loops_s();
+    int st = fibers_in(xfib, nx, xoff, xival, OCL_GB300_XFIBER, h->s.fibers[0]);
+    if (!st) st = fibers_in(yfib, ny, yoff, yival, OCL_GB300_YFIBER, h->s.fibers[1]);
+    if (!st) st = oclg::weave_loops(h->s);
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_loops_count(ocl_gb300_loops loops, uint64_t* nloops, uint64_t* npoints) {
+    if (!loops || !nloops || !npoints) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    *nloops = loops->s.off.empty() ? 0 : loops->s.off.size() - 1;
+    *npoints = loops->s.pts.size() / 3;
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_loops_get(ocl_gb300_loops loops, double* points, uint64_t* offsets) {
+    if (!loops || !offsets || (!points && !loops->s.pts.empty())) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (!loops->s.pts.empty()) std::memcpy(points, loops->s.pts.data(), loops->s.pts.size() * sizeof(double));
+    if (loops->s.off.empty()) offsets[0] = 0;
+    else std::memcpy(offsets, loops->s.off.data(), loops->s.off.size() * sizeof(uint64_t));
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_loops_fibers(ocl_gb300_loops loops, int dir, uint64_t* nfibers, uint64_t* nintervals, double* fib,
+                           uint64_t* offsets, double* ival, double* cc, int32_t* cctype) {
+    if (!loops || !nfibers || !nintervals || (dir != OCL_GB300_XFIBER && dir != OCL_GB300_YFIBER)) {
+        set_error("bad argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    const oclg::FiberSet& fs = loops->s.fibers[dir];
+    *nfibers = fs.count();
+    *nintervals = fs.ival.size() / 2;
+    if (!fib) return OCL_GB300_OK;
+    if (!offsets || (!ival && *nintervals)) {
+        set_error("null argument");
+        return OCL_GB300_BAD_ARG;
+    }
+    if (!fs.fib.empty()) std::memcpy(fib, fs.fib.data(), fs.fib.size() * sizeof(double));
+    if (fs.off.empty()) offsets[0] = 0;
+    else std::memcpy(offsets, fs.off.data(), fs.off.size() * sizeof(uint64_t));
+    if (!fs.ival.empty()) std::memcpy(ival, fs.ival.data(), fs.ival.size() * sizeof(double));
+    if (cc && !fs.cc.empty()) std::memcpy(cc, fs.cc.data(), fs.cc.size() * sizeof(double));
+    if (cctype && !fs.type.empty()) std::memcpy(cctype, fs.type.data(), fs.type.size() * sizeof(int32_t));
+    return OCL_GB300_OK;
+}
+
+int ocl_gb300_loops_release(ocl_gb300_loops loops) {
+    delete loops;
     return OCL_GB300_OK;
 }
 

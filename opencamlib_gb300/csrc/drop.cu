@@ -614,12 +614,13 @@ constexpr int EXACT_BINS = 1024;          // rank histogram of the large path's 
 
 // (Out of line: one copy serves the shared-memory and the global path.)
 // Gather every triangle whose certified FP32 upper bound lies above the start
-// height into (key, tri, hi, qt)[slot] for slot < cap (one thread per grid
-// cell under the cutter, all levels); returns the number found (may exceed cap).
+// height and reaches tcut into (key, tri, hi, qt)[slot] for slot < cap (one
+// thread per grid cell under the cutter, all levels); returns the number found
+// (may exceed cap).
 template <bool COMP>
 __device__ __noinline__ int exact_gather(const DropCtx& ctx, double x, double y, float cx, float cy, float z0l,
-                                            const float* s_hlb, int& s_n, unsigned long long* key, uint32_t* tri,
-                                            float* hiv, float* qtv, int cap) {
+                                            float tcut, const float* s_hlb, int& s_n, unsigned long long* key,
+                                            uint32_t* tri, float* hiv, float* qtv, int cap) {
     const int tid = threadIdx.x;
     const GridP& g = ctx.g;
     const float R = ctx.prof.R, gd = ctx.guard, Rg = R + gd, inv_step = (float)HLB_N / R;
@@ -637,21 +638,22 @@ __device__ __noinline__ int exact_gather(const DropCtx& ctx, double x, double y,
             float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
             float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
             float d = sqrtf(dx * dx + dy * dy);
-            if (!(d <= Rg && cell.maxz - hlb_at(s_hlb, d - gd, inv_step) > z0l - gd)) continue;
+            const float cub = cell.maxz - hlb_at(s_hlb, d - gd, inv_step);
+            if (!(d <= Rg && cub > z0l - gd && cub >= tcut - gd)) continue;
             for (uint32_t j = 0; j < cell.count; ++j) {
                 const Entry e = ctx.entries[cell.start + j];
                 float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
                 float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
                 float de = sqrtf(ex * ex + ey * ey);
                 float ub = e.maxz - hlb_at(s_hlb, de - gd, inv_step);
-                if (!(de <= Rg && ub > z0l - gd)) continue;
+                if (!(de <= Rg && ub > z0l - gd && ub >= tcut - gd)) continue;
                 const Tri32 t = ctx.t32[e.tri];
                 float qt, qth;
                 Iv v = COMP ? screen_composite(ctx.comp, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth)
                             : screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
                 if (!(v.hi > NEG_INF32)) continue;
                 const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
-                if (!(hi > z0l - gd)) continue;
+                if (!(hi > z0l - gd && hi >= tcut)) continue;
                 const int slot = atomicAdd(&s_n, 1);
                 if (slot < cap) {
                     key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
@@ -778,12 +780,39 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
     const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
     const float z0l = __double2float_rd(z0 - g.oz);
-    const int n = exact_gather<COMP>(ctx, x, y, cx, cy, z0l, S.hlb, *S.n, s_key, S.tri, S.hi, S.qt, EXACT_CAP);
+    const size_t base = (size_t)blockIdx.x * (size_t)G.cap;
+    unsigned long long* gk = G.key + base;
+    uint32_t* gt = G.tri + base;
+    float* gh = G.hi + base;
+    float* gq = G.qt + base;
+    // Only triangles whose upper bound reaches the fold threshold T matter,
+    // and T starts at the screen's certified lower bound less the guard: gather
+    // those first; should a branch threshold take T lower, gather again from
+    // there (the third time from the start height, which takes in every
+    // triangle the threshold can reach).
+    float tcut = ctx.blo[i] > NEG_INF32 ? ctx.blo[i] - ctx.guard : NEG_INF32;
+    int n = 0;
+    float T = NEG_INF32;
+    bool in_shared = true;
+    for (int pass = 0;; ++pass) {
+        n = exact_gather<COMP>(ctx, x, y, cx, cy, z0l, tcut, S.hlb, *S.n, s_key, S.tri, S.hi, S.qt, EXACT_CAP);
+        in_shared = n <= EXACT_CAP;
+        if (!in_shared) {
+            if (!(G.key && n <= G.cap)) {
+                if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
+                __syncthreads();
+                return;
+            }
+            exact_gather<COMP>(ctx, x, y, cx, cy, z0l, tcut, S.hlb, *S.n, gk, gt, gh, gq, G.cap);
+        }
+        T = in_shared ? exact_threshold(ctx, i, S.hi, S.qt, n, s_red) : exact_threshold(ctx, i, gh, gq, n, s_red);
+        if (!(T < tcut)) break;
+        tcut = pass == 0 ? T : NEG_INF32;
+    }
     CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     int capped = 0;
     unsigned evals = 0;
-    if (n <= EXACT_CAP) {
-        const float T = exact_threshold(ctx, i, S.hi, S.qt, n, s_red);
+    if (in_shared) {
         if (tid == 0) s_red = 0;
         __syncthreads();
         int kept = 0;
@@ -796,18 +825,11 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
         const int nk = s_red;
         exact_sort(s_key, n);
         if (tid < 32) exact_fold<COMP>(ctx, cl, s_key, nk, S.hi, S.tri, cx, cy, capped, evals);
-    } else if (G.key && n <= G.cap) {
-        // More candidates than shared memory holds: gathered again into this
+    } else {
+        // More candidates than shared memory holds: gathered into this
         // block's global scratch and folded in KD order one rank window at a
         // time (each window's ranks chosen so it fits shared memory), the
         // running height carried from window to window.
-        const size_t base = (size_t)blockIdx.x * (size_t)G.cap;
-        unsigned long long* gk = G.key + base;
-        uint32_t* gt = G.tri + base;
-        float* gh = G.hi + base;
-        float* gq = G.qt + base;
-        exact_gather<COMP>(ctx, x, y, cx, cy, z0l, S.hlb, *S.n, gk, gt, gh, gq, G.cap);
-        const float T = exact_threshold(ctx, i, gh, gq, n, s_red);
         constexpr unsigned long long DROPPED = 0xFFFFFFFF00000000ull;
         for (int k = tid; k < n; k += blockDim.x)
             if (!(gh[k] >= T)) gk[k] = DROPPED | (unsigned)k;
@@ -885,10 +907,6 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
             __syncthreads();
             cur = hi;
         }
-    } else {
-        if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
-        __syncthreads();
-        return;
     }
     if (tid < 32) {
         for (int o = 16; o > 0; o >>= 1) {

@@ -819,4 +819,94 @@ class BatchPushCutter : public Operation {
     bool y_direction = false;
 };
 
+// Waterline (src/algo/waterline.hpp:41-88): X and Y fibers at height z pushed
+// on the GPU, woven on the host into loops.  run2() (the reference's
+// SmartWeave) gives the same loops as run().
+class Waterline : public Operation {
+   public:
+    Waterline() {}
+    ~Waterline() override {}
+    void setZ(const double z) { zh = z; }
+    void run() override {
+        ocl_gb300_mesh m = mesh();
+        if (!m) return;
+        ocl_gb300_cutter d = cutter->desc();
+        ocl_gb300_loops h = nullptr;
+        if (!check(weave(m, d, &h))) return;
+        take(h);
+    }
+    virtual void run2() { run(); }
+    std::vector<std::vector<Point>> getLoops() const { return loops; }
+    std::vector<Fiber> getXFibers() const { return xfibers; }
+    std::vector<Fiber> getYFibers() const { return yfibers; }
+    void reset() override {
+        xfibers.clear();
+        yfibers.clear();
+        loops.clear();
+    }
+
+   protected:
+    virtual int weave(ocl_gb300_mesh m, const ocl_gb300_cutter& d, ocl_gb300_loops* h) {
+        return ocl_gb300_waterline(m, &d, zh, sampling, h, &stats);
+    }
+    // copies the loops and fibers out of the handle and releases it
+    void take(ocl_gb300_loops h) {
+        uint64_t nl = 0, np = 0;
+        ocl_gb300_loops_count(h, &nl, &np);
+        std::vector<double> pts(3 * np);
+        std::vector<uint64_t> off(nl + 1);
+        ocl_gb300_loops_get(h, pts.data(), off.data());
+        loops.assign(nl, std::vector<Point>());
+        for (uint64_t k = 0; k < nl; ++k)
+            for (uint64_t j = off[k]; j < off[k + 1]; ++j) loops[k].push_back(Point(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2]));
+        for (int dir = 0; dir < 2; ++dir) {
+            std::vector<Fiber>& out = dir == 0 ? xfibers : yfibers;
+            uint64_t nf = 0, nk = 0;
+            ocl_gb300_loops_fibers(h, dir, &nf, &nk, nullptr, nullptr, nullptr, nullptr, nullptr);
+            std::vector<double> fb(6 * nf), iv(2 * nk), cc(6 * nk);
+            std::vector<uint64_t> fo(nf + 1);
+            std::vector<int32_t> ty(2 * nk);
+            ocl_gb300_loops_fibers(h, dir, &nf, &nk, fb.data(), fo.data(), iv.data(), cc.data(), ty.data());
+            out.clear();
+            for (uint64_t f = 0; f < nf; ++f) {
+                Fiber fib(Point(fb[6 * f], fb[6 * f + 1], fb[6 * f + 2]), Point(fb[6 * f + 3], fb[6 * f + 4], fb[6 * f + 5]));
+                for (uint64_t j = fo[f]; j < fo[f + 1]; ++j) {
+                    Interval i(iv[2 * j], iv[2 * j + 1]);
+                    i.lower_cc = CCPoint(cc[6 * j], cc[6 * j + 1], cc[6 * j + 2], (CCType)ty[2 * j]);
+                    i.upper_cc = CCPoint(cc[6 * j + 3], cc[6 * j + 4], cc[6 * j + 5], (CCType)ty[2 * j + 1]);
+                    fib.ints.push_back(i);
+                }
+                out.push_back(fib);
+            }
+        }
+        ocl_gb300_loops_release(h);
+        nCalls = (int)stats.pairs;
+    }
+    double zh = 0.0;
+    std::vector<std::vector<Point>> loops;
+    std::vector<Fiber> xfibers, yfibers;
+};
+
+// AdaptiveWaterline (src/algo/adaptivewaterline.hpp:38-92): fibers bisected
+// where the loops bend; each bisection level pushed in one GPU call per
+// direction.
+class AdaptiveWaterline : public Waterline {
+   public:
+    AdaptiveWaterline() { sampling = 1.0; }
+    ~AdaptiveWaterline() override {}
+    void setMinSampling(double s) { min_sampling = s; }
+    void setCosLimit(double lim) { cosLimit = lim; }
+    void setSampling(double s) override {
+        sampling = s;
+        min_sampling = sampling / 10.0;
+    }
+
+   protected:
+    int weave(ocl_gb300_mesh m, const ocl_gb300_cutter& d, ocl_gb300_loops* h) override {
+        return ocl_gb300_adaptive_waterline(m, &d, zh, sampling, min_sampling, cosLimit, h, &stats);
+    }
+    double min_sampling = 0.1;
+    double cosLimit = 0.999;
+};
+
 }  // namespace ocl

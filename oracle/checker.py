@@ -290,6 +290,98 @@ def cutter_fields(cutter):
     return out
 
 
+def _waterline_lib():
+    L = _lib("ref")
+    if not hasattr(L, "_wl_ready"):
+        cd = C.POINTER(_abi.CutterDesc)
+        u64p = C.POINTER(C.c_uint64)
+        L.ref_waterline.argtypes = [_dp, C.c_long, cd, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _lp]
+        L.ref_waterline.restype = C.c_long
+        L.ref_weave.argtypes = [_dp, C.c_long, u64p, _dp, _dp, C.c_long, u64p, _dp, _lp]
+        L.ref_weave.restype = C.c_long
+        L.ref_loops_get.argtypes = [_dp, _lp]
+        L.ref_loops_get.restype = None
+        L.ref_fibers_get.argtypes = [C.c_int, _dp, u64p, _dp]
+        L.ref_fibers_get.restype = C.c_long
+        L._wl_ready = True
+    return L
+
+
+def _ref_loops(L, nloops, npts):
+    pts = np.zeros((npts.value, 3))
+    off = np.zeros(nloops + 1, dtype=np.int64)
+    L.ref_loops_get(_ptr(pts), off.ctypes.data_as(_lp))
+    return [pts[off[k]:off[k + 1]].copy() for k in range(nloops)]
+
+
+def _ref_fibers(L, d):
+    u64p = C.POINTER(C.c_uint64)
+    tot = np.zeros(1, dtype=np.uint64)
+    F = L.ref_fibers_get(d, None, tot.ctypes.data_as(u64p), None)
+    fib = np.zeros((F, 6))
+    off = np.zeros(F + 1, dtype=np.uint64)
+    iv = np.zeros((int(tot[0]), 2))
+    L.ref_fibers_get(d, _ptr(fib), off.ctypes.data_as(u64p), _ptr(iv))
+    return fib, off, iv
+
+
+def ref_waterline(tris, cutter, z, sampling, adaptive=False, min_sampling=None, cos_limit=0.999):
+    """The reference's Waterline::run or AdaptiveWaterline::run at height z:
+    (loops as (n, 3) arrays, X fibers, Y fibers), fibers as (endpoints
+    (F, 6), interval offsets (F+1), [lower, upper] t-values (K, 2)).  (The
+    run2 variants, SmartWeave, are not offered: the reference's
+    SmartWeave::build dereferences an end iterator when the fibers crossing
+    an interval are not adjacent, smart_weave.cpp:78-81.)"""
+    L = _waterline_lib()
+    tris = np.ascontiguousarray(tris, dtype=np.float64)
+    desc = cutter.desc()
+    npts = C.c_long(0)
+    mode = 2 if adaptive else 0
+    ms = sampling / 10.0 if min_sampling is None else min_sampling
+    n = L.ref_waterline(_ptr(tris), len(tris), C.byref(desc), z, sampling, ms, cos_limit, mode, C.byref(npts))
+    if n < 0:
+        raise RuntimeError("ref_waterline failed")
+    return _ref_loops(L, n, npts), _ref_fibers(L, 0), _ref_fibers(L, 1)
+
+
+def ref_weave(xfibers, yfibers):
+    """The reference's SimpleWeave on the given fibers (as ref_waterline
+    returns them): the loops."""
+    L = _waterline_lib()
+    u64p = C.POINTER(C.c_uint64)
+    args = []
+    for fib, off, iv in (xfibers, yfibers):
+        fib = np.ascontiguousarray(fib, dtype=np.float64)
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        iv = np.ascontiguousarray(iv, dtype=np.float64).reshape(-1, 2)
+        args.append((fib, off, iv))
+    npts = C.c_long(0)
+    (xf, xo, xi), (yf, yo, yi) = args
+    n = L.ref_weave(_ptr(xf), len(xf), xo.ctypes.data_as(u64p), _ptr(xi), _ptr(yf), len(yf),
+                    yo.ctypes.data_as(u64p), _ptr(yi), C.byref(npts))
+    return _ref_loops(L, n, npts)
+
+
+def canonical_loops(loops):
+    """Loops in a form that does not depend on where each loop starts or on
+    the order of the loops (the reference starts each loop at the CL vertex
+    with the lowest address): every loop rotated to its lexicographically
+    smallest rotation, then the loops sorted."""
+    out = []
+    for lp in loops:
+        a = np.asarray(lp, dtype=np.float64).reshape(-1, 3)
+        n = len(a)
+        best = None
+        for r in range(n):
+            cand = np.roll(a, -r, axis=0)
+            key = tuple(cand.ravel())
+            if best is None or key < best[0]:
+                best = (key, cand)
+        out.append(best[1] if best else a)
+    out.sort(key=lambda a: (len(a), tuple(a.ravel())))
+    return out
+
+
 def ref_preset_fields(preset: int, args):
     L = _lib("ref")
     a = _d(list(args) + [0.0] * (4 - len(args)))

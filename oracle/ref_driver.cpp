@@ -32,6 +32,10 @@
 #include "line.hpp"
 #include "arc.hpp"
 #include "kdtree.hpp"
+#include "fiber.hpp"
+#include "waterline.hpp"
+#include "adaptivewaterline.hpp"
+#include "simple_weave.hpp"
 
 #include "ocl_oracle.h"
 
@@ -142,6 +146,43 @@ void PeekComposite::dump(const ocl::CompositeCutter* c, double* out) {
         PeekCutter::dump(p->cutter[n], o);
         o[6] = p->radiusvec[n]; o[7] = p->heightvec[n]; o[8] = p->zoffset[n];
     }
+}
+
+// Waterline and AdaptiveWaterline with their fibers readable (protected in
+// the reference classes).
+struct RefWaterline : public ocl::Waterline {
+    const std::vector<ocl::Fiber>& fibers(int dir) const { return dir == 0 ? xfibers : yfibers; }
+};
+struct RefAdaptiveWaterline : public ocl::AdaptiveWaterline {
+    const std::vector<ocl::Fiber>& fibers(int dir) const { return dir == 0 ? xfibers : yfibers; }
+};
+
+// The last ref_waterline / ref_weave result, read back by ref_loops_get and
+// ref_fibers_get.
+struct WaterlineResult {
+    std::vector<std::vector<ocl::Point>> loops;
+    std::vector<ocl::Fiber> fibers[2];
+};
+WaterlineResult g_wl;
+
+void keep_loops(const std::vector<std::vector<ocl::Point>>& loops, long* npts) {
+    g_wl.loops = loops;
+    long n = 0;
+    for (const auto& l : loops) n += (long)l.size();
+    *npts = n;
+}
+
+// Fibers from endpoint rows (x1 y1 z1 x2 y2 z2), per-fiber interval offsets
+// and [lower, upper] t-values, as the weave receives them.
+std::vector<ocl::Fiber> make_fibers(const double* fib, long F, const uint64_t* off, const double* iv) {
+    std::vector<ocl::Fiber> out;
+    for (long k = 0; k < F; ++k) {
+        const double* f = fib + 6 * k;
+        ocl::Fiber fb(ocl::Point(f[0], f[1], f[2]), ocl::Point(f[3], f[4], f[5]));
+        for (uint64_t j = off[k]; j < off[k + 1]; ++j) fb.ints.push_back(ocl::Interval(iv[2 * j], iv[2 * j + 1]));
+        out.push_back(fb);
+    }
+    return out;
 }
 
 }  // namespace
@@ -373,6 +414,95 @@ int ref_preset_fields(int preset, const double* a, double* out) {
     }
     PeekComposite::dump(c.get(), out);
     return 0;
+}
+
+// Waterline::run / run2 (mode 0 / 1) and AdaptiveWaterline::run / run2
+// (mode 2 / 3) at height z; the loops and both fiber sets are kept for
+// ref_loops_get / ref_fibers_get.  Returns the number of loops, *npts the
+// number of loop points.
+long ref_waterline(const double* tris, long ntri, const ocl_gb300_cutter* c, double z, double sampling,
+                   double min_sampling, double cos_limit, int mode, long* npts) {
+    CutterHolder h;
+    if (!make_cutter(c, h)) return -1;
+    ocl::STLSurf s;
+    make_surf(tris, ntri, s);
+    if (mode < 2) {
+        RefWaterline wl;
+        wl.setSTL(s);
+        wl.setCutter(h.top);
+        wl.setZ(z);
+        wl.setSampling(sampling);
+        if (mode == 0) wl.run(); else wl.run2();
+        keep_loops(wl.getLoops(), npts);
+        g_wl.fibers[0] = wl.fibers(0);
+        g_wl.fibers[1] = wl.fibers(1);
+    } else {
+        RefAdaptiveWaterline wl;
+        wl.setSTL(s);
+        wl.setCutter(h.top);
+        wl.setZ(z);
+        wl.setSampling(sampling);
+        wl.setMinSampling(min_sampling);
+        wl.setCosLimit(cos_limit);
+        if (mode == 2) wl.run(); else wl.run2();
+        keep_loops(wl.getLoops(), npts);
+        g_wl.fibers[0] = wl.fibers(0);
+        g_wl.fibers[1] = wl.fibers(1);
+    }
+    return (long)g_wl.loops.size();
+}
+
+// SimpleWeave (build + face_traverse) on the given X and Y fibers.
+long ref_weave(const double* xfib, long nx, const uint64_t* xoff, const double* xiv, const double* yfib, long ny,
+               const uint64_t* yoff, const double* yiv, long* npts) {
+    g_wl.fibers[0] = make_fibers(xfib, nx, xoff, xiv);
+    g_wl.fibers[1] = make_fibers(yfib, ny, yoff, yiv);
+    ocl::weave::SimpleWeave w;
+    for (ocl::Fiber& f : g_wl.fibers[0]) w.addFiber(f);
+    for (ocl::Fiber& f : g_wl.fibers[1]) w.addFiber(f);
+    w.build();
+    w.face_traverse();
+    keep_loops(w.getLoops(), npts);
+    return (long)g_wl.loops.size();
+}
+
+// The kept loops: points (3 doubles each) and offsets (nloops + 1).
+void ref_loops_get(double* pts, long* off) {
+    long n = 0;
+    off[0] = 0;
+    for (size_t k = 0; k < g_wl.loops.size(); ++k) {
+        for (const ocl::Point& p : g_wl.loops[k]) {
+            pts[3 * n] = p.x; pts[3 * n + 1] = p.y; pts[3 * n + 2] = p.z;
+            ++n;
+        }
+        off[k + 1] = n;
+    }
+}
+
+// The kept fibers of one direction: count (fib == nullptr), or endpoints,
+// interval offsets and [lower, upper] t-values.
+long ref_fibers_get(int dir, double* fib, uint64_t* off, double* iv) {
+    const std::vector<ocl::Fiber>& fs = g_wl.fibers[dir];
+    if (!fib) {
+        long k = 0;
+        for (const ocl::Fiber& f : fs) k += (long)f.ints.size();
+        off[0] = (uint64_t)k;
+        return (long)fs.size();
+    }
+    uint64_t n = 0;
+    for (size_t k = 0; k < fs.size(); ++k) {
+        const ocl::Fiber& f = fs[k];
+        const double e[6] = {f.p1.x, f.p1.y, f.p1.z, f.p2.x, f.p2.y, f.p2.z};
+        std::memcpy(fib + 6 * k, e, sizeof(e));
+        off[k] = n;
+        for (const ocl::Interval& i : f.ints) {
+            iv[2 * n] = i.lower;
+            iv[2 * n + 1] = i.upper;
+            ++n;
+        }
+    }
+    off[fs.size()] = n;
+    return (long)fs.size();
 }
 
 }  // extern "C"

@@ -7,12 +7,17 @@
 //   facade_test apdc <tris.bin> <spans.bin> <out.bin> <sampling> <min_sampling> <cos_limit> <cutter> <args...>
 //   facade_test rotate <tris.bin> <angles.bin> <out.bin>
 //   facade_test stldrop <file.stl> <cl.bin> <out.bin> <cutter> <args...>
+//   facade_test waterline <tris.bin> <params.bin> <out.bin> <cutter> <args...>
 //
 // rotate: STLSurf::rotate(xr, yr, zr); output the triangles, then the bbox (6).
 // stldrop: STLReader -> STLSurf -> BatchDropCutter, three runs on one
 // surface: as read; after addTriangle of a horizontal triangle over the
 // surface's bbox at maxz + 1; after rotate(0, 0, pi/2).  Output: the three
 // runs' points one after the other (the device copy must follow each change).
+//
+// waterline: params = z, sampling, adaptive (0/1), min_sampling, cos_limit;
+// Waterline (or AdaptiveWaterline) run(); output: loop count, then per loop
+// its point count and points (3 doubles each), then the X and Y fiber counts.
 //
 // tris.bin: N x 9 doubles; cl.bin: M x 3; fibers.bin: F x 6; spans.bin: S x 11.
 // cutter: cyl d l | ball d l | bull d r l | cone d angle l | ballcone d1 d2 angle
@@ -50,7 +55,7 @@ static std::unique_ptr<ocl::MillingCutter> make_cutter(int argc, char** argv, in
 
 int main(int argc, char** argv) {
     if (argc < 5) {
-        std::fprintf(stderr, "usage: facade_test drop|push|path|apdc|rotate|stldrop ...\n");
+        std::fprintf(stderr, "usage: facade_test drop|push|path|apdc|rotate|stldrop|waterline ...\n");
         return 2;
     }
     std::string mode = argv[1];
@@ -122,6 +127,37 @@ int main(int argc, char** argv) {
         apdc.run();
         if (!apdc.lastError().empty()) return 1;
         put_points(apdc.getPoints());
+    } else if (mode == "waterline") {
+        auto cutter = make_cutter(argc, argv, 5);
+        if (P.size() < 5) return 2;
+        std::unique_ptr<ocl::Waterline> wl;
+        if (P[2] != 0.0) {
+            auto* a = new ocl::AdaptiveWaterline();
+            a->setSampling(P[1]);
+            a->setMinSampling(P[3]);
+            a->setCosLimit(P[4]);
+            wl.reset(a);
+        } else {
+            wl.reset(new ocl::Waterline());
+            wl->setSampling(P[1]);
+        }
+        wl->setSTL(surf);
+        wl->setCutter(cutter.get());
+        wl->setZ(P[0]);
+        wl->run();
+        if (!wl->lastError().empty()) return 1;
+        const std::vector<std::vector<ocl::Point>> loops = wl->getLoops();
+        out.push_back((double)loops.size());
+        for (const auto& lp : loops) {
+            out.push_back((double)lp.size());
+            for (const ocl::Point& q : lp) {
+                out.push_back(q.x);
+                out.push_back(q.y);
+                out.push_back(q.z);
+            }
+        }
+        out.push_back((double)wl->getXFibers().size());
+        out.push_back((double)wl->getYFibers().size());
     } else if (mode == "drop") {
         auto cutter = make_cutter(argc, argv, 5);
         ocl::BatchDropCutter bdc;

@@ -10,7 +10,8 @@ the GPU tests run without it.
 
 The real-mesh fixtures (real_*.npz) are made from the reference's stl/
 folder next to its sources (REF_SRC, as for oracle/Makefile) when missing or
-with --real.
+with --real; the waterline fixtures (waterline_*.npz) when missing or with
+--waterline.
 """
 from __future__ import annotations
 
@@ -100,6 +101,37 @@ def real_mesh_case(name, stl_dir):
     np.savez_compressed(os.path.join(HERE, "real_" + name + ".npz"), **out)
 
 
+# Waterline / AdaptiveWaterline cases: (fixture, mesh, cutters, heights,
+# sampling, min_sampling); the reference's Waterline::run and
+# AdaptiveWaterline::run (cos limit 0.999) at each height.
+WATERLINE_CUTTERS = ("cyl", "ball", "bull", "cone", "ballcone")
+
+
+def waterline_case(name, tris, cutters, zs, sampling, min_sampling):
+    out = {"tris": tris, "zs": np.asarray(zs, dtype=np.float64), "sampling": sampling, "min_sampling": min_sampling}
+    for cname in cutters:
+        for k, z in enumerate(zs):
+            for mode in ("wl", "awl"):
+                loops, xf, yf = ck.ref_waterline(tris, CUTTERS[cname](), z, sampling, adaptive=mode == "awl",
+                                                 min_sampling=min_sampling)
+                key = f"{cname}_{mode}_{k}"
+                out[key + "_pts"] = np.concatenate(loops).reshape(-1, 3) if loops else np.zeros((0, 3))
+                out[key + "_off"] = np.cumsum([0] + [len(lp) for lp in loops]).astype(np.int64)
+                for d, (fib, off, iv) in enumerate((xf, yf)):
+                    out[f"{key}_f{d}"], out[f"{key}_o{d}"], out[f"{key}_i{d}"] = fib, off.astype(np.int64), iv
+    np.savez_compressed(os.path.join(HERE, "waterline_" + name + ".npz"), **out)
+
+
+def waterline_fixtures(stl_dir):
+    hf = w.heightfield(24, 24, seed=1)
+    waterline_case("heightfield", hf, WATERLINE_CUTTERS, (11.0, 14.0, 20.0), 1.0, 0.1)
+    sop = ck.ref_stl_read(os.path.join(stl_dir, "sphere_on_plate.stl"))
+    lo, hi = sop.reshape(-1, 3).min(axis=0), sop.reshape(-1, 3).max(axis=0)
+    zs = tuple(float(z) for z in lo[2] + (hi[2] - lo[2]) * np.array([0.1, 0.45, 0.8]))
+    waterline_case("sphere_on_plate", sop, ("ball", "bull"), zs, float(hi[0] - lo[0]) / 60.0,
+                   float(hi[0] - lo[0]) / 600.0)
+
+
 def main():
     ck.build(ref=True)
     if not ck.available("ref"):
@@ -120,6 +152,9 @@ def main():
     if "--real" in sys.argv or not all(os.path.exists(os.path.join(HERE, f"real_{m}.npz")) for m in REAL_MESHES):
         for m in REAL_MESHES:
             real_mesh_case(m, stl_dir)
+    if "--waterline" in sys.argv or not all(os.path.exists(os.path.join(HERE, f"waterline_{m}.npz"))
+                                            for m in ("heightfield", "sphere_on_plate")):
+        waterline_fixtures(stl_dir)
     print("golden fixtures written to", HERE)
 
 

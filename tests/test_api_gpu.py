@@ -162,3 +162,31 @@ def test_stlreader_into_stlsurf_and_drop(ocl, oracle_lib, tmp_path):
     z2 = run()  # the rotated surface is a new device mesh
     zr = oracle_lib.drop(s.array(), c, g["cl"][:200], "port")[0]
     assert np.abs(z2 - zr).max() <= 1e-5
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_waterline_mirror(ocl, adaptive):
+    """ocl.Waterline / ocl.AdaptiveWaterline as the reference's Python
+    binding is used (setSTL, setCutter, setZ, setSampling, run, getLoops)."""
+    from oracle import checker
+    g = golden("waterline_heightfield")
+    s = _surface(ocl, g["tris"])
+    for k, z in enumerate(g["zs"]):
+        wl = ocl.AdaptiveWaterline() if adaptive else ocl.Waterline()
+        wl.setSTL(s)
+        wl.setCutter(CUTTERS["bull"]())
+        wl.setZ(float(z))
+        wl.setSampling(float(g["sampling"]))
+        if adaptive:
+            wl.setMinSampling(float(g["min_sampling"]))
+        wl.run()
+        loops = [np.array([[p.x, p.y, p.z] for p in lp]) for lp in wl.getLoops()]
+        key = f"bull_{'awl' if adaptive else 'wl'}_{k}"
+        pts, off = g[key + "_pts"], g[key + "_off"]
+        ref = [pts[off[j]:off[j + 1]] for j in range(len(off) - 1)]
+        a, b = checker.canonical_loops(loops), checker.canonical_loops(ref)
+        assert len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b))
+        assert len(wl.getXFibers()) == len(g[key + "_f0"])
+        xf = wl.getXFibers()
+        n = sum(len(f.ints) for f in xf)
+        assert n == len(g[key + "_i0"])

@@ -123,3 +123,33 @@ def test_facade_stlreader_surface_cache(exe, oracle_lib, tmp_path):
         s3.rotate(0.0, 0.0, 1.5707963267948966)
         t3 = s3.array()
     assert np.abs(out[2, :, 2] - oracle_lib.drop(t3, ball, cl, "port")[0]).max() <= 1e-5
+
+
+def _facade_loops(out):
+    n = int(out[0])
+    k, loops = 1, []
+    for _ in range(n):
+        m = int(out[k])
+        loops.append(out[k + 1:k + 1 + 3 * m].reshape(-1, 3))
+        k += 1 + 3 * m
+    return loops, int(out[k]), int(out[k + 1])
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+@pytest.mark.parametrize("cname", ["ball", "bull", "cone"])
+def test_facade_waterline(exe, tmp_path, cname, adaptive):
+    """ocl::Waterline / ocl::AdaptiveWaterline (setSTL, setCutter, setZ,
+    setSampling, [setMinSampling, setCosLimit], run, getLoops, getXFibers,
+    getYFibers) against the reference's loops."""
+    from oracle import checker
+    g = golden("waterline_heightfield")
+    for k, z in enumerate(g["zs"]):
+        params = [float(z), float(g["sampling"]), 1.0 if adaptive else 0.0, float(g["min_sampling"]), 0.999]
+        out = _run(exe, tmp_path, "waterline", g["tris"], params, ARGS[cname])
+        loops, nx, ny = _facade_loops(out)
+        key = f"{cname}_{'awl' if adaptive else 'wl'}_{k}"
+        pts, off = g[key + "_pts"], g[key + "_off"]
+        ref = [pts[off[j]:off[j + 1]] for j in range(len(off) - 1)]
+        a, b = checker.canonical_loops(loops), checker.canonical_loops(ref)
+        assert len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b)), key
+        assert nx == len(g[key + "_f0"]) and ny == len(g[key + "_f1"])
