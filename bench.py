@@ -64,6 +64,11 @@ def parse():
                     help="run only the request-loop measurement and print it")
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the 64-job batching measurement and print it (for profiling)")
+    ap.add_argument("--waterline-only", action="store_true",
+                    help="run only the waterline measurement and print it (with --wl-levels / --wl-cutters a "
+                         "small case for profiling)")
+    ap.add_argument("--wl-levels", type=int, default=50, help="waterline heights (evenly from 1 to 49 mm)")
+    ap.add_argument("--wl-cutters", default="ball,bull", help="waterline cutters (ball, bull)")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one device step with statistics, print its counters and exit (for ncu)")
     return ap.parse_args()
@@ -150,7 +155,7 @@ def cpu_baseline(tris, cl, sample, nthreads=0):
                       f"(seeded uniform sample of the 0.1 mm raster), {total:.2f} s of CPU loop time"}
 
 
-def aux_measurements(cl_mesh, cuts, with_cpu):
+def aux_measurements(cl_mesh, cuts, with_cpu, wl_levels=50, wl_cutters=("ball", "bull")):
     """The other operations on the path, measured beside the headline:
     Waterline at the waterline workload's full size (sphere-on-plate + torus,
     499,202 triangles; 50 heights z = 1..49 mm; X and Y fibers over the mesh
@@ -166,9 +171,11 @@ def aux_measurements(cl_mesh, cuts, with_cpu):
     out = {}
     tris = w.sphere_torus(1)
     mesh = _native.DeviceMesh(tris)
-    zs = np.linspace(1.0, 49.0, 50)
+    zs = np.linspace(1.0, 49.0, wl_levels)
     wl = {}
     for name, c in (("ball", cu.BallCutter(6.0, 20.0)), ("bull", cu.BullCutter(6.0, 1.0, 20.0))):
+        if name not in wl_cutters:
+            continue
         bb = tris.reshape(-1, 3)
         extent = float(bb[:, 0].max() - bb[:, 0].min()) + 4 * c.radius
         sampling = extent / 2000.0
@@ -183,7 +190,7 @@ def aux_measurements(cl_mesh, cuts, with_cpu):
                "loop_points": int(sum(len(lp) for lv in levels for lp in lv.loops)),
                "wall_ms": wall * 1e3, "push_device_ms": st.kernel_ms, "weave_and_host_ms": wall * 1e3 - st.kernel_ms,
                "fibers_per_s": nfib / wall, "push_fibers_per_s": nfib / (st.kernel_ms / 1e3),
-               "pairs": int(st.pairs)}
+               "candidates": int(st.pairs), "fp64_pushes": int(st.refined)}
         if with_cpu:
             from oracle import checker
             sub = [lv.fibers(d)[0][::50] for lv in levels[::5] for d in (0, 1)]
@@ -198,6 +205,8 @@ def aux_measurements(cl_mesh, cuts, with_cpu):
         wl[name] = rec
     out["waterline"] = wl
     mesh.release()
+    if cl_mesh is None:
+        return out
     # paths: zig-zag of 100 lines across the bump mesh
     m2 = _native.DeviceMesh(cl_mesh)
     spans = []
@@ -582,6 +591,10 @@ def main():
     rank, world, local, dist = dist_setup(args.gpus)
     import torch
     torch.cuda.set_device(local)
+    if args.waterline_only:
+        wl = aux_measurements(None, None, not args.no_cpu_baseline, args.wl_levels, args.wl_cutters.split(","))
+        print(json.dumps({"waterline": wl["waterline"]}), flush=True)
+        return
     import opencamlib_gb300 as ocl
     from opencamlib_gb300 import _abi
     from opencamlib_gb300 import workloads as w

@@ -242,8 +242,10 @@ int ocl_gb300_batch_release(ocl_gb300_batch batch);
  * requests with host buffers; a scheduler thread keeps up to `slots` batches
  * on the GPU at once (batches as in ocl_gb300_batch_*), admits queued
  * requests into the next batch while its CL points fit the slot's share of
- * the device-memory budget, and sends an adaptive request's bisection levels
- * through successive batches (each level rejoins the head of the queue).
+ * the device-memory budget and max_batch_points (a drop request that does
+ * not fit whole is split, its pieces going through successive batches), and
+ * sends an adaptive request's bisection levels through successive batches
+ * (each level rejoins the head of the queue).
  * Results are those of ocl_gb300_drop / ocl_gb300_adaptive_path_drop for the
  * same request, whatever else is in the mix.  Meshes added to a server must
  * outlive it; request buffers must stay valid until ocl_gb300_server_wait
@@ -253,7 +255,8 @@ typedef struct ocl_gb300_server_opts {
     int32_t slots;              /* batches on the GPU at once (0: 2; at most 16) */
     int32_t max_batch_requests; /* requests per batch (0: 64) */
     int32_t list_capacity;      /* candidates kept per CL point (16..256; 0: 256) */
-    int32_t reserved;
+    int32_t max_batch_points;   /* CL points per batch (0: 262,144); a larger drop request is split into
+                                   pieces over successive batches, an adaptive level is not split */
 } ocl_gb300_server_opts;
 
 typedef struct ocl_gb300_request_info {
@@ -277,13 +280,14 @@ int ocl_gb300_server_create(const ocl_gb300_server_opts* opts, ocl_gb300_server*
 int ocl_gb300_server_add_mesh(ocl_gb300_server server, ocl_gb300_mesh mesh, int32_t* mesh_id);
 /* BatchDropCutter request: host cl_xyz (M x 3) in; z_out (M), cc_out (M x 3),
  * type_out (M) written when the request completes.  Rejected at once
- * (BAD_ARG: unknown mesh or bad cutter; OOM: more points than one batch may
- * hold under the budget). */
+ * (BAD_ARG: unknown mesh or bad cutter). */
 int ocl_gb300_server_submit_drop(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
                                  const double* cl_xyz, uint64_t M, double* z_out, double* cc_out,
                                  int32_t* type_out, uint64_t* request_id);
 /* AdaptivePathDropCutter request over S spans (as ocl_gb300_adaptive_path_drop);
- * *count receives the number of points; status CAPACITY if cap is too small. */
+ * *count receives the number of points; status CAPACITY if cap is too small.
+ * Rejected at once with OOM when its first level holds more points than one
+ * batch's buffers may under the budget. */
 int ocl_gb300_server_submit_adaptive(ocl_gb300_server server, int32_t mesh_id, const ocl_gb300_cutter* cutter,
                                      const double* spans, uint64_t S, double sampling, double min_sampling,
                                      double cos_limit, double* xyz_out, double* cc_out, int32_t* type_out,
@@ -398,6 +402,16 @@ int ocl_gb300_loops_release(ocl_gb300_loops loops);
  * first and the last always; lists of 0 or 1 points unchanged); keep must
  * hold n entries.  Host code only (no device needed). */
 int ocl_gb300_line_filter(const double* xyz, uint64_t n, double tol, uint64_t* keep, uint64_t* nkeep);
+
+/* The same filter as a device pass over many point lists at once (the CL
+ * points of many PathDropCutter / AdaptivePathDropCutter paths), one warp per
+ * list.  Device pointers: d_xyz (3 doubles per point), list p is points
+ * [d_offsets[p], d_offsets[p+1]); d_keep receives at the same offsets the
+ * indices (within the list) of the points kept, d_nkeep[p] their count.
+ * Enqueued on `stream` (a cudaStream_t; NULL: the default stream); the
+ * decisions are ocl_gb300_line_filter's, bit for bit. */
+int ocl_gb300_line_filter_device(const double* d_xyz, const uint64_t* d_offsets, uint64_t npaths, double tol,
+                                 uint64_t* d_keep, uint64_t* d_nkeep, void* stream);
 
 /* ---- introspection (parity checks of the index and the FP32 screen) ------ */
 /* The KD-tree leaf visit order the device holds: order[k] = insertion index

@@ -104,7 +104,7 @@ class BatchInfo(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("slots", C.c_int32), ("max_batch_requests", C.c_int32),
-                ("list_capacity", C.c_int32), ("reserved", C.c_int32)]
+                ("list_capacity", C.c_int32), ("max_batch_points", C.c_int32)]
 
 
 class RequestInfo(C.Structure):

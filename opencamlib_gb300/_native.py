@@ -23,7 +23,7 @@ _u64p = C.POINTER(C.c_uint64)
 # every entry point declared in include/ocl_gb300.h
 EXPORTS = [
     "ocl_gb300_mesh_create", "ocl_gb300_mesh_release", "ocl_gb300_mesh_size", "ocl_gb300_mesh_bbox",
-    "ocl_gb300_stl_read", "ocl_gb300_line_filter",
+    "ocl_gb300_stl_read", "ocl_gb300_line_filter", "ocl_gb300_line_filter_device",
     "ocl_gb300_drop", "ocl_gb300_drop_device", "ocl_gb300_drop_device_noalloc", "ocl_gb300_push", "ocl_gb300_path_drop",
     "ocl_gb300_adaptive_path_drop", "ocl_gb300_stage_times", "ocl_gb300_fma_peaks", "ocl_gb300_last_error", "ocl_gb300_version",
     "ocl_gb300_device_available", "ocl_gb300_mesh_kd_order", "ocl_gb300_mesh_kd_rank", "ocl_gb300_overlap_sets",
@@ -72,6 +72,8 @@ def lib():
     L.ocl_gb300_fma_peaks.argtypes = [_dp, _dp]
     L.ocl_gb300_stl_read.argtypes = [C.c_char_p, _dp, C.c_uint64, _u64p]
     L.ocl_gb300_line_filter.argtypes = [_dp, C.c_uint64, C.c_double, _u64p, _u64p]
+    L.ocl_gb300_line_filter_device.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p,
+                                               C.c_void_p, C.c_void_p]
     _i64p = C.POINTER(C.c_int64)
     L.ocl_gb300_mesh_kd_order.argtypes = [C.c_void_p, C.c_int, _i64p]
     L.ocl_gb300_mesh_kd_rank.argtypes = [C.c_void_p, _i64p]
@@ -202,6 +204,14 @@ def weave(xfibers, yfibers) -> "Loops":
     check(lib().ocl_gb300_weave(_p(xf), len(xf), _p(xo, _u64p), _p(xi) if xi.size else None, _p(yf), len(yf),
                                 _p(yo, _u64p), _p(yi) if yi.size else None, C.byref(h)))
     return Loops(h)
+
+
+def line_filter_device(d_xyz: int, d_offsets: int, npaths: int, tol: float, d_keep: int, d_nkeep: int,
+                       stream: int = 0) -> None:
+    """LineCLFilter over many point lists on the device (pointers as ints;
+    see ocl_gb300_line_filter_device); enqueued on `stream`."""
+    check(lib().ocl_gb300_line_filter_device(C.c_void_p(d_xyz), C.c_void_p(d_offsets), int(npaths), float(tol),
+                                             C.c_void_p(d_keep), C.c_void_p(d_nkeep), C.c_void_p(stream)))
 
 
 def fma_peaks() -> tuple:
@@ -497,8 +507,8 @@ class Server:
     """Request loop over device-resident meshes (ocl_gb300_server_*):
     submit_drop / submit_adaptive from any thread, wait() for results."""
 
-    def __init__(self, hbm_budget_bytes=0, slots=0, max_batch_requests=0, list_capacity=0):
-        opts = _abi.ServerOpts(hbm_budget_bytes, slots, max_batch_requests, list_capacity, 0)
+    def __init__(self, hbm_budget_bytes=0, slots=0, max_batch_requests=0, list_capacity=0, max_batch_points=0):
+        opts = _abi.ServerOpts(hbm_budget_bytes, slots, max_batch_requests, list_capacity, max_batch_points)
         h = C.c_void_p()
         check(lib().ocl_gb300_server_create(C.byref(opts), C.byref(h)))
         self._h = h

@@ -416,7 +416,39 @@ void mesh_destroy(Mesh* m) {
     }
     cudaFree(m->drop_kd.d_nodes);
     cudaFree(m->drop_kd.d_order);
+    cudaFree(m->d_edge_sin);
     delete m;
+}
+
+// BullCutter's push through an edge (src/cutters/bullcutter.cpp:131-132)
+// takes theta = atan(dz / xyNorm(p2 - p1)) and sin(theta): a value of the
+// edge alone, computed here with the host's atan and sin so that it is the
+// reference's double (the device's atan and sin can differ in the last bit).
+int ensure_edge_sin(Mesh& m) {
+    if (m.d_edge_sin || m.n == 0) return OCL_GB300_OK;
+    std::vector<Tri64> t(m.n);
+    CK(cudaMemcpy(t.data(), m.d_t64, m.n * sizeof(Tri64), cudaMemcpyDeviceToHost));
+    std::vector<double> s(3 * m.n);
+    for (uint64_t i = 0; i < m.n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double* p1 = &t[i].p[3 * k];
+            const double* p2 = &t[i].p[3 * ((k + 1) % 3)];
+            const double dx = p2[0] - p1[0], dy = p2[1] - p1[1], dz = p2[2] - p1[2];
+            const double xy = std::sqrt(dx * dx + dy * dy);
+            s[3 * i + k] = std::sin(std::atan(dz / xy));
+        }
+    double* d = nullptr;
+    if (cudaMalloc(&d, s.size() * sizeof(double)) != cudaSuccess) {
+        set_error("edge slopes: device allocation failed");
+        return OCL_GB300_OOM;
+    }
+    if (cudaMemcpy(d, s.data(), s.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        set_error("edge slopes: copy failed");
+        return OCL_GB300_DEVICE_ERROR;
+    }
+    m.d_edge_sin = d;
+    return OCL_GB300_OK;
 }
 
 }  // namespace oclg

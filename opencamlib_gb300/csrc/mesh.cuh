@@ -63,10 +63,16 @@ struct Mesh {
     uint64_t nentries = 0;
     PushIndex push[2];
     PushIndex drop_kd;               // XY tree of the drop-cutter search (device ids)
+    // per triangle (device order) and edge n (vertex n to vertex n+1):
+    // sin(atan(dz / xy length)), the bull push's edge slope, computed on the
+    // host with the host's libm as the reference does; built on first use
+    double* d_edge_sin = nullptr;
     std::mutex mu;
 };
 
 int upload_kd(Mesh& M, const KDTreeD& kd, PushIndex& out);
+// The edge slopes of d_edge_sin, built on first use.
+int ensure_edge_sin(Mesh& m);
 // The YZ (X-fibers) or XZ (Y-fibers) tree of the push-cutter, built on first use.
 int ensure_push_index(Mesh& m, int dir);
 std::string& last_error_ref();

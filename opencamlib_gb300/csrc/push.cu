@@ -33,6 +33,7 @@ struct PushCtx {
     CutterP cp;
     int dir;
     const Tri64* t64;
+    const double* esin;  // edge slopes, 3 per triangle
     const KDNodeD* nodes;
     const int32_t* order;
     const double* fib;
@@ -42,7 +43,7 @@ struct PushCtx {
     unsigned long long* cursor;
     uint32_t* counts;
     uint64_t* offs;
-    unsigned long long* counters;  // [0] calls, [1] capped, [2] merge overflow
+    unsigned long long* counters;  // [0] calls, [1] capped, [2] merge overflow, [3] cursor, [4] FP64 pushes
 };
 
 __device__ __forceinline__ bool iv_outside(const Ival64& a, const Ival64& b) {
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     int n = 0;
     bool overflow = false;
     unsigned long long calls = 0;
+    unsigned pushed = 0;
     int capped = 0;
     uint2* st = s_stack[wl];
     const unsigned amask = __ballot_sync(0xffffffffu, active);
@@ -142,7 +144,8 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         if (nd.leaf_begin >= 0) {
             for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
                 if (!in) continue;
-                const Tri64& t = ctx.t64[ctx.order[k]];
+                const int32_t ti = ctx.order[k];
+                const Tri64& t = ctx.t64[ti];
                 double halfw = r;  // how far along the fiber the axis can be from the triangle
                 // the KD walk accepts whole leaves; every push contact lies on the
                 // cutter's surface: within the radius of the axis and no lower
@@ -195,7 +198,8 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
                 }
                 Ival64 iv;
                 iv_init(iv);
-                push_triangle64(ctx.cp, fb, iv, t, &capped);
+                ++pushed;
+                push_triangle64(ctx.cp, fb, iv, t, ctx.esin ? ctx.esin + 3 * (size_t)ti : nullptr, &capped);
                 if (!overflow && !fiber_add(ints, n, iv, cap)) overflow = true;
                 ++calls;
             }
@@ -247,11 +251,13 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         }
     }
     for (int o = 16; o > 0; o >>= 1) calls += __shfl_xor_sync(0xffffffffu, calls, o);
+    for (int o = 16; o > 0; o >>= 1) pushed += __shfl_xor_sync(0xffffffffu, pushed, o);
     for (int o = 16; o > 0; o >>= 1) capped += __shfl_xor_sync(0xffffffffu, capped, o);
     int ov = overflow ? 1 : 0;
     for (int o = 16; o > 0; o >>= 1) ov += __shfl_xor_sync(0xffffffffu, ov, o);
     if (lane == 0) {
         atomicAdd(&ctx.counters[0], calls);
+        if (pushed) atomicAdd(&ctx.counters[4], (unsigned long long)pushed);
         if (capped) atomicAdd(&ctx.counters[1], (unsigned long long)capped);
         if (ov) atomicAdd(&ctx.counters[2], (unsigned long long)ov);
     }
@@ -281,6 +287,9 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
     if (F == 0) return OCL_GB300_OK;
     if (m.n > 0) {
         int st = ensure_push_index(m, dir);
+        bool bull = cp.kind == OCL_CUTTER_BULL;
+        for (int k = 0; k < cp.nsub && cp.kind == OCL_CUTTER_COMPOSITE; ++k) bull = bull || cp.sub[k].kind == OCL_CUTTER_BULL;
+        if (!st && bull) st = ensure_edge_sin(m);
         if (st) return st;
     }
     cudaEvent_t e0, e1;
@@ -289,7 +298,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
     DevBuf<double> dfib(6 * F);
     DevBuf<uint32_t> dcounts(F);
     DevBuf<uint64_t> doffs(F);
-    DevBuf<unsigned long long> dcnt(4);
+    DevBuf<unsigned long long> dcnt(5);
     DevBuf<PushCtx> dctx(1);
     if (!dfib.ok() || !dcounts.ok() || !doffs.ok() || !dcnt.ok() || !dctx.ok()) return OCL_GB300_OOM;
     CK(cudaMemcpy(dfib.p, fibers, 6 * F * sizeof(double), cudaMemcpyHostToDevice));
@@ -297,7 +306,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
     std::vector<PushRec> hrec;
     std::vector<uint32_t> hcounts(F);
     std::vector<uint64_t> hoffs(F);
-    unsigned long long hc[4] = {0, 0, 0, 0};
+    unsigned long long hc[5] = {0, 0, 0, 0, 0};
     float ms = 0;
     unsigned long long second_overflow = 0;
     for (int attempt = 0; attempt < 3; ++attempt) {
@@ -308,6 +317,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
         h.cp = cp;
         h.dir = dir;
         h.t64 = m.d_t64;
+        h.esin = m.d_edge_sin;
         h.nodes = m.n > 0 ? m.push[dir].d_nodes : nullptr;
         h.order = m.n > 0 ? m.push[dir].d_order : nullptr;
         h.fib = dfib.p;
@@ -319,7 +329,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
         h.offs = doffs.p;
         h.counters = dcnt.p;
         CK(cudaMemcpy(dctx.p, &h, sizeof(h), cudaMemcpyHostToDevice));
-        CK(cudaMemset(dcnt.p, 0, 4 * sizeof(unsigned long long)));
+        CK(cudaMemset(dcnt.p, 0, 5 * sizeof(unsigned long long)));
         const unsigned warps = (unsigned)((F + 31) / 32);
         CK(cudaEventRecord(e0));
         k_push<<<(warps + 3) / 4, 128>>>(dctx.p, nullptr, 0, nullptr);
@@ -363,6 +373,8 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->pairs = hc[0];
+        stats->screened = hc[0];
+        stats->refined = hc[4];
         stats->iter_limit_hits = hc[1];
         stats->kernel_ms = ms;
     }

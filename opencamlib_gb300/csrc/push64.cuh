@@ -370,7 +370,10 @@ __device__ inline double brent_aell(double a, double b, const AEll& E, int* capp
     return b;
 }
 
-__device__ inline bool bull_edge_push(const BasicP& c, const Fib64& f, Ival64& i, D3 p1, D3 p2, int* capped) {
+// sin_theta: sin(atan(dz / xy length)) of the edge, computed on the host
+// (Mesh::d_edge_sin).
+__device__ inline bool bull_edge_push(const BasicP& c, const Fib64& f, Ival64& i, D3 p1, D3 p2, double sin_theta,
+                                      int* capped) {
     bool result = false;
     if (zero_tol(xynorm(p2 - p1))) return false;
     if (zero_tol(p2.z - p1.z)) return false;
@@ -381,8 +384,7 @@ __device__ inline bool bull_edge_push(const BasicP& c, const Fib64& f, Ival64& i
     major.z = 0;
     E.major = xynormalize(major);
     E.minor = xyperp(E.major);
-    double theta = atan((p2.z - p1.z) / xynorm(p2 - p1));
-    E.a = fabs(c.radius2 / sin(theta));
+    E.a = fabs(c.radius2 / sin_theta);
     E.b = c.radius2;
     E.offset = c.radius1;
     // aligned_solver
@@ -499,7 +501,8 @@ __device__ inline bool cone_edge_push(const BasicP& c, const Fib64& f, Ival64& i
     return result;
 }
 
-__device__ inline bool edge_push_basic(const BasicP& c, const Fib64& f, Ival64& i, const Tri64& t, int* capped) {
+__device__ inline bool edge_push_basic(const BasicP& c, const Fib64& f, Ival64& i, const Tri64& t, const double* esin,
+                                       int* capped) {
     bool result = false;
     for (int n = 0; n < 3; ++n) {
         D3 p1 = tri_p(t, n), p2 = tri_p(t, (n + 1) % 3);
@@ -509,7 +512,7 @@ __device__ inline bool edge_push_basic(const BasicP& c, const Fib64& f, Ival64& 
             if (shaft_edge_push(c, f, i, p1, p2)) r = true;
             bool g = false;
             if (c.kind == OCL_CUTTER_BALL) g = ball_edge_push(c, f, i, p1, p2);
-            else if (c.kind == OCL_CUTTER_BULL) g = bull_edge_push(c, f, i, p1, p2, capped);
+            else if (c.kind == OCL_CUTTER_BULL) g = bull_edge_push(c, f, i, p1, p2, esin[n], capped);
             else if (c.kind == OCL_CUTTER_CONE) g = cone_edge_push(c, f, i, p1, p2);
             if (g) r = true;
         }
@@ -526,7 +529,8 @@ __device__ __forceinline__ int height_index(const CutterP& c, double h) {
 
 // CompositeCutter vertex/facet/edge push: per sub-cutter on a shifted fiber,
 // keep endpoints whose CC height belongs to that sub-cutter.
-__device__ inline void comp_push(const CutterP& c, const Fib64& f, Ival64& i, const Tri64& t, int which, int* capped) {
+__device__ inline void comp_push(const CutterP& c, const Fib64& f, Ival64& i, const Tri64& t, const double* esin,
+                                 int which, int* capped) {
     double ct[2 * OCL_GB300_MAX_SUB];
     CCp cc[2 * OCL_GB300_MAX_SUB];
     int nc = 0;
@@ -540,7 +544,7 @@ __device__ inline void comp_push(const CutterP& c, const Fib64& f, Ival64& i, co
         bool hit;
         if (which == 0) hit = vertex_push_basic(s, cf, ci, t);
         else if (which == 1) hit = facet_push_basic(s, cf, ci, t);
-        else hit = edge_push_basic(s, cf, ci, t, capped);
+        else hit = edge_push_basic(s, cf, ci, t, esin, capped);
         if (hit) {
             if (n == height_index(c, ci.ucc.p.z - f.p1.z)) { ct[nc] = ci.upper; cc[nc] = ci.ucc; ++nc; }
             if (n == height_index(c, ci.lcc.p.z - f.p1.z)) { ct[nc] = ci.lower; cc[nc] = ci.lcc; ++nc; }
@@ -549,16 +553,18 @@ __device__ inline void comp_push(const CutterP& c, const Fib64& f, Ival64& i, co
     for (int k = 0; k < nc; ++k) iv_update(i, ct[k], cc[k]);
 }
 
-__device__ inline void push_triangle64(const CutterP& c, const Fib64& f, Ival64& i, const Tri64& t, int* capped) {
+// esin: the triangle's three edge slopes (Mesh::d_edge_sin)
+__device__ inline void push_triangle64(const CutterP& c, const Fib64& f, Ival64& i, const Tri64& t, const double* esin,
+                                       int* capped) {
     if (c.kind == OCL_CUTTER_COMPOSITE) {
-        comp_push(c, f, i, t, 0, capped);
-        comp_push(c, f, i, t, 1, capped);
-        comp_push(c, f, i, t, 2, capped);
+        comp_push(c, f, i, t, esin, 0, capped);
+        comp_push(c, f, i, t, esin, 1, capped);
+        comp_push(c, f, i, t, esin, 2, capped);
         return;
     }
     vertex_push_basic(c.b, f, i, t);
     facet_push_basic(c.b, f, i, t);
-    edge_push_basic(c.b, f, i, t, capped);
+    edge_push_basic(c.b, f, i, t, esin, capped);
 }
 
 }  // namespace oclg

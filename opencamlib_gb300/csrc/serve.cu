@@ -10,9 +10,14 @@
 //     device-memory budget (inputs, outputs and batch workspace); a request
 //     that could never fit is rejected when it is submitted;
 //   * continuous batching: a request that arrives while others run joins the
-//     next batch to form; an adaptive path request contributes one
-//     bisection level per batch and goes back to the head of the queue for
-//     its next level, so its levels overlap with other requests' work;
+//     next batch to form; a batch holds at most `max_batch_points` CL points,
+//     so batches stay short and a request never waits long for the next
+//     one; a drop request larger than what is left in a batch contributes a
+//     piece of its points and goes to the back of the queue for the rest
+//     (large requests share the GPU round robin with the ones behind them);
+//     an adaptive path request contributes one bisection level per
+//     batch and goes back to the head of the queue for its next level, so
+//     its levels overlap with other requests' work;
 //   * each request's latency is the time from submission to the completion
 //     of its last batch; the server keeps p50 / p99 over completed requests.
 // The device work of a request is the same as that of the single-request
@@ -74,14 +79,18 @@ struct Request {
     bool cancel = false;
     int batches = 0;
     uint64_t points = 0;
+    uint64_t done = 0;  // drop: points already dispatched to finished batches
     Clock::time_point submitted, started, finished;
-    uint64_t step_points() const { return kind == KIND_DROP ? M : run.points().size() / 3; }
-    const double* step_cl() const { return kind == KIND_DROP ? cl : run.points().data(); }
+    // points of the request's next step: a drop's remaining points, an
+    // adaptive request's next bisection level
+    uint64_t step_points() const { return kind == KIND_DROP ? M - done : run.points().size() / 3; }
+    const double* step_cl() const { return kind == KIND_DROP ? cl + 3 * done : run.points().data(); }
 };
 
 struct Item {
     Request* r;
-    uint64_t off, n;
+    uint64_t off, n;  // the item's points in the slot's buffers
+    uint64_t src;     // drop: first point of the piece in the request
 };
 
 struct Slot {
@@ -105,7 +114,8 @@ struct Slot {
 struct Server {
     ocl_gb300_server_opts opts{};
     int device = 0;
-    uint64_t slot_points = 0;  // most CL points one batch takes
+    uint64_t slot_points = 0;  // most CL points one batch takes (the budget's share and max_batch_points)
+    uint64_t io_points = 0;    // most CL points the budget's share holds (an adaptive level must fit)
     std::vector<Mesh*> meshes;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -173,22 +183,26 @@ void Server::complete(Request* r, int status) {
 bool Server::launch(Slot& s) {
     s.items.clear();
     s.points = 0;
-    while (!pending.empty() && (int)s.items.size() < opts.max_batch_requests) {
+    while (!pending.empty() && (int)s.items.size() < opts.max_batch_requests && s.points < slot_points) {
         Request* r = pending.front();
         if (r->cancel) {
             pending.pop_front();
             complete(r, OCL_GB300_CANCELLED);
             continue;
         }
-        const uint64_t n = r->step_points();
-        if (!s.items.empty() && s.points + n > slot_points) break;
+        uint64_t n = r->step_points();
+        if (r->kind == KIND_DROP) {
+            n = std::min(n, slot_points - s.points);  // a piece; the rest in later batches
+        } else if (!s.items.empty() && s.points + n > slot_points) {
+            break;  // an adaptive level is not split
+        }
         pending.pop_front();
         if (!r->admitted) {
             r->admitted = true;
             r->started = Clock::now();
         }
         r->in_flight = true;
-        s.items.push_back({r, s.points, n});
+        s.items.push_back({r, s.points, n, r->kind == KIND_DROP ? r->done : 0});
         s.points += n;
     }
     if (s.items.empty()) return false;
@@ -250,11 +264,19 @@ void Server::finish(Slot& s, bool ok, const std::string& err) {
         }
         if (r->kind == KIND_DROP) {
             for (uint64_t i = 0; i < it->n; ++i) {
-                r->z_out[i] = s.hz[it->off + i];
-                r->type_out[i] = s.hty[it->off + i];
+                r->z_out[it->src + i] = s.hz[it->off + i];
+                r->type_out[it->src + i] = s.hty[it->off + i];
             }
-            std::memcpy(r->cc_out, s.hcc + 3 * it->off, 3 * it->n * sizeof(double));
-            complete(r, OCL_GB300_OK);
+            std::memcpy(r->cc_out + 3 * it->src, s.hcc + 3 * it->off, 3 * it->n * sizeof(double));
+            r->done = it->src + it->n;
+            if (r->done == r->M) {
+                complete(r, OCL_GB300_OK);
+            } else if (r->cancel) {
+                complete(r, OCL_GB300_CANCELLED);
+            } else {
+                r->in_flight = false;
+                pending.push_back(r);  // its next piece after what is queued (round robin)
+            }
             continue;
         }
         r->run.consume(s.hz + it->off, s.hcc + 3 * it->off, s.hty + it->off);
@@ -314,16 +336,18 @@ int server_create(const ocl_gb300_server_opts* o, Server** out) {
     if (s->opts.slots <= 0) s->opts.slots = 2;
     if (s->opts.max_batch_requests <= 0) s->opts.max_batch_requests = 64;
     if (s->opts.list_capacity == 0) s->opts.list_capacity = CAND_K;
+    if (s->opts.max_batch_points == 0) s->opts.max_batch_points = 1 << 18;
     if (s->opts.slots > 16 || s->opts.list_capacity < 16 || s->opts.list_capacity > CAND_K ||
-        s->opts.hbm_budget_bytes < (64ull << 20)) {
-        set_error("server: slots 1..16, list capacity 16..256, budget at least 64 MiB");
+        s->opts.hbm_budget_bytes < (64ull << 20) || s->opts.max_batch_points < 0) {
+        set_error("server: slots 1..16, list capacity 16..256, budget at least 64 MiB, max_batch_points >= 0");
         return OCL_GB300_BAD_ARG;
     }
     CK(cudaGetDevice(&s->device));
     // each slot: a quarter of its share for the batch's inputs and outputs,
     // the rest for the batch workspace (chunked into waves by the batch)
     const uint64_t share = s->opts.hbm_budget_bytes / (uint64_t)s->opts.slots;
-    s->slot_points = std::max<uint64_t>(share / 4 / POINT_IO_BYTES, 1);
+    s->slot_points = std::max<uint64_t>(std::min<uint64_t>(share / 4 / POINT_IO_BYTES, s->opts.max_batch_points), 1);
+    const uint64_t io_points = std::max<uint64_t>(share / 4 / POINT_IO_BYTES, 1);
     s->slots.resize(s->opts.slots);
     for (Slot& sl : s->slots) {
         CK(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
@@ -335,6 +359,7 @@ int server_create(const ocl_gb300_server_opts* o, Server** out) {
         const uint64_t chunk = std::max<uint64_t>(1024, std::min<uint64_t>(1ull << 20, ws / (2 * per_point)));
         sl.batch = batch_new(ws, chunk, s->opts.list_capacity);
     }
+    s->io_points = io_points;
     Server* raw = s.release();
     raw->th = std::thread([raw] { raw->loop(); });
     *out = raw;
@@ -381,10 +406,11 @@ static int enqueue_request(Server& s, std::unique_ptr<Request> r, int32_t mesh_i
         set_error("server: the mesh has no triangles");
         return OCL_GB300_BAD_ARG;
     }
-    if (r->step_points() > s.slot_points) {
+    if (r->kind == KIND_ADAPTIVE && r->step_points() > s.io_points) {
         ++s.rejected;
         set_error("server: a request of " + std::to_string(r->step_points()) +
-                  " CL points exceeds what one batch may hold under the budget (" + std::to_string(s.slot_points) + ")");
+                  " CL points per level exceeds what one batch may hold under the budget (" +
+                  std::to_string(s.io_points) + ")");
         return OCL_GB300_OOM;
     }
     r->id = s.next_id++;

@@ -206,6 +206,8 @@ int push_fibers(Mesh& m, const CutterP& cp, int dir, FiberSet& fs, ocl_gb300_sta
                                fs.type.data(), cap, &st);
         if (acc) {
             acc->pairs += st.pairs;
+            acc->screened += st.screened;
+            acc->refined += st.refined;
             acc->iter_limit_hits += st.iter_limit_hits;
             acc->kernel_ms += st.kernel_ms;
             acc->launches += 2;

@@ -382,6 +382,33 @@ def canonical_loops(loops):
     return out
 
 
+def loops_close(a, b, tol):
+    """True when the loop lists a and b are the same cyclic point sequences
+    up to tol per coordinate (any start, any loop order)."""
+    if len(a) != len(b):
+        return False
+    A = sorted((np.asarray(x, dtype=np.float64).reshape(-1, 3) for x in a), key=lambda x: (len(x), x.min(axis=0).round(6).tolist()))
+    B = sorted((np.asarray(x, dtype=np.float64).reshape(-1, 3) for x in b), key=lambda x: (len(x), x.min(axis=0).round(6).tolist()))
+    used = [False] * len(B)
+    for x in A:
+        found = False
+        for j, y in enumerate(B):
+            if used[j] or len(y) != len(x):
+                continue
+            if len(x) == 0:
+                found = True
+            for r in np.nonzero(np.all(np.abs(x - y[0]) <= tol, axis=1))[0]:
+                if np.all(np.abs(np.roll(x, -int(r), axis=0) - y) <= tol):
+                    found = True
+                    break
+            if found:
+                used[j] = True
+                break
+        if not found:
+            return False
+    return True
+
+
 def ref_preset_fields(preset: int, args):
     L = _lib("ref")
     a = _d(list(args) + [0.0] * (4 - len(args)))

@@ -117,9 +117,11 @@ def test_injected_failures(env):
     with pytest.raises(ocl.OclError) as e:
         srv.submit_drop(mid + 7, c, w.raster(10, 10, 1.0))
     assert e.value.status == _abi.BAD_ARG
-    # more points than one batch may hold under a 64 MiB budget
+    # an adaptive request whose first level holds more points than one
+    # batch's buffers may under a 64 MiB budget (drops are split instead)
+    many = np.array([[0, 5.0 + 1e-4 * k, 5.0, -60.0, 5.0 + 1e-4 * k, 95.0, -60.0, 0, 0, 0, 0] for k in range(200000)])
     with pytest.raises(ocl.OclError) as e:
-        srv.submit_drop(mid, c, w.raster(1000, 1000, 0.1))
+        srv.submit_adaptive(mid, c, many, 1.0, 0.1)
     assert e.value.status == _abi.OOM
     # a cancelled request (admission paused so it is still queued)
     srv.pause(True)
@@ -140,4 +142,29 @@ def test_injected_failures(env):
     assert srv.wait(late)[0] == _abi.OK
     s = srv.stats()
     assert s["rejected"] == 2 and s["cancelled"] == 1 and s["completed"] == 2
+    srv.close()
+
+
+def test_large_drop_split_over_batches(env):
+    """A drop request larger than a batch goes through in pieces; each
+    piece's points equal the request run alone, and a small request that
+    arrives meanwhile finishes before the large one."""
+    ocl, meshes = env
+    c = cu.BullCutter(8.0, 1.5, 20.0)
+    big = w.raster(200, 150, 0.5, z0=-60.0, x0=2.0, y0=3.0)
+    small = w.raster(10, 10, 5.0, z0=-60.0, x0=7.0, y0=9.0)
+    srv = ocl.Server(hbm_budget_bytes=2 << 30, slots=1, max_batch_points=4096)
+    mid = srv.add_mesh(meshes[2])
+    hb = srv.submit_drop(mid, c, big)
+    hs = srv.submit_drop(mid, c, small)
+    st, res_b, info_b = srv.wait(hb)
+    assert st == _abi.OK
+    st, res_s, info_s = srv.wait(hs)
+    assert st == _abi.OK
+    assert info_b["batches"] >= len(big) // 4096
+    assert info_s["latency_ms"] < info_b["latency_ms"]  # the small one did not wait for all of the large one
+    for a, b in zip(res_b, meshes[2].drop(c, big, precision="mixed")[:3]):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(res_s, meshes[2].drop(c, small, precision="mixed")[:3]):
+        np.testing.assert_array_equal(a, b)
     srv.close()

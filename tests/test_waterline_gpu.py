@@ -1,9 +1,11 @@
 """Waterline and AdaptiveWaterline on the GPU (ocl_gb300_waterline,
 _levels, _adaptive_waterline): fibers pushed on the device, woven on the
 host.  Checked against the reference's own Waterline::run and
-AdaptiveWaterline::run stored in the golden fixtures (fibers bit for bit,
-loops as cyclic point sequences), and, at a larger size, against the
-oracle's push fibers woven by the same host weave."""
+AdaptiveWaterline::run stored in the golden fixtures (made on another
+machine, whose libm's atan and sin may round a bull edge's slope
+differently in the last bit: interval ends within 1e-7 mm, loops the same
+cyclic point sequences within 1e-7 mm), and bit for bit against the oracle
+port run here (same fibers pushed on the host, woven by the same weave)."""
 import numpy as np
 import pytest
 
@@ -35,13 +37,22 @@ def golden_loops(g, key):
     return [pts[off[k]:off[k + 1]] for k in range(len(off) - 1)]
 
 
-def check_against(g, key, res):
-    assert same_loops(res.loops, golden_loops(g, key)), key
+def check_against(g, key, res, tris, cutter):
+    fibers = []
     for d in (0, 1):
         fib, off, iv, _, _ = res.fibers(d)
         np.testing.assert_array_equal(fib, g[f"{key}_f{d}"], err_msg=key)
         np.testing.assert_array_equal(off.astype(np.int64), g[f"{key}_o{d}"], err_msg=key)
-        np.testing.assert_array_equal(iv, g[f"{key}_i{d}"], err_msg=key)
+        ext = np.abs(fib[:, 3:5] - fib[:, 0:2]).max()  # fiber length: t to mm
+        assert np.abs(iv - g[f"{key}_i{d}"]).max(initial=0.0) * ext <= 1e-7, key
+        # bit for bit against the oracle port on this machine
+        port, _ = checker.push(tris, cutter, d, fib, "port")
+        np.testing.assert_array_equal(off.astype(np.int64), np.cumsum([0] + [len(r) for r in port]), err_msg=key)
+        np.testing.assert_array_equal(iv, np.array([[r[0], r[1]] for rr in port for r in rr]).reshape(-1, 2),
+                                      err_msg=key)
+        fibers.append((fib, off, iv))
+    assert checker.loops_close(res.loops, golden_loops(g, key), 1e-7), key
+    assert same_loops(res.loops, _native.weave(*fibers).loops), key
 
 
 @pytest.mark.parametrize("name", ["heightfield", "sphere_on_plate"])
@@ -53,7 +64,7 @@ def test_waterline_matches_reference(ocl, name):
         c = CUTTERS[cname]()
         for k, z in enumerate(g["zs"]):
             res, st = mesh.waterline(c, float(z), float(g["sampling"]))
-            check_against(g, f"{cname}_wl_{k}", res)
+            check_against(g, f"{cname}_wl_{k}", res, g["tris"], c)
             assert st.iter_limit_hits == 0
 
 
@@ -66,7 +77,7 @@ def test_adaptive_waterline_matches_reference(ocl, name):
         c = CUTTERS[cname]()
         for k, z in enumerate(g["zs"]):
             res, _ = mesh.adaptive_waterline(c, float(z), float(g["sampling"]), float(g["min_sampling"]))
-            check_against(g, f"{cname}_awl_{k}", res)
+            check_against(g, f"{cname}_awl_{k}", res, g["tris"], c)
 
 
 def test_levels_equal_single_heights(ocl):
