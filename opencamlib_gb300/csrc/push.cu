@@ -88,14 +88,93 @@ __device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap)
     return true;
 }
 
+// The prefilter of one (fiber, candidate) pair: false when the candidate's
+// push interval is provably empty or strictly inside an interval the fiber
+// holds (Fiber::addInterval ignores such an interval), so leaving it out
+// changes nothing.  The KD walk accepts whole leaves; every push contact lies
+// on the cutter's surface: within the radius of the axis and no lower than
+// the profile height at its distance.  A triangle farther than the radius
+// from the fiber's line, or entirely below the profile at its nearest
+// distance, has an empty interval.
+struct FiberGeom {
+    bool xf;         // X fiber
+    double r;        // cutter radius
+    double cr;       // the fiber's fixed coordinate across (y of an X fiber)
+    double z;        // its height
+    double f0, finv; // along-coordinate of p1, 1 / length (0: degenerate)
+};
+
+__device__ __forceinline__ bool push_needed(const CutterP& cp, const FiberGeom& g, const Tri64& t, const Ival64* ints,
+                                            int n, bool overflow) {
+    double halfw = g.r;  // how far along the fiber the axis can be from the triangle
+    {
+        const double lo = g.xf ? t.bb[2] : t.bb[0], hi = g.xf ? t.bb[3] : t.bb[1];
+        const double gap = fmax(lo - g.cr, g.cr - hi);
+        const double mg = 1e-9 * (1.0 + fabs(g.cr) + g.r + fabs(g.z));
+        if (gap > g.r + mg) return false;
+        const double hmin = gap > mg ? height_any(cp, fmin(gap - mg, g.r)) : 0.0;
+        if (t.bb[5] < g.z + fmax(hmin, 0.0) - mg) return false;
+        // a contact at distance q across the fiber and height h above the tip
+        // lies within sqrt(r^2 - q^2), and within the cutter's width at h, of
+        // the axis
+        const double gg = fmax(gap - mg, 0.0);
+        halfw = sqrt(fmax(g.r * g.r - gg * gg, 0.0));
+        if (cp.kind != OCL_CUTTER_COMPOSITE) {
+            const double wz = width_basic(cp.b, t.bb[5] - g.z + mg);
+            if (wz >= 0.0) halfw = fmin(halfw, wz);
+        }
+        halfw += mg;
+    }
+    if (n > 0 && !overflow && g.finv != 0.0) {
+        double a = ((g.xf ? t.bb[0] : t.bb[2]) - halfw - g.f0) * g.finv;
+        double b = ((g.xf ? t.bb[1] : t.bb[3]) + halfw - g.f0) * g.finv;
+        if (a > b) {
+            const double s = a;
+            a = b;
+            b = s;
+        }
+        a -= 1e-9 * (1.0 + fabs(a));
+        b += 1e-9 * (1.0 + fabs(b));
+        for (int q = 0; q < n; ++q)
+            if (a > ints[q].lower && b < ints[q].upper) return false;
+    }
+    return true;
+}
+
+// Per-warp shared state of k_push.
+constexpr int PUSH_CHUNK = 32;  // candidates buffered per warp before they are screened and pushed
+struct PushWarp {
+    uint2 stack[KD_STACK];
+    uint32_t tri[PUSH_CHUNK];   // buffered candidates (device triangle ids), in the KD visit order
+    uint32_t msk[PUSH_CHUNK];   // lanes whose search reached each candidate
+    unsigned pm[PUSH_CHUNK];    // lanes that must push each candidate
+    int po[PUSH_CHUNK + 1];     // pairs before each candidate
+    Fib64 fib[32];              // the lanes' fibers
+    Ival64 res[32];             // one round of pushed intervals
+    int owner[32];              // their lanes
+};
+
 // list == nullptr: fibers 0..F-1 with the intervals in local memory;
 // otherwise the listed fibers with PUSH_CAP_BIG intervals each in scratch.
+//
+// A warp walks the KD tree for its 32 fibers (lanes) together and buffers
+// the candidates it reaches, with the lanes that reached each, 32 at a time.
+// Each lane then screens its own fiber against the buffered candidates
+// (push_needed, against the intervals it held when the chunk began: they
+// only grow, so what is inside them stays inside).  The (lane, candidate)
+// pairs that must be pushed are spread over all lanes, one FP64 push per lane
+// per round, in candidate-major order; after each round every lane merges its
+// own pushed intervals into its fiber in candidate order with
+// Fiber::addInterval's rules.  So every fiber sees every candidate's interval
+// in the reference's order, and intervals strictly inside one it holds are
+// ignored exactly as the reference ignores them.
 __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, const uint32_t* __restrict__ list,
                                               int nlist, Ival64* __restrict__ scratch) {
     const PushCtx& ctx = *ctxp;
-    __shared__ uint2 s_stack[4][KD_STACK];
+    __shared__ PushWarp s_warp[4];
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
+    PushWarp& W = s_warp[wl];
     const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
     const int count = list ? nlist : ctx.F;
     if (base >= count) return;
@@ -106,19 +185,23 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     fb.p1 = d3(ctx.fib[6 * f], ctx.fib[6 * f + 1], ctx.fib[6 * f + 2]);
     fb.p2 = d3(ctx.fib[6 * f + 3], ctx.fib[6 * f + 4], ctx.fib[6 * f + 5]);
     fb.dir = normalize3(fb.p2 - fb.p1);  // Fiber::calcDir (fiber.cpp:35-39)
+    W.fib[lane] = fb;
     const double r = ctx.cp.radius;
     // pushCutter3's search point and KDTree::search_cutter_overlap box
     double clx, cly;
     if (ctx.dir == OCL_GB300_XFIBER) { clx = 0; cly = fb.p1.y; }
     else { clx = fb.p1.x; cly = 0; }
     const double bb[6] = {clx - r, clx + r, cly - r, cly + r, fb.p1.z, fb.p1.z + ctx.cp.length};
-    // a triangle's interval lies where the cutter's axis passes within the
-    // cutter radius of the triangle's bbox: [bb_min - r, bb_max + r] along the
-    // fiber, in fiber parameter units (with a margin for rounding)
-    const bool xf = ctx.dir == OCL_GB300_XFIBER;
-    const double f0 = xf ? fb.p1.x : fb.p1.y;
-    const double fl = xf ? fb.p2.x - fb.p1.x : fb.p2.y - fb.p1.y;
-    const double finv = fl != 0.0 ? 1.0 / fl : 0.0;
+    FiberGeom geo;
+    geo.xf = ctx.dir == OCL_GB300_XFIBER;
+    geo.r = r;
+    geo.cr = geo.xf ? fb.p1.y : fb.p1.x;
+    geo.z = fb.p1.z;
+    geo.f0 = geo.xf ? fb.p1.x : fb.p1.y;
+    {
+        const double fl = geo.xf ? fb.p2.x - fb.p1.x : fb.p2.y - fb.p1.y;
+        geo.finv = fl != 0.0 ? 1.0 / fl : 0.0;
+    }
     Ival64 local_ints[PUSH_CAP];
     Ival64* ints = list ? scratch + (size_t)slot * PUSH_CAP_BIG : local_ints;
     const int cap = list ? PUSH_CAP_BIG : PUSH_CAP;
@@ -127,14 +210,59 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     unsigned long long calls = 0;
     unsigned pushed = 0;
     int capped = 0;
-    uint2* st = s_stack[wl];
+    uint2* st = W.stack;
     const unsigned amask = __ballot_sync(0xffffffffu, active);
     int sp = 0;
+    int nc = 0;  // buffered candidates (warp-uniform)
     if (ctx.nodes && amask) {
         if (lane == 0) st[0] = make_uint2(0u, amask);
         sp = 1;
     }
     __syncwarp();
+    // screens, pushes and merges the buffered candidates (warp-collective)
+    auto flush = [&]() {
+        unsigned need = 0;
+        for (int c = 0; c < nc; ++c) {
+            if (!((W.msk[c] >> lane) & 1u)) continue;
+            ++calls;
+            if (push_needed(ctx.cp, geo, ctx.t64[W.tri[c]], ints, n, overflow)) need |= 1u << c;
+        }
+        int tot = 0;
+        for (int c = 0; c < nc; ++c) {
+            const unsigned m = __ballot_sync(0xffffffffu, (need >> c) & 1u);
+            if (lane == 0) {
+                W.pm[c] = m;
+                W.po[c] = tot;
+            }
+            tot += __popc(m);
+        }
+        if (lane == 0) W.po[nc] = tot;
+        __syncwarp();
+        for (int b0 = 0; b0 < tot; b0 += 32) {
+            const int q = b0 + lane;
+            int own = -1;
+            if (q < tot) {
+                int c = 0;  // the last candidate with po[c] <= q (it has pairs)
+                for (int s = 16; s > 0; s >>= 1)
+                    if (c + s < nc && W.po[c + s] <= q) c += s;
+                own = (int)__fns(W.pm[c], 0, q - W.po[c] + 1);
+                const uint32_t ti = W.tri[c];
+                Ival64 iv;
+                iv_init(iv);
+                push_triangle64(ctx.cp, W.fib[own], iv, ctx.t64[ti], ctx.esin ? ctx.esin + 3 * (size_t)ti : nullptr,
+                                &capped);
+                W.res[lane] = iv;
+                ++pushed;
+            }
+            W.owner[lane] = own;
+            __syncwarp();
+            const int nr = min(32, tot - b0);
+            for (int j = 0; j < nr; ++j)
+                if (W.owner[j] == lane && !overflow && !fiber_add(ints, n, W.res[j], cap)) overflow = true;
+            __syncwarp();
+        }
+        nc = 0;
+    };
     while (sp > 0) {
         --sp;
         const uint2 e = st[sp];
@@ -143,66 +271,17 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         const bool in = (e.y >> lane) & 1u;
         if (nd.leaf_begin >= 0) {
             for (int k = nd.leaf_begin; k < nd.leaf_end; ++k) {
-                if (!in) continue;
-                const int32_t ti = ctx.order[k];
-                const Tri64& t = ctx.t64[ti];
-                double halfw = r;  // how far along the fiber the axis can be from the triangle
-                // the KD walk accepts whole leaves; every push contact lies on the
-                // cutter's surface: within the radius of the axis and no lower
-                // than the profile height at its distance.  A triangle farther
-                // than the radius from the fiber's line, or entirely below the
-                // profile at its nearest distance, has an empty interval.
-                {
-                    const double cr = xf ? fb.p1.y : fb.p1.x;
-                    const double lo = xf ? t.bb[2] : t.bb[0], hi = xf ? t.bb[3] : t.bb[1];
-                    const double gap = fmax(lo - cr, cr - hi);
-                    const double mg = 1e-9 * (1.0 + fabs(cr) + r + fabs(fb.p1.z));
-                    if (gap > r + mg) {
-                        ++calls;
-                        continue;
-                    }
-                    const double hmin = gap > mg ? height_any(ctx.cp, fmin(gap - mg, r)) : 0.0;
-                    if (t.bb[5] < fb.p1.z + fmax(hmin, 0.0) - mg) {
-                        ++calls;
-                        continue;
-                    }
-                    // a contact at distance q across the fiber and height h above
-                    // the tip lies within sqrt(r^2 - q^2), and within the
-                    // cutter's width at h, of the axis
-                    const double g = fmax(gap - mg, 0.0);
-                    halfw = sqrt(fmax(r * r - g * g, 0.0));
-                    if (ctx.cp.kind != OCL_CUTTER_COMPOSITE) {
-                        const double wz = width_basic(ctx.cp.b, t.bb[5] - fb.p1.z + mg);
-                        if (wz >= 0.0) halfw = fmin(halfw, wz);
-                    }
-                    halfw += mg;
+                if (lane == 0) {
+                    W.tri[nc] = (uint32_t)ctx.order[k];
+                    W.msk[nc] = e.y;
                 }
-                if (n > 0 && !overflow && finv != 0.0) {
-                    // Fiber::addInterval ignores an interval strictly inside one
-                    // it holds: pass over triangles whose bound already is
-                    double a = ((xf ? t.bb[0] : t.bb[2]) - halfw - f0) * finv;
-                    double b = ((xf ? t.bb[1] : t.bb[3]) + halfw - f0) * finv;
-                    if (a > b) {
-                        const double s = a;
-                        a = b;
-                        b = s;
-                    }
-                    a -= 1e-9 * (1.0 + fabs(a));
-                    b += 1e-9 * (1.0 + fabs(b));
-                    bool inside = false;
-                    for (int q = 0; q < n && !inside; ++q) inside = a > ints[q].lower && b < ints[q].upper;
-                    if (inside) {
-                        ++calls;
-                        continue;
-                    }
+                ++nc;
+                if (nc == PUSH_CHUNK) {
+                    __syncwarp();
+                    flush();
                 }
-                Ival64 iv;
-                iv_init(iv);
-                ++pushed;
-                push_triangle64(ctx.cp, fb, iv, t, ctx.esin ? ctx.esin + 3 * (size_t)ti : nullptr, &capped);
-                if (!overflow && !fiber_add(ints, n, iv, cap)) overflow = true;
-                ++calls;
             }
+            __syncwarp();
             continue;
         }
         bool vh, vl;
@@ -222,6 +301,10 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         }
         sp += (ml ? 1 : 0) + (mh ? 1 : 0);
         __syncwarp();
+    }
+    if (nc > 0) {
+        __syncwarp();
+        flush();
     }
     // reserve output slots for the warp
     int cnt = active ? n : 0;

@@ -18,6 +18,10 @@
 //     an adaptive path request contributes one bisection level per
 //     batch and goes back to the head of the queue for its next level, so
 //     its levels overlap with other requests' work;
+//   * with two or more slots the first is a fast lane on a high-priority
+//     stream: it takes only adaptive levels and drops (or pieces left) of at
+//     most 16,384 points, so an adaptive request's next level does not wait
+//     behind large drops, whose batches run on the other slots;
 //   * each request's latency is the time from submission to the completion
 //     of its last batch; the server keeps p50 / p99 over completed requests.
 // The device work of a request is the same as that of the single-request
@@ -107,7 +111,12 @@ struct Slot {
     std::vector<Item> items;
     uint64_t points = 0;
     bool busy = false;
+    bool fast = false;  // takes adaptive levels and small drops only, on a high-priority stream
 };
+
+// drop requests (or their remaining pieces) of at most this many points may
+// go through the fast slot
+constexpr uint64_t FAST_POINTS = 16384;
 
 }  // namespace
 
@@ -183,20 +192,26 @@ void Server::complete(Request* r, int status) {
 bool Server::launch(Slot& s) {
     s.items.clear();
     s.points = 0;
-    while (!pending.empty() && (int)s.items.size() < opts.max_batch_requests && s.points < slot_points) {
-        Request* r = pending.front();
+    for (auto it = pending.begin();
+         it != pending.end() && (int)s.items.size() < opts.max_batch_requests && s.points < slot_points;) {
+        Request* r = *it;
         if (r->cancel) {
-            pending.pop_front();
+            it = pending.erase(it);
             complete(r, OCL_GB300_CANCELLED);
             continue;
         }
         uint64_t n = r->step_points();
+        // the fast slot takes adaptive levels and small drops only
+        if (s.fast && r->kind == KIND_DROP && n > FAST_POINTS) {
+            ++it;
+            continue;
+        }
         if (r->kind == KIND_DROP) {
             n = std::min(n, slot_points - s.points);  // a piece; the rest in later batches
         } else if (!s.items.empty() && s.points + n > slot_points) {
             break;  // an adaptive level is not split
         }
-        pending.pop_front();
+        it = pending.erase(it);
         if (!r->admitted) {
             r->admitted = true;
             r->started = Clock::now();
@@ -349,8 +364,15 @@ int server_create(const ocl_gb300_server_opts* o, Server** out) {
     s->slot_points = std::max<uint64_t>(std::min<uint64_t>(share / 4 / POINT_IO_BYTES, s->opts.max_batch_points), 1);
     const uint64_t io_points = std::max<uint64_t>(share / 4 / POINT_IO_BYTES, 1);
     s->slots.resize(s->opts.slots);
-    for (Slot& sl : s->slots) {
-        CK(cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking));
+    int prio_low = 0, prio_high = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+    for (size_t k = 0; k < s->slots.size(); ++k) {
+        Slot& sl = s->slots[k];
+        // with two or more slots the first is the fast one: its batches (the
+        // next bisection level of every adaptive request in flight, small
+        // drops) are short and its stream's blocks go first on the SMs
+        sl.fast = s->slots.size() >= 2 && k == 0;
+        CK(cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.fast ? prio_high : prio_low));
         CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
         // chunks small enough that a wave of two fits the workspace (about
         // 70 bytes per point plus 12 per list entry plus a bull edge plan)
