@@ -14,6 +14,8 @@
 #include <vector>
 
 #include "drop.cuh"
+#include "drop_util.cuh"
+#include "geom32.cuh"
 #include "push64.cuh"
 #include "util.cuh"
 
@@ -29,9 +31,23 @@ struct PushRec {
 };
 static_assert(sizeof(PushRec) == 72, "PushRec layout");
 
+constexpr int WUB_N = 256;  // entries of the cutter width upper-bound table
+
 struct PushCtx {
     CutterP cp;
     int dir;
+    // FP32 prefilter: grid entries (bbox local to the origin, rounded
+    // outward, max z rounded up), the origin, the error budget of local FP32
+    // coordinates, a lower bound of the cutter's height at each radius and an
+    // upper bound of its width at each height
+    const Entry* ent;
+    double ox, oy, oz;
+    float E;
+    float R, inv_rstep;     // hlb: height lower bound at radius >= k R / HLB_N
+    float inv_hstep;        // wub: width upper bound at heights <= (k + 1) H / WUB_N
+    bool use_wub;           // basic cutters (the composite's width bound is R)
+    float hlb[HLB_N];
+    float wub[WUB_N];
     const Tri64* t64;
     const double* esin;  // edge slopes, 3 per triangle
     const KDNodeD* nodes;
@@ -88,14 +104,62 @@ __device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap)
     return true;
 }
 
+// The fiber in the FP32 frame of the prefilter.
+struct FiberGeom32 {
+    float cr;     // across coordinate, local to the origin
+    float z;      // height, local
+    float f0;     // along coordinate of p1, local
+    float finv;   // 1 / length along (0: degenerate)
+    float tmarg;  // error of an along coordinate in t units
+};
+
 // The prefilter of one (fiber, candidate) pair: false when the candidate's
 // push interval is provably empty or strictly inside an interval the fiber
 // holds (Fiber::addInterval ignores such an interval), so leaving it out
-// changes nothing.  The KD walk accepts whole leaves; every push contact lies
-// on the cutter's surface: within the radius of the axis and no lower than
-// the profile height at its distance.  A triangle farther than the radius
-// from the fiber's line, or entirely below the profile at its nearest
-// distance, has an empty interval.
+// changes nothing.  Every push contact lies on the cutter's surface: within
+// the radius of the axis and no lower than the profile height at its
+// distance; so a triangle farther than the radius from the fiber's line, or
+// entirely below the profile at its nearest distance, has an empty interval,
+// and an interval lies within the triangle's along-extent grown by the
+// cutter's half-width at the triangle's distance and height.  Evaluated in
+// FP32 on the grid entries, every bound taken outward by the error budget E
+// of the local frame (entry bboxes rounded outward, fiber coordinates rounded
+// to nearest, each FP32 operation's rounding), the cutter's height and width
+// from the conservative tables of PushCtx.
+__device__ __forceinline__ bool push_needed32(const PushCtx& ctx, const FiberGeom32& g, bool xf, const Entry& e,
+                                              const Ival64* ints, int n, bool overflow) {
+    const float E = ctx.E;
+    const float lo = xf ? e.miny : e.minx, hi = xf ? e.maxy : e.maxx;
+    const float gap = fmaxf(lo - g.cr, g.cr - hi);
+    if (gap > ctx.R + E) return false;
+    const float dlb = gap - E;  // the true distance is at least this
+    if (e.maxz < g.z + fmaxf(hlb_at(ctx.hlb, dlb, ctx.inv_rstep), 0.0f) - E) return false;
+    if (n == 0 || overflow || g.finv == 0.0f) return true;
+    const float gl = fmaxf(dlb, 0.0f);
+    float halfw = __fsqrt_ru(fmaxf(__fmaf_ru(-gl, gl, __fmul_ru(ctx.R, ctx.R)), 0.0f));
+    if (ctx.use_wub) {
+        const float hub = __fadd_ru(__fsub_ru(e.maxz, g.z), E);
+        int k = (int)(fmaxf(hub, 0.0f) * ctx.inv_hstep);
+        k = min(k, WUB_N - 1);
+        halfw = fminf(halfw, ctx.wub[k]);
+    }
+    halfw = __fadd_ru(halfw, E);
+    const float alo = xf ? e.minx : e.miny, ahi = xf ? e.maxx : e.maxy;
+    float a = (alo - halfw - g.f0) * g.finv;
+    float b = (ahi + halfw - g.f0) * g.finv;
+    if (a > b) {
+        const float t = a;
+        a = b;
+        b = t;
+    }
+    const double da = (double)a - (double)(g.tmarg + 2.4e-7f * fabsf(a));
+    const double db = (double)b + (double)(g.tmarg + 2.4e-7f * fabsf(b));
+    for (int q = 0; q < n; ++q)
+        if (da > ints[q].lower && db < ints[q].upper) return false;
+    return true;
+}
+
+// The fiber in FP64 (the reference's search box and the FP32 frame's inputs).
 struct FiberGeom {
     bool xf;         // X fiber
     double r;        // cutter radius
@@ -103,43 +167,6 @@ struct FiberGeom {
     double z;        // its height
     double f0, finv; // along-coordinate of p1, 1 / length (0: degenerate)
 };
-
-__device__ __forceinline__ bool push_needed(const CutterP& cp, const FiberGeom& g, const Tri64& t, const Ival64* ints,
-                                            int n, bool overflow) {
-    double halfw = g.r;  // how far along the fiber the axis can be from the triangle
-    {
-        const double lo = g.xf ? t.bb[2] : t.bb[0], hi = g.xf ? t.bb[3] : t.bb[1];
-        const double gap = fmax(lo - g.cr, g.cr - hi);
-        const double mg = 1e-9 * (1.0 + fabs(g.cr) + g.r + fabs(g.z));
-        if (gap > g.r + mg) return false;
-        const double hmin = gap > mg ? height_any(cp, fmin(gap - mg, g.r)) : 0.0;
-        if (t.bb[5] < g.z + fmax(hmin, 0.0) - mg) return false;
-        // a contact at distance q across the fiber and height h above the tip
-        // lies within sqrt(r^2 - q^2), and within the cutter's width at h, of
-        // the axis
-        const double gg = fmax(gap - mg, 0.0);
-        halfw = sqrt(fmax(g.r * g.r - gg * gg, 0.0));
-        if (cp.kind != OCL_CUTTER_COMPOSITE) {
-            const double wz = width_basic(cp.b, t.bb[5] - g.z + mg);
-            if (wz >= 0.0) halfw = fmin(halfw, wz);
-        }
-        halfw += mg;
-    }
-    if (n > 0 && !overflow && g.finv != 0.0) {
-        double a = ((g.xf ? t.bb[0] : t.bb[2]) - halfw - g.f0) * g.finv;
-        double b = ((g.xf ? t.bb[1] : t.bb[3]) + halfw - g.f0) * g.finv;
-        if (a > b) {
-            const double s = a;
-            a = b;
-            b = s;
-        }
-        a -= 1e-9 * (1.0 + fabs(a));
-        b += 1e-9 * (1.0 + fabs(b));
-        for (int q = 0; q < n; ++q)
-            if (a > ints[q].lower && b < ints[q].upper) return false;
-    }
-    return true;
-}
 
 // Per-warp shared state of k_push.
 constexpr int PUSH_CHUNK = 32;  // candidates buffered per warp before they are screened and pushed
@@ -160,7 +187,7 @@ struct PushWarp {
 // A warp walks the KD tree for its 32 fibers (lanes) together and buffers
 // the candidates it reaches, with the lanes that reached each, 32 at a time.
 // Each lane then screens its own fiber against the buffered candidates
-// (push_needed, against the intervals it held when the chunk began: they
+// (push_needed32, against the intervals it held when the chunk began: they
 // only grow, so what is inside them stays inside).  The (lane, candidate)
 // pairs that must be pushed are spread over all lanes, one FP64 push per lane
 // per round, in candidate-major order; after each round every lane merges its
@@ -202,6 +229,12 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         const double fl = geo.xf ? fb.p2.x - fb.p1.x : fb.p2.y - fb.p1.y;
         geo.finv = fl != 0.0 ? 1.0 / fl : 0.0;
     }
+    FiberGeom32 g32;
+    g32.cr = (float)(geo.cr - (geo.xf ? ctx.oy : ctx.ox));
+    g32.z = (float)(geo.z - ctx.oz);
+    g32.f0 = (float)(geo.f0 - (geo.xf ? ctx.ox : ctx.oy));
+    g32.finv = (float)geo.finv;
+    g32.tmarg = 2.0f * ctx.E * fabsf(g32.finv);
     Ival64 local_ints[PUSH_CAP];
     Ival64* ints = list ? scratch + (size_t)slot * PUSH_CAP_BIG : local_ints;
     const int cap = list ? PUSH_CAP_BIG : PUSH_CAP;
@@ -225,7 +258,7 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         for (int c = 0; c < nc; ++c) {
             if (!((W.msk[c] >> lane) & 1u)) continue;
             ++calls;
-            if (push_needed(ctx.cp, geo, ctx.t64[W.tri[c]], ints, n, overflow)) need |= 1u << c;
+            if (push_needed32(ctx, g32, geo.xf, ctx.ent[W.tri[c]], ints, n, overflow)) need |= 1u << c;
         }
         int tot = 0;
         for (int c = 0; c < nc; ++c) {
@@ -346,6 +379,57 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     }
 }
 
+void fill_prof(const CutterP& cp, Prof32& prof, float* hlb, bool& composite);
+
+// The FP32 prefilter's tables and error budget for one call.
+static void fill_push_screen(const Mesh& m, const CutterP& cp, const double* fibers, uint64_t F, PushCtx& h) {
+    h.ent = m.d_entries;
+    h.ox = m.grid.ox;
+    h.oy = m.grid.oy;
+    h.oz = m.grid.oz;
+    Prof32 prof;
+    bool composite = false;
+    fill_prof(cp, prof, h.hlb, composite);
+    const double R = cp.radius;
+    h.R = (float)R;
+    h.inv_rstep = (float)(HLB_N / R);
+    // largest local coordinate of the mesh and of the fibers
+    double maxabs = 0.5 * std::max(m.bb[1] - m.bb[0], std::max(m.bb[3] - m.bb[2], m.bb[5] - m.bb[4])) + R + 1.0;
+    for (uint64_t k = 0; k < F; ++k) {
+        const double* f = fibers + 6 * k;
+        for (int j = 0; j < 2; ++j) {
+            maxabs = std::max(maxabs, std::fabs(f[3 * j] - h.ox) + 1.0);
+            maxabs = std::max(maxabs, std::fabs(f[3 * j + 1] - h.oy) + 1.0);
+            maxabs = std::max(maxabs, std::fabs(f[3 * j + 2] - h.oz) + 1.0);
+        }
+    }
+    h.E = (float)(8.0 * maxabs * std::ldexp(1.0, -24) + 4e-6 * std::max(1.0, R));
+    // width(h) of a basic cutter is non-decreasing in h: the bin's upper end
+    // bounds it from above (the composite's bound is the radius)
+    h.use_wub = !composite;
+    const double H = std::max(cp.length, R);
+    h.inv_hstep = (float)(WUB_N / H);
+    for (int k = 0; k < WUB_N; ++k) {
+        double w = R;
+        if (!composite) {
+            const BasicP& b = cp.b;
+            const double hh = H * (k + 1) / WUB_N;
+            switch (b.kind) {
+            case OCL_CUTTER_CYL: w = b.radius; break;
+            case OCL_CUTTER_BALL: w = hh >= b.radius ? b.radius : std::sqrt(b.radius * b.radius - (b.radius - hh) * (b.radius - hh)); break;
+            case OCL_CUTTER_BULL:
+                w = hh >= b.radius2 ? b.radius
+                                    : b.radius1 + std::sqrt(b.radius2 * b.radius2 - (b.radius2 - hh) * (b.radius2 - hh));
+                break;
+            case OCL_CUTTER_CONE: w = hh < b.center_height ? hh * b.tan_angle : b.radius; break;
+            }
+            w = std::min(w + 1e-6 * (1.0 + R), R + 1e-6 * (1.0 + R));
+        }
+        const float f = (float)w;
+        h.wub[k] = ((double)f >= w) ? f : std::nextafter(f, 3.0e38f);
+    }
+}
+
 int ensure_push_index(Mesh& m, int dir) {
     PushIndex& pi = m.push[dir];
     if (pi.built) return OCL_GB300_OK;
@@ -401,6 +485,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
         h.dir = dir;
         h.t64 = m.d_t64;
         h.esin = m.d_edge_sin;
+        fill_push_screen(m, cp, fibers, F, h);
         h.nodes = m.n > 0 ? m.push[dir].d_nodes : nullptr;
         h.order = m.n > 0 ? m.push[dir].d_order : nullptr;
         h.fib = dfib.p;
