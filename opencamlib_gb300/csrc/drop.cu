@@ -768,11 +768,135 @@ __device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsi
     }
 }
 
+// One handed-back point of a cylinder, ball or bull cutter, by the whole
+// block.  For these cutters a triangle lifts the running height to its own
+// highest contact M_t or not at all, M_t not depending on the running height
+// (liftZ is a strict >; the below test only passes over triangles that
+// cannot lift; no part's contact depends on the height), so the fold over
+// the KD-ordered candidates is the highest M_t, with the CC point of the
+// first triangle in KD order that reaches it (later ones only tie).  Every
+// thread evaluates in FP64 its share of the triangles under the cutter whose
+// FP32 upper bound reaches the fold threshold (the certified lower bound less
+// the guard: a triangle below it cannot give the result), from that
+// threshold, and the block reduces (height, then KD rank): no list, no sort,
+// no capacity limit.
+__device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t i, const ExactShared& S) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const GridP& g = ctx.g;
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
+    const float z0l = __double2float_rd(z0 - g.oz);
+    const float gd = ctx.guard;
+    const float tcut = ctx.blo[i] > NEG_INF32 ? ctx.blo[i] - gd : NEG_INF32;
+    const double t64 = tcut > NEG_INF32 ? fmax(z0, (double)tcut + g.oz) : z0;
+    const float R = ctx.prof.R, Rg = R + gd, inv_step = (float)HLB_N / R;
+    const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
+    double bz = t64;
+    uint32_t br = 0xFFFFFFFFu;
+    D3 bcc = d3(0, 0, 0);
+    int bty = OCL_CC_NONE;
+    int capped = 0;
+    unsigned evals = 0;
+    for (int L = g.nlev - 1; L >= 0; --L) {
+        int c0, c1, r0, r1;
+        if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
+        const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
+        const Cell* cells = ctx.cells + g.cell_off[L];
+        for (int k = tid; k < ncells; k += blockDim.x) {
+            const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
+            if (cell.count == 0) continue;
+            const float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
+            const float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
+            const float d = sqrtf(dx * dx + dy * dy);
+            const float cub = cell.maxz - hlb_at(S.hlb, d - gd, inv_step);
+            if (!(d <= Rg && cub > z0l - gd && cub >= tcut - gd)) continue;
+            for (uint32_t j = 0; j < cell.count; ++j) {
+                const Entry e = ctx.entries[cell.start + j];
+                const float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                const float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                const float de = sqrtf(ex * ex + ey * ey);
+                const float ub = e.maxz - hlb_at(S.hlb, de - gd, inv_step);
+                if (!(de <= Rg && ub > z0l - gd && ub >= tcut - gd)) continue;
+                const Tri32 t = ctx.t32[e.tri];
+                float qt, qth;
+                const Iv v = screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
+                if (!(v.hi > NEG_INF32)) continue;
+                const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
+                if (!(hi > z0l - gd && hi >= tcut)) continue;
+                CL64 mine{x, y, t64, d3(0, 0, 0), OCL_CC_NONE};
+                fold_one(ctx, mine, (uint32_t)e.tri, cx, cy, capped, tcut);
+                ++evals;
+                if (mine.z > t64 && (mine.z > bz || (mine.z == bz && t.kd_rank < br))) {
+                    bz = mine.z;
+                    br = t.kd_rank;
+                    bcc = mine.cc;
+                    bty = mine.type;
+                }
+            }
+        }
+    }
+    // block reduction: the highest height, then the lowest KD rank
+    for (int o = 16; o > 0; o >>= 1) {
+        const double oz_ = __shfl_xor_sync(0xffffffffu, bz, o);
+        const uint32_t orr = __shfl_xor_sync(0xffffffffu, br, o);
+        const double ocx = __shfl_xor_sync(0xffffffffu, bcc.x, o);
+        const double ocy = __shfl_xor_sync(0xffffffffu, bcc.y, o);
+        const double ocz = __shfl_xor_sync(0xffffffffu, bcc.z, o);
+        const int oty = __shfl_xor_sync(0xffffffffu, bty, o);
+        if (oz_ > bz || (oz_ == bz && orr < br)) {
+            bz = oz_;
+            br = orr;
+            bcc = d3(ocx, ocy, ocz);
+            bty = oty;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        capped += __shfl_xor_sync(0xffffffffu, capped, o);
+    }
+    // per-warp results through the (idle) key array
+    struct WarpBest {
+        double z, cx, cy, cz;
+        uint32_t rank;
+        int type;
+        unsigned evals;
+        int capped;
+    };
+    WarpBest* wb = reinterpret_cast<WarpBest*>(S.key);
+    if (lane == 0) wb[wid] = WarpBest{bz, bcc.x, bcc.y, bcc.z, br, bty, evals, capped};
+    __syncthreads();
+    if (tid == 0) {
+        WarpBest b = wb[0];
+        unsigned ev = b.evals;
+        int cp = b.capped;
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            const WarpBest c = wb[w];
+            ev += c.evals;
+            cp += c.capped;
+            if (c.z > b.z || (c.z == b.z && c.rank < b.rank)) b = c;
+        }
+        const uint32_t o = ctx.perm[i];
+        const bool lifted = b.rank != 0xFFFFFFFFu;
+        ctx.out_z[o] = lifted ? b.z : z0;
+        ctx.out_cc[3 * o] = lifted ? b.cx : 0.0;
+        ctx.out_cc[3 * o + 1] = lifted ? b.cy : 0.0;
+        ctx.out_cc[3 * o + 2] = lifted ? b.cz : 0.0;
+        ctx.out_type[o] = lifted ? b.type : OCL_CC_NONE;
+        if (ev) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)ev);
+        if (cp) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)cp);
+    }
+    __syncthreads();
+}
+
 // One handed-back point, by the whole block.
 template <bool COMP>
 __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
                                             const ExactGlobal& G, uint32_t* __restrict__ list2,
                                             unsigned long long* __restrict__ nlist2) {
+    if (!COMP && ctx.cp.kind != OCL_CUTTER_CONE) {
+        exact_point_max(ctx, i, S);
+        return;
+    }
     unsigned long long* s_key = S.key;
     int& s_red = *S.red;
     const int tid = threadIdx.x, lane = tid & 31;

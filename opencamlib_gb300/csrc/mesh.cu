@@ -291,6 +291,21 @@ int upload_kd(Mesh& M, const KDTreeD& kd, PushIndex& out) {
     CK(cudaMalloc(&out.d_order, std::max<size_t>(ord.size(), 1) * sizeof(int32_t)));
     if (!kd.nodes.empty())
         CK(cudaMemcpy(out.d_nodes, kd.nodes.data(), kd.nodes.size() * sizeof(KDNodeD), cudaMemcpyHostToDevice));
+    {
+        // FP32 copies of the cuts, rounded both ways (a walk in FP32 that
+        // prunes only where both roundings agree visits every leaf the FP64
+        // walk visits)
+        std::vector<float2> c32(std::max<size_t>(kd.nodes.size(), 1));
+        for (size_t k = 0; k < kd.nodes.size(); ++k) {
+            const double c = kd.nodes[k].cut;
+            float lo = (float)c, hi = (float)c;
+            if ((double)lo > c) lo = std::nextafter(lo, -3.0e38f);
+            if ((double)hi < c) hi = std::nextafter(hi, 3.0e38f);
+            c32[k] = make_float2(lo, hi);
+        }
+        CK(cudaMalloc(&out.d_cut32, c32.size() * sizeof(float2)));
+        CK(cudaMemcpy(out.d_cut32, c32.data(), c32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    }
     if (!ord.empty())
         CK(cudaMemcpy(out.d_order, ord.data(), ord.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     out.built = true;
@@ -413,9 +428,11 @@ void mesh_destroy(Mesh* m) {
     for (int k = 0; k < 2; ++k) {
         cudaFree(m->push[k].d_nodes);
         cudaFree(m->push[k].d_order);
+        cudaFree(m->push[k].d_cut32);
     }
     cudaFree(m->drop_kd.d_nodes);
     cudaFree(m->drop_kd.d_order);
+    cudaFree(m->drop_kd.d_cut32);
     cudaFree(m->d_edge_sin);
     delete m;
 }

@@ -42,6 +42,7 @@ void kd_build_host(const std::vector<double>& bb6, uint64_t n, unsigned bucket, 
 struct PushIndex {
     bool built = false;
     KDNodeD* d_nodes = nullptr;
+    float2* d_cut32 = nullptr;   // per node: the cut rounded down and up to float
     int32_t* d_order = nullptr;  // device-order triangle ids in leaf visit order
     int nnodes = 0;
     int max_depth = 0;
