@@ -51,6 +51,7 @@ struct PushCtx {
     const Tri64* t64;
     const double* esin;  // edge slopes, 3 per triangle
     const KDNodeD* nodes;
+    const float2* cut32;  // the nodes' cuts rounded down / up to float
     const int32_t* order;
     const double* fib;
     int F;
@@ -68,10 +69,19 @@ __device__ __forceinline__ bool iv_outside(const Ival64& a, const Ival64& b) {
     return false;
 }
 
-// Fiber::addInterval on a per-lane array; returns false on capacity overflow.
-__device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap) {
+// FP32 bounds of an interval for the prefilter: the lower end rounded up,
+// the upper end rounded down (a bound strictly inside them is strictly
+// inside the interval).
+__device__ __forceinline__ float2 iv_inner32(const Ival64& i) {
+    return make_float2(__double2float_ru(i.lower), __double2float_rd(i.upper));
+}
+
+// Fiber::addInterval on a per-lane array (with the FP32 inner bounds of
+// every interval kept beside it); returns false on capacity overflow.
+__device__ inline bool fiber_add(Ival64* ints, float2* in32, int& n, const Ival64& i, int cap) {
     if (i.lower == 0.0 && i.upper == 0.0) return true;  // Interval::empty (interval.cpp:113-118)
     if (n == 0) {
+        in32[n] = iv_inner32(i);
         ints[n++] = i;
         return true;
     }
@@ -82,6 +92,7 @@ __device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap)
         if (!iv_outside(i, ints[k])) missing = false;
     if (missing) {
         if (n == cap) return false;
+        in32[n] = iv_inner32(i);
         ints[n++] = i;
         return true;
     }
@@ -94,12 +105,14 @@ __device__ inline bool fiber_add(Ival64* ints, int& n, const Ival64& i, int cap)
             iv_lower(sum, ints[k].lower, ints[k].lcc);
             iv_upper(sum, ints[k].upper, ints[k].ucc);
         } else {
+            in32[w] = in32[k];
             ints[w++] = ints[k];
         }
     }
     iv_lower(sum, i.lower, i.lcc);
     iv_upper(sum, i.upper, i.ucc);
     n = w;
+    in32[n] = iv_inner32(sum);
     ints[n++] = sum;
     return true;
 }
@@ -127,7 +140,7 @@ struct FiberGeom32 {
 // to nearest, each FP32 operation's rounding), the cutter's height and width
 // from the conservative tables of PushCtx.
 __device__ __forceinline__ bool push_needed32(const PushCtx& ctx, const FiberGeom32& g, bool xf, const Entry& e,
-                                              const Ival64* ints, int n, bool overflow) {
+                                              const float2* in32, int n, bool overflow) {
     const float E = ctx.E;
     const float lo = xf ? e.miny : e.minx, hi = xf ? e.maxy : e.maxx;
     const float gap = fmaxf(lo - g.cr, g.cr - hi);
@@ -152,10 +165,10 @@ __device__ __forceinline__ bool push_needed32(const PushCtx& ctx, const FiberGeo
         a = b;
         b = t;
     }
-    const double da = (double)a - (double)(g.tmarg + 2.4e-7f * fabsf(a));
-    const double db = (double)b + (double)(g.tmarg + 2.4e-7f * fabsf(b));
+    a = __fsub_rd(a, g.tmarg + 2.4e-7f * fabsf(a));
+    b = __fadd_ru(b, g.tmarg + 2.4e-7f * fabsf(b));
     for (int q = 0; q < n; ++q)
-        if (da > ints[q].lower && db < ints[q].upper) return false;
+        if (a > in32[q].x && b < in32[q].y) return false;
     return true;
 }
 
@@ -196,7 +209,7 @@ struct PushWarp {
 // in the reference's order, and intervals strictly inside one it holds are
 // ignored exactly as the reference ignores them.
 __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, const uint32_t* __restrict__ list,
-                                              int nlist, Ival64* __restrict__ scratch) {
+                                              int nlist, Ival64* __restrict__ scratch, float2* __restrict__ scratch32) {
     const PushCtx& ctx = *ctxp;
     __shared__ PushWarp s_warp[4];
     const int lane = threadIdx.x & 31;
@@ -219,6 +232,12 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     if (ctx.dir == OCL_GB300_XFIBER) { clx = 0; cly = fb.p1.y; }
     else { clx = fb.p1.x; cly = 0; }
     const double bb[6] = {clx - r, clx + r, cly - r, cly + r, fb.p1.z, fb.p1.z + ctx.cp.length};
+    // the box in FP32, minima rounded down, maxima up (the walk prunes a
+    // subtree only where the FP32 test is certain: it visits every leaf the
+    // FP64 test visits, and the triangles of any other leaf lie outside the
+    // box, so their push intervals are empty and change nothing)
+    float bb32[6];
+    for (int k = 0; k < 6; ++k) bb32[k] = (k & 1) ? __double2float_ru(bb[k]) : __double2float_rd(bb[k]);
     FiberGeom geo;
     geo.xf = ctx.dir == OCL_GB300_XFIBER;
     geo.r = r;
@@ -236,7 +255,9 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
     g32.finv = (float)geo.finv;
     g32.tmarg = 2.0f * ctx.E * fabsf(g32.finv);
     Ival64 local_ints[PUSH_CAP];
+    float2 local_in32[PUSH_CAP];
     Ival64* ints = list ? scratch + (size_t)slot * PUSH_CAP_BIG : local_ints;
+    float2* in32 = list ? scratch32 + (size_t)slot * PUSH_CAP_BIG : local_in32;
     const int cap = list ? PUSH_CAP_BIG : PUSH_CAP;
     int n = 0;
     bool overflow = false;
@@ -258,7 +279,7 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
         for (int c = 0; c < nc; ++c) {
             if (!((W.msk[c] >> lane) & 1u)) continue;
             ++calls;
-            if (push_needed32(ctx, g32, geo.xf, ctx.ent[W.tri[c]], ints, n, overflow)) need |= 1u << c;
+            if (push_needed32(ctx, g32, geo.xf, ctx.ent[W.tri[c]], in32, n, overflow)) need |= 1u << c;
         }
         int tot = 0;
         for (int c = 0; c < nc; ++c) {
@@ -291,7 +312,7 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
             __syncwarp();
             const int nr = min(32, tot - b0);
             for (int j = 0; j < nr; ++j)
-                if (W.owner[j] == lane && !overflow && !fiber_add(ints, n, W.res[j], cap)) overflow = true;
+                if (W.owner[j] == lane && !overflow && !fiber_add(ints, in32, n, W.res[j], cap)) overflow = true;
             __syncwarp();
         }
         nc = 0;
@@ -318,12 +339,13 @@ __global__ void __launch_bounds__(128) k_push(const PushCtx* __restrict__ ctxp, 
             continue;
         }
         bool vh, vl;
+        const float2 c32 = ctx.cut32[e.x];
         if ((nd.dim & 1) == 0) {
-            const bool only_lo = nd.cut > bb[nd.dim + 1];
+            const bool only_lo = c32.x > bb32[nd.dim + 1];  // cut > box max, certainly
             vh = in && !only_lo && nd.hi >= 0;
             vl = in && nd.lo >= 0;
         } else {
-            const bool only_hi = nd.cut < bb[nd.dim - 1];
+            const bool only_hi = c32.y < bb32[nd.dim - 1];  // cut < box min, certainly
             vh = in && nd.hi >= 0;
             vl = in && !only_hi && nd.lo >= 0;
         }
@@ -487,6 +509,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
         h.esin = m.d_edge_sin;
         fill_push_screen(m, cp, fibers, F, h);
         h.nodes = m.n > 0 ? m.push[dir].d_nodes : nullptr;
+        h.cut32 = m.n > 0 ? m.push[dir].d_cut32 : nullptr;
         h.order = m.n > 0 ? m.push[dir].d_order : nullptr;
         h.fib = dfib.p;
         h.F = (int)F;
@@ -500,7 +523,7 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
         CK(cudaMemset(dcnt.p, 0, 5 * sizeof(unsigned long long)));
         const unsigned warps = (unsigned)((F + 31) / 32);
         CK(cudaEventRecord(e0));
-        k_push<<<(warps + 3) / 4, 128>>>(dctx.p, nullptr, 0, nullptr);
+        k_push<<<(warps + 3) / 4, 128>>>(dctx.p, nullptr, 0, nullptr, nullptr);
         CK(cudaGetLastError());
         CK(cudaMemcpy(hc, dcnt.p, sizeof(hc), cudaMemcpyDeviceToHost));
         second_overflow = 0;
@@ -513,11 +536,12 @@ int push_run(Mesh& m, const CutterP& cp, int dir, const double* fibers, uint64_t
                 if (hcounts[k] == 0xFFFFFFFFu) lst.push_back((uint32_t)k);
             DevBuf<uint32_t> dl(lst.size());
             DevBuf<Ival64> scratch(lst.size() * (size_t)PUSH_CAP_BIG);
-            if (!dl.ok() || !scratch.ok()) return OCL_GB300_OOM;
+            DevBuf<float2> scratch32(lst.size() * (size_t)PUSH_CAP_BIG);
+            if (!dl.ok() || !scratch.ok() || !scratch32.ok()) return OCL_GB300_OOM;
             CK(cudaMemcpy(dl.p, lst.data(), lst.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
             CK(cudaMemset(dcnt.p + 2, 0, sizeof(unsigned long long)));
             const unsigned w2 = (unsigned)((lst.size() + 31) / 32);
-            k_push<<<(w2 + 3) / 4, 128>>>(dctx.p, dl.p, (int)lst.size(), scratch.p);
+            k_push<<<(w2 + 3) / 4, 128>>>(dctx.p, dl.p, (int)lst.size(), scratch.p, scratch32.p);
             CK(cudaGetLastError());
             CK(cudaMemcpy(hc, dcnt.p, sizeof(hc), cudaMemcpyDeviceToHost));
             second_overflow = hc[2];

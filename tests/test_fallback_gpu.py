@@ -72,14 +72,24 @@ def test_exact_kernel_matches_oracle(ocl, oracle_lib, name):
     _same((z, cc, ty), (z64, cc64, ty64))
 
 
-@pytest.mark.parametrize("name", ["cyl", "cylcone", "bull"])
+LARGE = {
+    # the composite folds in KD order: gathered into the exact kernel's
+    # global scratch and folded one rank window at a time
+    "compcyl": lambda: cu.CompCylCutter(6.0, 20.0),
+    "cylcone": lambda: cu.CylConeCutter(2.0, 6.0, math.pi / 4),
+    # a maximum: every triangle evaluated by the whole block, reduced
+    "cyl": lambda: cu.CylCutter(6.0, 20.0),
+    "bull": lambda: cu.BullCutter(6.0, 1.0, 20.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LARGE))
 def test_exact_kernel_windows_over_large_lists(ocl, oracle_lib, name):
     # 160 x 160 cells over 12 mm: ~10,000 triangles under a 6 mm cutter, more
-    # than the exact kernel's shared memory holds: gathered into its global
-    # scratch and folded in KD order one rank window at a time
+    # than the exact kernel's shared memory holds
     tris = flat_plate(161)
     cl = points(64, 6)
-    c = CASES[name][1]()
+    c = LARGE[name]()
     mesh = ocl.DeviceMesh(tris)
     z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
     assert st.fallback > 0 and st.plain_points == 0
@@ -89,15 +99,22 @@ def test_exact_kernel_windows_over_large_lists(ocl, oracle_lib, name):
 
 
 def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
-    # 1024 x 1024 cells over 12 mm: ~400,000 triangles under a 6 mm cutter,
-    # more than the exact kernel's global scratch holds
+    # 1024 x 1024 cells over 12 mm: ~400,000 tied triangles under a 6 mm
+    # flat bottom.  A composite (CompCylCutter) folds in KD order and has
+    # more than the exact kernel's global scratch holds: the plain kernel.
+    # The plain cylinder, whose fold is a maximum, is evaluated by the whole
+    # block without a list and never goes there.
     tris = flat_plate(1025)
     cl = points(16, 6)
-    c = cu.CylCutter(6.0, 20.0)
     mesh = ocl.DeviceMesh(tris)
+    c = cu.CompCylCutter(6.0, 20.0)
     z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
     assert st.plain_points > 0
     assert st.violations == 0
+    _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
+    c = cu.CylCutter(6.0, 20.0)
+    z, cc, ty, st = mesh.drop(c, cl, precision="mixed")
+    assert st.fallback > 0 and st.plain_points == 0
     _same((z, cc, ty), oracle_lib.drop(tris, c, cl, "port"))
 
 
