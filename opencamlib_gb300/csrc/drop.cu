@@ -769,18 +769,35 @@ __device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsi
 }
 
 // One handed-back point of a cylinder, ball or bull cutter, by the whole
-// block.  For these cutters a triangle lifts the running height to its own
-// highest contact M_t or not at all, M_t not depending on the running height
-// (liftZ is a strict >; the below test only passes over triangles that
-// cannot lift; no part's contact depends on the height), so the fold over
-// the KD-ordered candidates is the highest M_t, with the CC point of the
-// first triangle in KD order that reaches it (later ones only tie).  Every
-// thread evaluates in FP64 its share of the triangles under the cutter whose
-// FP32 upper bound reaches the fold threshold (the certified lower bound less
-// the guard: a triangle below it cannot give the result), from that
-// threshold, and the block reduces (height, then KD rank): no list, no sort,
-// no capacity limit.
-__device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t i, const ExactShared& S) {
+// block.  For these cutters a triangle's own drop does not depend on the
+// running height: it lifts to its highest contact M_t or not at all (liftZ
+// is a strict >; part skips only pass over parts below the running height),
+// and the fold over the KD-ordered candidates would be the highest M_t with
+// the CC point of the first triangle in KD order reaching it -- but for the
+// below test (a triangle whose bbox top is not above the running height is
+// passed over): a contact can lie an ulp or so above its own triangle's top,
+// and such a triangle is passed over once the height reached that top.
+// So every thread evaluates in FP64 its share of the triangles under the
+// cutter whose FP32 upper bound reaches the fold threshold (the certified
+// lower bound less the guard), from that threshold, and the block reduces
+// (height, then KD rank) while it also keeps the highest contact that lies
+// above its own triangle's top.  If none lies within delta of the maximum,
+// the reduction is the fold's result: a triangle further below cannot stop
+// one of the top ones (its height stays below their tops).  Otherwise the
+// triangles within delta of the maximum are gathered again, sorted by KD
+// rank and folded in order with the below test (heights only: their drops
+// are known), and the winner is evaluated once more for its CC point.
+// One triangle's drop from height z (out of line: the scan around it keeps
+// its registers).
+__device__ __noinline__ CL64 drop_from(const DropCtx& ctx, double x, double y, double z, uint32_t tri, float cx,
+                                       float cy, int& capped, float zfloor) {
+    CL64 m{x, y, z, d3(0, 0, 0), OCL_CC_NONE};
+    fold_one(ctx, m, tri, cx, cy, capped, zfloor);
+    return m;
+}
+
+__device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
+                                             uint32_t* __restrict__ list2, unsigned long long* __restrict__ nlist2) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const GridP& g = ctx.g;
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
@@ -791,50 +808,59 @@ __device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t 
     const double t64 = tcut > NEG_INF32 ? fmax(z0, (double)tcut + g.oz) : z0;
     const float R = ctx.prof.R, Rg = R + gd, inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    double bz = t64;
+    // visits, in the same order for both passes, every triangle under the
+    // cutter whose FP32 upper bound reaches `cut`, with its drop from t64
+    auto scan = [&](float cut, auto&& visit) {
+        for (int L = g.nlev - 1; L >= 0; --L) {
+            int c0, c1, r0, r1;
+            if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
+            const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
+            const Cell* cells = ctx.cells + g.cell_off[L];
+            for (int k = tid; k < ncells; k += blockDim.x) {
+                const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
+                if (cell.count == 0) continue;
+                const float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
+                const float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
+                const float d = sqrtf(dx * dx + dy * dy);
+                const float cub = cell.maxz - hlb_at(S.hlb, d - gd, inv_step);
+                if (!(d <= Rg && cub > z0l - gd && cub >= cut - gd)) continue;
+                for (uint32_t j = 0; j < cell.count; ++j) {
+                    const Entry e = ctx.entries[cell.start + j];
+                    const float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
+                    const float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
+                    const float de = sqrtf(ex * ex + ey * ey);
+                    const float ub = e.maxz - hlb_at(S.hlb, de - gd, inv_step);
+                    if (!(de <= Rg && ub > z0l - gd && ub >= cut - gd)) continue;
+                    const Tri32 t = ctx.t32[e.tri];
+                    float qt, qth;
+                    const Iv v =
+                        screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
+                    if (!(v.hi > NEG_INF32)) continue;
+                    const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
+                    if (!(hi > z0l - gd && hi >= cut)) continue;
+                    visit((uint32_t)e.tri, t.kd_rank);
+                }
+            }
+        }
+    };
+    double bz = t64, em = -1e300;
     uint32_t br = 0xFFFFFFFFu;
     D3 bcc = d3(0, 0, 0);
     int bty = OCL_CC_NONE;
     int capped = 0;
     unsigned evals = 0;
-    for (int L = g.nlev - 1; L >= 0; --L) {
-        int c0, c1, r0, r1;
-        if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
-        const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
-        const Cell* cells = ctx.cells + g.cell_off[L];
-        for (int k = tid; k < ncells; k += blockDim.x) {
-            const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
-            if (cell.count == 0) continue;
-            const float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
-            const float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
-            const float d = sqrtf(dx * dx + dy * dy);
-            const float cub = cell.maxz - hlb_at(S.hlb, d - gd, inv_step);
-            if (!(d <= Rg && cub > z0l - gd && cub >= tcut - gd)) continue;
-            for (uint32_t j = 0; j < cell.count; ++j) {
-                const Entry e = ctx.entries[cell.start + j];
-                const float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
-                const float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
-                const float de = sqrtf(ex * ex + ey * ey);
-                const float ub = e.maxz - hlb_at(S.hlb, de - gd, inv_step);
-                if (!(de <= Rg && ub > z0l - gd && ub >= tcut - gd)) continue;
-                const Tri32 t = ctx.t32[e.tri];
-                float qt, qth;
-                const Iv v = screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
-                if (!(v.hi > NEG_INF32)) continue;
-                const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
-                if (!(hi > z0l - gd && hi >= tcut)) continue;
-                CL64 mine{x, y, t64, d3(0, 0, 0), OCL_CC_NONE};
-                fold_one(ctx, mine, (uint32_t)e.tri, cx, cy, capped, tcut);
-                ++evals;
-                if (mine.z > t64 && (mine.z > bz || (mine.z == bz && t.kd_rank < br))) {
-                    bz = mine.z;
-                    br = t.kd_rank;
-                    bcc = mine.cc;
-                    bty = mine.type;
-                }
-            }
+    scan(tcut, [&](uint32_t tri, uint32_t rank) {
+        const CL64 mine = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
+        ++evals;
+        if (!(mine.z > t64)) return;
+        if (mine.z > ctx.t64[tri].bb[5]) em = fmax(em, mine.z);
+        if (mine.z > bz || (mine.z == bz && rank < br)) {
+            bz = mine.z;
+            br = rank;
+            bcc = mine.cc;
+            bty = mine.type;
         }
-    }
+    });
     // block reduction: the highest height, then the lowest KD rank
     for (int o = 16; o > 0; o >>= 1) {
         const double oz_ = __shfl_xor_sync(0xffffffffu, bz, o);
@@ -849,6 +875,7 @@ __device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t 
             bcc = d3(ocx, ocy, ocz);
             bty = oty;
         }
+        em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
     }
     for (int o = 16; o > 0; o >>= 1) {
         evals += __shfl_xor_sync(0xffffffffu, evals, o);
@@ -856,34 +883,96 @@ __device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t 
     }
     // per-warp results through the (idle) key array
     struct WarpBest {
-        double z, cx, cy, cz;
+        double z, cx, cy, cz, em;
         uint32_t rank;
         int type;
         unsigned evals;
         int capped;
     };
     WarpBest* wb = reinterpret_cast<WarpBest*>(S.key);
-    if (lane == 0) wb[wid] = WarpBest{bz, bcc.x, bcc.y, bcc.z, br, bty, evals, capped};
+    if (lane == 0) wb[wid] = WarpBest{bz, bcc.x, bcc.y, bcc.z, em, br, bty, evals, capped};
     __syncthreads();
     if (tid == 0) {
         WarpBest b = wb[0];
-        unsigned ev = b.evals;
-        int cp = b.capped;
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            const WarpBest c = wb[w];
-            ev += c.evals;
-            cp += c.capped;
-            if (c.z > b.z || (c.z == b.z && c.rank < b.rank)) b = c;
+            WarpBest c = wb[w];
+            b.evals += c.evals;
+            b.capped += c.capped;
+            b.em = fmax(b.em, c.em);
+            if (c.z > b.z || (c.z == b.z && c.rank < b.rank)) {
+                c.evals = b.evals;
+                c.capped = b.capped;
+                c.em = b.em;
+                b = c;
+            }
         }
+        wb[0] = b;
+    }
+    __syncthreads();
+    const WarpBest best = wb[0];
+    __syncthreads();
+    const bool lifted = best.rank != 0xFFFFFFFFu;
+    const double delta = 1e-9 * (1.0 + fabs(best.z));
+    double zo = lifted ? best.z : z0;
+    D3 cco = lifted ? d3(best.cx, best.cy, best.cz) : d3(0, 0, 0);
+    int tyo = lifted ? best.type : OCL_CC_NONE;
+    unsigned ev2 = 0;
+    if (lifted && best.em >= best.z - delta) {
+        // a contact above its own triangle's top near the maximum: the
+        // triangles within delta of it, folded in KD order with the below test
+        double* Md = reinterpret_cast<double*>(S.hi);  // hi and qt together: EXACT_CAP doubles
+        if (tid == 0) *S.n = 0;
+        __syncthreads();
+        const double top = best.z - delta;
+        scan(__double2float_rd(top - g.oz), [&](uint32_t tri, uint32_t rank) {
+            const CL64 mine = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
+            ++ev2;
+            if (!(mine.z >= top)) return;
+            const int slot = atomicAdd(S.n, 1);
+            if (slot < EXACT_CAP) {
+                S.key[slot] = ((unsigned long long)rank << 32) | (unsigned)slot;
+                S.tri[slot] = tri;
+                Md[slot] = mine.z;
+            }
+        });
+        __syncthreads();
+        const int n2 = *S.n;
+        __syncthreads();
+        if (n2 > EXACT_CAP) {
+            if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
+            __syncthreads();
+            return;
+        }
+        exact_sort(S.key, n2);
+        if (tid == 0) {
+            double Z = -1e300;
+            int win = -1;
+            for (int k = 0; k < n2; ++k) {
+                const uint32_t slot = (uint32_t)S.key[k];
+                const double M = Md[slot];
+                if (Z < ctx.t64[S.tri[slot]].bb[5] && M > Z) {
+                    Z = M;
+                    win = (int)S.tri[slot];
+                }
+            }
+            const CL64 w = drop_from(ctx, x, y, t64, (uint32_t)win, cx, cy, capped, tcut);
+            zo = w.z;
+            cco = w.cc;
+            tyo = w.type;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) ev2 += __shfl_xor_sync(0xffffffffu, ev2, o);
+    if (lane == 0 && ev2) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)ev2);
+    if (tid == 0) {
         const uint32_t o = ctx.perm[i];
-        const bool lifted = b.rank != 0xFFFFFFFFu;
-        ctx.out_z[o] = lifted ? b.z : z0;
-        ctx.out_cc[3 * o] = lifted ? b.cx : 0.0;
-        ctx.out_cc[3 * o + 1] = lifted ? b.cy : 0.0;
-        ctx.out_cc[3 * o + 2] = lifted ? b.cz : 0.0;
-        ctx.out_type[o] = lifted ? b.type : OCL_CC_NONE;
-        if (ev) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)ev);
-        if (cp) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)cp);
+        ctx.out_z[o] = zo;
+        ctx.out_cc[3 * o] = cco.x;
+        ctx.out_cc[3 * o + 1] = cco.y;
+        ctx.out_cc[3 * o + 2] = cco.z;
+        ctx.out_type[o] = tyo;
+        if (best.evals) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)best.evals);
+        if (best.capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)best.capped);
+        if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
     }
     __syncthreads();
 }
@@ -894,7 +983,7 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
                                             const ExactGlobal& G, uint32_t* __restrict__ list2,
                                             unsigned long long* __restrict__ nlist2) {
     if (!COMP && ctx.cp.kind != OCL_CUTTER_CONE) {
-        exact_point_max(ctx, i, S);
+        exact_point_max(ctx, i, S, list2, nlist2);
         return;
     }
     unsigned long long* s_key = S.key;

@@ -148,3 +148,30 @@ def test_handed_back_points_on_the_bump_field(ocl):
         handed_back += st.fallback
         _same((z, cc, ty), mesh.drop(c, cl, precision="fp64")[:3])
     assert handed_back > 0
+
+
+@pytest.mark.parametrize("name,cutter", [("cyl20", lambda: cu.CylCutter(20.0, 40.0)),
+                                         ("bull12", lambda: cu.BullCutter(12.0, 2.0, 24.0)),
+                                         ("ball10", lambda: cu.BallCutter(10.0, 20.0))])
+def test_exact_max_path_with_tiny_lists(ocl, name, cutter):
+    """Lists of 16 candidates hand almost every point of a box with fillets
+    back to the exact kernel; its block-parallel maximum (with the replay of
+    the below test where a contact lies above its own triangle's top) must
+    equal the plain FP64 kernel, which folds every candidate in KD order."""
+    import torch
+    tris = w.mesh_of_size("box", 30000, 7)
+    c = cutter()
+    pts = w.batch_points(tris, 15000, c.radius)
+    mesh = ocl.DeviceMesh(tris)
+    d_cl = torch.from_numpy(pts).cuda()
+    M = len(pts)
+    d_z = torch.empty(M, dtype=torch.float64, device="cuda")
+    d_cc = torch.empty((M, 3), dtype=torch.float64, device="cuda")
+    d_ty = torch.empty(M, dtype=torch.int32, device="cuda")
+    b = ocl.DropBatch([(mesh, c, d_cl.data_ptr(), M, d_z.data_ptr(), d_cc.data_ptr(), d_ty.data_ptr())],
+                      list_capacity=16)
+    st = b.run(stats=True)
+    torch.cuda.synchronize()
+    assert st.fallback > 0 and st.violations == 0
+    z64, cc64, ty64, _ = mesh.drop(c, pts, precision="fp64")
+    _same((d_z.cpu().numpy(), d_cc.cpu().numpy(), d_ty.cpu().numpy()), (z64, cc64, ty64))
