@@ -768,25 +768,6 @@ __device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsi
     }
 }
 
-// One handed-back point of a cylinder, ball or bull cutter, by the whole
-// block.  For these cutters a triangle's own drop does not depend on the
-// running height: it lifts to its highest contact M_t or not at all (liftZ
-// is a strict >; part skips only pass over parts below the running height),
-// and the fold over the KD-ordered candidates would be the highest M_t with
-// the CC point of the first triangle in KD order reaching it -- but for the
-// below test (a triangle whose bbox top is not above the running height is
-// passed over): a contact can lie an ulp or so above its own triangle's top,
-// and such a triangle is passed over once the height reached that top.
-// So every thread evaluates in FP64 its share of the triangles under the
-// cutter whose FP32 upper bound reaches the fold threshold (the certified
-// lower bound less the guard), from that threshold, and the block reduces
-// (height, then KD rank) while it also keeps the highest contact that lies
-// above its own triangle's top.  If none lies within delta of the maximum,
-// the reduction is the fold's result: a triangle further below cannot stop
-// one of the top ones (its height stays below their tops).  Otherwise the
-// triangles within delta of the maximum are gathered again, sorted by KD
-// rank and folded in order with the below test (heights only: their drops
-// are known), and the winner is evaluated once more for its CC point.
 // One triangle's drop from height z (out of line: the scan around it keeps
 // its registers).
 __device__ __noinline__ CL64 drop_from(const DropCtx& ctx, double x, double y, double z, uint32_t tri, float cx,
@@ -796,8 +777,23 @@ __device__ __noinline__ CL64 drop_from(const DropCtx& ctx, double x, double y, d
     return m;
 }
 
-__device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
-                                             uint32_t* __restrict__ list2, unsigned long long* __restrict__ nlist2) {
+// One handed-back point of a cylinder, ball or bull cutter, by the whole
+// block, when the candidates reaching the fold threshold are many.  A
+// triangle's drop from a height is its facet contact if that lifts, else
+// the highest of its vertex and edge contacts that lifts, and passes over
+// the triangle if its bbox top is not above the height (the reference's
+// short-circuit and below test); the vertex and edge contacts agree with
+// the facet contact up to rounding.  So the fold's result lies within
+// rounding of the highest drop from below, Mmax: every thread evaluates its
+// share of the triangles (FP32 upper bound reaching the threshold) from the
+// threshold in FP64 and the block reduces the maximum; then only the
+// triangles whose drop from below comes within delta (far above rounding) of
+// it can decide the result: they are gathered, sorted by KD rank and folded
+// in order with the exact per-triangle code (a triangle further below lifts
+// the height to below them and cannot stop one of them).  Returns false,
+// with nothing written, when more than EXACT_CAP triangles come within delta
+// (the general path then takes the point).
+__device__ __noinline__ bool exact_point_top(const DropCtx& ctx, const uint32_t i, const ExactShared& S) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const GridP& g = ctx.g;
     const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
@@ -808,8 +804,7 @@ __device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t 
     const double t64 = tcut > NEG_INF32 ? fmax(z0, (double)tcut + g.oz) : z0;
     const float R = ctx.prof.R, Rg = R + gd, inv_step = (float)HLB_N / R;
     const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    // visits, in the same order for both passes, every triangle under the
-    // cutter whose FP32 upper bound reaches `cut`, with its drop from t64
+    // visits every triangle under the cutter whose FP32 upper bound reaches `cut`
     auto scan = [&](float cut, auto&& visit) {
         for (int L = g.nlev - 1; L >= 0; --L) {
             int c0, c1, r0, r1;
@@ -838,143 +833,68 @@ __device__ __noinline__ void exact_point_max(const DropCtx& ctx, const uint32_t 
                     if (!(v.hi > NEG_INF32)) continue;
                     const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
                     if (!(hi > z0l - gd && hi >= cut)) continue;
-                    visit((uint32_t)e.tri, t.kd_rank);
+                    visit((uint32_t)e.tri, t.kd_rank, hi);
                 }
             }
         }
     };
-    double bz = t64, em = -1e300;
-    uint32_t br = 0xFFFFFFFFu;
-    D3 bcc = d3(0, 0, 0);
-    int bty = OCL_CC_NONE;
+    double bz = -1e300;
     int capped = 0;
     unsigned evals = 0;
-    scan(tcut, [&](uint32_t tri, uint32_t rank) {
-        const CL64 mine = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
+    scan(tcut, [&](uint32_t tri, uint32_t, float) {
+        const CL64 m = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
         ++evals;
-        if (!(mine.z > t64)) return;
-        if (mine.z > ctx.t64[tri].bb[5]) em = fmax(em, mine.z);
-        if (mine.z > bz || (mine.z == bz && rank < br)) {
-            bz = mine.z;
-            br = rank;
-            bcc = mine.cc;
-            bty = mine.type;
-        }
+        if (m.z > t64) bz = fmax(bz, m.z);
     });
-    // block reduction: the highest height, then the lowest KD rank
-    for (int o = 16; o > 0; o >>= 1) {
-        const double oz_ = __shfl_xor_sync(0xffffffffu, bz, o);
-        const uint32_t orr = __shfl_xor_sync(0xffffffffu, br, o);
-        const double ocx = __shfl_xor_sync(0xffffffffu, bcc.x, o);
-        const double ocy = __shfl_xor_sync(0xffffffffu, bcc.y, o);
-        const double ocz = __shfl_xor_sync(0xffffffffu, bcc.z, o);
-        const int oty = __shfl_xor_sync(0xffffffffu, bty, o);
-        if (oz_ > bz || (oz_ == bz && orr < br)) {
-            bz = oz_;
-            br = orr;
-            bcc = d3(ocx, ocy, ocz);
-            bty = oty;
-        }
-        em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        evals += __shfl_xor_sync(0xffffffffu, evals, o);
-        capped += __shfl_xor_sync(0xffffffffu, capped, o);
-    }
-    // per-warp results through the (idle) key array
-    struct WarpBest {
-        double z, cx, cy, cz, em;
-        uint32_t rank;
-        int type;
-        unsigned evals;
-        int capped;
-    };
-    WarpBest* wb = reinterpret_cast<WarpBest*>(S.key);
-    if (lane == 0) wb[wid] = WarpBest{bz, bcc.x, bcc.y, bcc.z, em, br, bty, evals, capped};
+    for (int o = 16; o > 0; o >>= 1) bz = fmax(bz, __shfl_xor_sync(0xffffffffu, bz, o));
+    double* wz = reinterpret_cast<double*>(S.key);  // per-warp maxima (the key array is idle)
+    if (lane == 0) wz[wid] = bz;
     __syncthreads();
-    if (tid == 0) {
-        WarpBest b = wb[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            WarpBest c = wb[w];
-            b.evals += c.evals;
-            b.capped += c.capped;
-            b.em = fmax(b.em, c.em);
-            if (c.z > b.z || (c.z == b.z && c.rank < b.rank)) {
-                c.evals = b.evals;
-                c.capped = b.capped;
-                c.em = b.em;
-                b = c;
-            }
-        }
-        wb[0] = b;
-    }
+    double mmax = -1e300;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mmax = fmax(mmax, wz[w]);
+    if (tid == 0) *S.n = 0;
     __syncthreads();
-    const WarpBest best = wb[0];
-    __syncthreads();
-    const bool lifted = best.rank != 0xFFFFFFFFu;
-    const double delta = 1e-9 * (1.0 + fabs(best.z));
-    double zo = lifted ? best.z : z0;
-    D3 cco = lifted ? d3(best.cx, best.cy, best.cz) : d3(0, 0, 0);
-    int tyo = lifted ? best.type : OCL_CC_NONE;
+    CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
     unsigned ev2 = 0;
-    if (lifted && best.em >= best.z - delta) {
-        // a contact above its own triangle's top near the maximum: the
-        // triangles within delta of it, folded in KD order with the below test
-        double* Md = reinterpret_cast<double*>(S.hi);  // hi and qt together: EXACT_CAP doubles
-        if (tid == 0) *S.n = 0;
-        __syncthreads();
-        const double top = best.z - delta;
-        scan(__double2float_rd(top - g.oz), [&](uint32_t tri, uint32_t rank) {
-            const CL64 mine = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
+    if (mmax > -1e300) {
+        const double top = mmax - 1e-9 * (1.0 + fabs(mmax));
+        scan(__double2float_rd(top - g.oz), [&](uint32_t tri, uint32_t rank, float hi) {
+            const CL64 m = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
             ++ev2;
-            if (!(mine.z >= top)) return;
+            if (!(m.z >= top)) return;
             const int slot = atomicAdd(S.n, 1);
             if (slot < EXACT_CAP) {
                 S.key[slot] = ((unsigned long long)rank << 32) | (unsigned)slot;
                 S.tri[slot] = tri;
-                Md[slot] = mine.z;
+                S.hi[slot] = hi;
             }
         });
         __syncthreads();
         const int n2 = *S.n;
         __syncthreads();
-        if (n2 > EXACT_CAP) {
-            if (tid == 0) list2[atomicAdd(nlist2, 1ull)] = i;
-            __syncthreads();
-            return;
-        }
+        if (n2 > EXACT_CAP) return false;
         exact_sort(S.key, n2);
-        if (tid == 0) {
-            double Z = -1e300;
-            int win = -1;
-            for (int k = 0; k < n2; ++k) {
-                const uint32_t slot = (uint32_t)S.key[k];
-                const double M = Md[slot];
-                if (Z < ctx.t64[S.tri[slot]].bb[5] && M > Z) {
-                    Z = M;
-                    win = (int)S.tri[slot];
-                }
-            }
-            const CL64 w = drop_from(ctx, x, y, t64, (uint32_t)win, cx, cy, capped, tcut);
-            zo = w.z;
-            cco = w.cc;
-            tyo = w.type;
-        }
+        if (tid < 32) exact_fold<false>(ctx, cl, S.key, n2, S.hi, S.tri, cx, cy, capped, ev2);
     }
-    for (int o = 16; o > 0; o >>= 1) ev2 += __shfl_xor_sync(0xffffffffu, ev2, o);
-    if (lane == 0 && ev2) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)ev2);
-    if (tid == 0) {
-        const uint32_t o = ctx.perm[i];
-        ctx.out_z[o] = zo;
-        ctx.out_cc[3 * o] = cco.x;
-        ctx.out_cc[3 * o + 1] = cco.y;
-        ctx.out_cc[3 * o + 2] = cco.z;
-        ctx.out_type[o] = tyo;
-        if (best.evals) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)best.evals);
-        if (best.capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)best.capped);
+    for (int o = 16; o > 0; o >>= 1) {
+        evals += __shfl_xor_sync(0xffffffffu, evals, o);
+        ev2 += __shfl_xor_sync(0xffffffffu, ev2, o);
+        capped += __shfl_xor_sync(0xffffffffu, capped, o);
+    }
+    if (lane == 0) {
+        if (evals + ev2) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)(evals + ev2));
         if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
     }
+    if (tid == 0) {
+        const uint32_t o = ctx.perm[i];
+        ctx.out_z[o] = cl.z;
+        ctx.out_cc[3 * o] = cl.cc.x;
+        ctx.out_cc[3 * o + 1] = cl.cc.y;
+        ctx.out_cc[3 * o + 2] = cl.cc.z;
+        ctx.out_type[o] = cl.type;
+    }
     __syncthreads();
+    return true;
 }
 
 // One handed-back point, by the whole block.
@@ -982,10 +902,7 @@ template <bool COMP>
 __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
                                             const ExactGlobal& G, uint32_t* __restrict__ list2,
                                             unsigned long long* __restrict__ nlist2) {
-    if (!COMP && ctx.cp.kind != OCL_CUTTER_CONE) {
-        exact_point_max(ctx, i, S, list2, nlist2);
-        return;
-    }
+    if (!COMP && ctx.cp.kind != OCL_CUTTER_CONE && exact_point_top(ctx, i, S)) return;
     unsigned long long* s_key = S.key;
     int& s_red = *S.red;
     const int tid = threadIdx.x, lane = tid & 31;
