@@ -1194,6 +1194,21 @@ struct DropWork {
     }
     DevBuf<uint8_t> sort_tmp;
     DevBuf<unsigned char> exact_scratch;  // handed-back points with many candidates
+    // the pilot pass: every PILOT-th sorted point, its results and counters
+    DevBuf<double> pcl, pz, pcc;
+    DevBuf<int32_t> pty;
+    DevBuf<uint32_t> piota;
+    DevBuf<unsigned long long> pcounters;
+    size_t pcap = 0;
+    bool ensure_pilot(size_t Mp) {
+        if (Mp <= pcap && pcounters.p) return true;
+        const size_t c = std::max<size_t>(Mp, 256);
+        if (!pcl.alloc(3 * c) || !pz.alloc(c) || !pcc.alloc(3 * c) || !pty.alloc(c) || !piota.alloc(c) ||
+            !pcounters.alloc(C_NCOUNTERS + 1))
+            return false;
+        pcap = c;
+        return true;
+    }
     DropCtx* host_ctx = nullptr;  // launch context (kernel parameter)
     // per-call stage events, a ring over the last STAGE_RING calls (read
     // afterwards by ocl_gb300_stage_times without syncing the calls)
@@ -1334,6 +1349,95 @@ void init_drop_ctx(const Mesh& m, const CutterP& cp, DropCtx& h) {
     h.guard = 4.0f * h.E + 1e-5f * (float)cp.radius;
 }
 
+// ---------------------------------------------------------------------------
+// Pilot points.  A screen culls against its running lower bound; started
+// near the final height it screens a fraction of the pairs.  Every
+// PILOT-th point in Morton order (one per 4 x 4 block of a raster) is dropped
+// first; a point's height is then bounded from below by each nearby pilot's
+// contact point cc (a point of the surface: the cutter above p cannot reach
+// below it), z >= cc.z - height(|cc - p|) where the distance is within the
+// radius.  The bound, rounded down in the local FP32 frame less a margin,
+// seeds the screen (the seeding kernel keeps the larger of it and its own).
+// ---------------------------------------------------------------------------
+constexpr int PILOT = 16;
+constexpr uint64_t PILOT_MIN_POINTS = 4096;  // smaller calls run without pilots
+
+__global__ void k_pilot_gather(const double* __restrict__ cls, uint64_t M, double* __restrict__ pcl,
+                               uint32_t* __restrict__ iota, uint64_t Mp) {
+    const uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (j >= Mp) return;
+    const uint64_t i = j * PILOT;
+    pcl[3 * j] = cls[3 * i];
+    pcl[3 * j + 1] = cls[3 * i + 1];
+    pcl[3 * j + 2] = cls[3 * i + 2];
+    iota[j] = (uint32_t)j;
+}
+
+__global__ void k_pilot_seed(const __grid_constant__ DropCtx ctx, const double* __restrict__ pcc,
+                             const int32_t* __restrict__ pty, uint64_t Mp) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)ctx.M) return;
+    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
+    const double R = ctx.cp.radius;
+    const int64_t g = (int64_t)(i / PILOT);
+    double best = -1e300;
+    for (int64_t q = g - 1; q <= g + 1; ++q) {
+        if (q < 0 || q >= (int64_t)Mp || pty[q] == OCL_CC_NONE) continue;
+        const double dx = pcc[3 * q] - x, dy = pcc[3 * q + 1] - y;
+        const double d = sqrt(dx * dx + dy * dy);
+        if (!(d <= R * (1.0 - 1e-9) - 1e-9)) continue;  // clear of the rim by more than rounding
+        best = fmax(best, pcc[3 * q + 2] - height_any(ctx.cp, d));
+    }
+    float b = __double2float_rd(z0 - ctx.g.oz);
+    if (best > z0) b = fmaxf(b, __double2float_rd(best - ctx.g.oz) - 2.0f * ctx.E);
+    ctx.blo[i] = b;
+}
+
+// The mixed-precision pipeline over the sorted points of `h` (M of them):
+// screens, bull edges, refinement, hand-back; cnt are the pass's counters.
+// ev_screen / ev_refine (may be null) mark the end of the screen and
+// refinement stages.
+static int enqueue_mixed(DropWork& w, const Mesh& m, const CutterP& cp, DropCtx& h, uint64_t M,
+                         unsigned long long* cnt, cudaStream_t stream, cudaEvent_t ev_screen, cudaEvent_t ev_refine,
+                         uint64_t& launches) {
+    h.counters = cnt;
+    h.sparse_n = cnt + C_SPARSE;
+    const bool composite = h.composite_screen;
+    const int TB = 256;
+    const unsigned nb = (unsigned)((M + TB - 1) / TB);
+    const unsigned warps = (unsigned)((M + 31) / 32);
+    const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
+    launch_screen(h, cp, sblocks, stream);
+    if (ev_screen) CK(cudaEventRecord(ev_screen, stream));
+    h.edge_slots = nullptr;
+    h.edge_n = nullptr;
+    h.edge_res = nullptr;
+    if (cp.kind == OCL_CUTTER_BULL && m.n < (1ull << 30)) {
+        if (!w.ensure_edges(M)) return OCL_GB300_OOM;
+        h.edge_slots = w.edge_slots.p;
+        h.edge_n = w.edge_n.p;
+        h.edge_res = w.edge_res.p;
+        k_bull_plan<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h, w.edge_queue.p, cnt + C_EDGEQ);
+        const unsigned eb = (unsigned)std::min<uint64_t>((M * EDGE_SLOTS + 127) / 128, 152u * 16u);
+        k_bull_eval<<<eb, 128, 0, stream>>>(h, w.edge_queue.p, cnt + C_EDGEQ);
+        launches += 2;
+    }
+    if (h.edge_res) k_drop_refine<true><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+    else k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+    if (ev_refine) CK(cudaEventRecord(ev_refine, stream));
+    k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, cnt + C_FALLBACK);
+    // the fallback grids stride over however many points were handed back
+    if (!w.exact_scratch.reserve(EXACT_GBYTES)) return OCL_GB300_OOM;
+    int st = launch_exact(h, composite, w.list.p, cnt + C_FALLBACK, w.list2.p, cnt + C_PLAIN,
+                          (unsigned)std::min<uint64_t>(M, (uint64_t)EXACT_GBLOCKS), stream,
+                          exact_global_in(w.exact_scratch.p));
+    if (st) return st;
+    const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
+    k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(h, w.list2.p, cnt + C_PLAIN);
+    launches += 7;  // seed, dense and sparse screen, refine, collect, exact, plain
+    return OCL_GB300_OK;
+}
+
 int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int precision, double* d_z, double* d_cc,
              int32_t* d_type, cudaStream_t stream, ocl_gb300_stats* stats) {
     if (M == 0) return OCL_GB300_OK;
@@ -1353,7 +1457,6 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
     if (!w.host_ctx) w.host_ctx = new DropCtx();
     DropCtx* h = w.host_ctx;  // passed by value as the kernels' __grid_constant__ parameter
     init_drop_ctx(m, cp, *h);
-    const bool composite = h->composite_screen;
     h->cl = w.cls.p;
     h->perm = w.perm.p;
     h->M = (int)M;
@@ -1404,39 +1507,41 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         k_drop_kd<false><<<(warps + 3) / 4, 128, 0, stream>>>(*h, nullptr, nullptr);
         launches += 1;
     } else {
-        const unsigned sblocks = (warps + SCREEN_WARPS - 1) / SCREEN_WARPS;
-        launch_screen(*h, cp, sblocks, stream);
-        CK(cudaEventRecord(ev[2], stream));
-        if (cp.kind == OCL_CUTTER_BULL && m.n < (1ull << 30)) {
-            if (!w.ensure_edges(M)) return OCL_GB300_OOM;
-            h->edge_slots = w.edge_slots.p;
-            h->edge_n = w.edge_n.p;
-            h->edge_res = w.edge_res.p;
-            k_bull_plan<<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h, w.edge_queue.p, w.counters.p + C_EDGEQ);
-            const unsigned eb = (unsigned)std::min<uint64_t>((M * EDGE_SLOTS + 127) / 128, 152u * 16u);
-            k_bull_eval<<<eb, 128, 0, stream>>>(*h, w.edge_queue.p, w.counters.p + C_EDGEQ);
+        const bool pilot = M >= PILOT_MIN_POINTS;
+        if (pilot) {
+            // the pilot points first (their own pipeline, counters and
+            // outputs), then their bounds into blo for the main pass
+            const uint64_t Mp = (M + PILOT - 1) / PILOT;
+            if (!w.ensure_pilot(Mp)) return OCL_GB300_OOM;
+            CK(cudaMemsetAsync(w.pcounters.p, 0, (C_NCOUNTERS + 1) * sizeof(unsigned long long), stream));
+            k_pilot_gather<<<(unsigned)((Mp + TB - 1) / TB), TB, 0, stream>>>(w.cls.p, M, w.pcl.p, w.piota.p, Mp);
+            DropCtx hp = *h;
+            hp.cl = w.pcl.p;
+            hp.perm = w.piota.p;
+            hp.M = (int)Mp;
+            hp.out_z = w.pz.p;
+            hp.out_cc = w.pcc.p;
+            hp.out_type = w.pty.p;
+            st = enqueue_mixed(w, m, cp, hp, Mp, w.pcounters.p, stream, nullptr, nullptr, launches);
+            if (st) return st;
+            k_pilot_seed<<<nb, TB, 0, stream>>>(*h, w.pcc.p, w.pty.p, Mp);
             launches += 2;
+            h->piloted = true;
         }
-        if (h->edge_res) k_drop_refine<true><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
-        else k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(*h);
-        CK(cudaEventRecord(ev[3], stream));
-        k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, w.counters.p + C_FALLBACK);
-        // the fallback grids stride over however many points were handed back
-        if (!w.exact_scratch.reserve(EXACT_GBYTES)) return OCL_GB300_OOM;
-        st = launch_exact(*h, composite, w.list.p, w.counters.p + C_FALLBACK, w.list2.p, w.counters.p + C_PLAIN,
-                          (unsigned)std::min<uint64_t>(M, (uint64_t)EXACT_GBLOCKS), stream,
-                          exact_global_in(w.exact_scratch.p));
+        st = enqueue_mixed(w, m, cp, *h, M, w.counters.p, stream, ev[2], ev[3], launches);
         if (st) return st;
-        const unsigned fb_blocks = std::min<unsigned>((warps + 3) / 4, 152u * 16u);
-        k_drop_kd<true><<<fb_blocks, 128, 0, stream>>>(*h, w.list2.p, w.counters.p + C_PLAIN);
-        launches += 7;  // seed, dense and sparse screen, refine, collect, exact, plain
     }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev[4], stream));
     if (stats) {
-        unsigned long long c[C_NCOUNTERS];
+        unsigned long long c[C_NCOUNTERS], pc[C_NCOUNTERS];
         CK(cudaMemcpyAsync(c, w.counters.p, sizeof(c), cudaMemcpyDeviceToHost, stream));
+        std::memset(pc, 0, sizeof(pc));
+        if (h->piloted) CK(cudaMemcpyAsync(pc, w.pcounters.p, sizeof(pc), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
+        // the pilot pass's work counts with the call's (its points are
+        // dropped again by the main pass, whose outcome counters stand)
+        for (int k : {C_PAIRS, C_REFINED, C_SCREENED, C_CAPPED, C_VIOLATION}) c[k] += pc[k];
         float t_all = 0, t_scr = 0, t_ref = 0, t_fb = 0;
         cudaEventElapsedTime(&t_all, ev[0], ev[4]);
         cudaEventElapsedTime(&t_scr, ev[1], ev[2]);
