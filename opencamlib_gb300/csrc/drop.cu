@@ -1354,7 +1354,8 @@ void init_drop_ctx(const Mesh& m, const CutterP& cp, DropCtx& h) {
 // near the final height it screens a fraction of the pairs.  Every
 // PILOT-th point in Morton order (one per 4 x 4 block of a raster) is dropped
 // first; a point's height is then bounded from below by each nearby pilot's
-// contact point cc (a point of the surface: the cutter above p cannot reach
+// contact point cc (a point of the surface: the cylinder's, ball's and
+// bull's drop is their highest contact with the surface, so it cannot lie
 // below it), z >= cc.z - height(|cc - p|) where the distance is within the
 // radius.  The bound, rounded down in the local FP32 frame less a margin,
 // seeds the screen (the seeding kernel keeps the larger of it and its own).
@@ -1507,7 +1508,12 @@ int drop_run(Mesh& m, const CutterP& cp, const double* d_cl, uint64_t M, int pre
         k_drop_kd<false><<<(warps + 3) / 4, 128, 0, stream>>>(*h, nullptr, nullptr);
         launches += 1;
     } else {
-        const bool pilot = M >= PILOT_MIN_POINTS;
+        // (the bound needs a drop that returns the highest contact: the
+        // cylinder, ball and bull do; the cone's tip short-circuits its rim,
+        // so its drop can lie below a surface point's bound, and the
+        // composites inherit that)
+        const bool pilot = M >= PILOT_MIN_POINTS && (cp.kind == OCL_CUTTER_CYL || cp.kind == OCL_CUTTER_BALL ||
+                                                      cp.kind == OCL_CUTTER_BULL);
         if (pilot) {
             // the pilot points first (their own pipeline, counters and
             // outputs), then their bounds into blo for the main pass
