@@ -58,7 +58,6 @@ struct DropCtx {
     int cand_cap;           // list capacity per CL point
     float* blo;             // per CL: certified lower bound (local frame)
     bool seeded;            // blo holds the seeding kernel's bounds on entry to the screen
-    bool piloted;           // blo holds the pilot points' bounds before the seeding kernel runs
     uint32_t* sparse_list;  // warps handed from the dense to the sparse screen kernel
     unsigned long long* sparse_n;
     // bull: edge contacts evaluated ahead of the fold (null: evaluated inline)

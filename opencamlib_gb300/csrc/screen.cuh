@@ -530,7 +530,6 @@ __device__ __forceinline__ void seed_warp(const DropCtx& ctx, const int base) {
     const double ymin = warp_mind(active ? y : 1e300), ymax = warp_maxd(active ? y : -1e300);
     float blo = z0l;
     if ((xmax - xmin) + (ymax - ymin) > ctx.cp.radius) blo = seed_blo<KIND, CK>(ctx, x, y, active, z0l);
-    if (ctx.piloted && active) blo = fmaxf(blo, ctx.blo[i]);
     if (active) ctx.blo[i] = blo;
 }
 
