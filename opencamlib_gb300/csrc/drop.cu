@@ -12,12 +12,9 @@
 //                     whole-triangle screen [lo, hi].  A lane keeps a running
 //                     certified lower bound and a short list of triangles whose
 //                     hi reaches it.
-//      k_drop_refine  the listed triangles in FP64 with the reference
-//                     semantics: the highest contact, ties by the reference's
-//                     KD visit order (cylinder, ball, bull: one warp per 32
-//                     points spreads the pairs over its lanes, then folds the
-//                     few triangles near the top in order; cone, composites:
-//                     one thread per point folds its list in order).
+//      k_drop_refine  one thread per point evaluates its listed triangles in
+//                     FP64 with the reference semantics and keeps the highest
+//                     contact (ties: the reference's KD visit order).
 //      k_drop_kd      points whose list overflowed are redone in plain FP64.
 //   3. Plain FP64 (OCL_GB300_PREC_FP64): k_drop_kd for every point; it runs
 //      the reference's KD search and evaluates every exact-overlap pair in FP64.
@@ -563,6 +560,18 @@ __global__ void __launch_bounds__(128) k_drop_refine(const __grid_constant__ Dro
     refine_point<BULL_PLAN>(ctx, i);
 }
 
+template <bool BULL_PLAN>
+__global__ void __launch_bounds__(128) k_drop_refine_b(const __grid_constant__ BatchView bv) {
+    __shared__ DropCtx s_ctx;
+    __shared__ TileState ts;
+    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
+    uint2 tile;
+    while (batch_next_tile(bv, ts, s_ctx, tile)) {
+        const uint32_t i = tile.y * TILE_POINTS + threadIdx.x;
+        if (i < (uint32_t)s_ctx.M) refine_point<BULL_PLAN>(s_ctx, i);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Exact fold of one handed-back CL point per block.
 // The block gathers every triangle whose certified FP32 upper bound lies above
@@ -766,262 +775,6 @@ __device__ __noinline__ CL64 drop_from(const DropCtx& ctx, double x, double y, d
     CL64 m{x, y, z, d3(0, 0, 0), OCL_CC_NONE};
     fold_one(ctx, m, tri, cx, cy, capped, zfloor);
     return m;
-}
-
-// MillingCutter::dropCutter for a bull with its sloped edges' contacts taken
-// from the plan: planned(tq, e) is the planned result of edge e, or null (an
-// edge the plan left out cannot reach the floor: it cannot lift).  Facet,
-// vertices and horizontal edges are evaluated here.
-template <class Planned>
-__device__ __forceinline__ void fold_bull_with(const DropCtx& ctx, CL64& cl, uint32_t tq, float cxl, float cyl,
-                                               Planned&& planned, int& capped) {
-    const Tri64& t = ctx.t64[tq];
-    if (!overlaps64(ctx.cp.radius, cl.x, cl.y, t) || !(cl.z < t.bb[5])) return;
-    const Tri32 t3 = ctx.t32[tq];
-    const uint32_t fl = t3.flags;
-    const float wx = cxl - t3.v0[0], wy = cyl - t3.v0[1];
-    BasicP b = ctx.cp.b;
-    b.kind = OCL_CUTTER_BULL;
-    const float vlim = __double2float_rd(cl.z - ctx.g.oz) - t3.v0[2] - ctx.guard - ctx.E;
-    Prof32 pb = ctx.prof;
-    pb.kind = OCL_CUTTER_BULL;
-    if (!(facet32(pb, t3, wx, wy, ctx.E, ctx.E * 4.0f * t3.bary_scale + 1e-6f).hi < vlim) &&
-        facet_drop_base(b, cl, t, fl))
-        return;
-    const float vx[3] = {0.0f, t3.e1[0], t3.e2[0]};
-    const float vy[3] = {0.0f, t3.e1[1], t3.e2[1]};
-    const float vz[3] = {0.0f, t3.e1[2], t3.e2[2]};
-    for (int k = 0; k < 3; ++k) {
-        if (vertex32(ctx.prof, vx[k] - wx, vy[k] - wy, vz[k], ctx.E).hi < vlim) continue;
-        const D3 p = tri_p(t, k);
-        const double q = xynorm(d3(cl.x, cl.y, cl.z) - p);
-        if (q <= b.radius) liftz(cl, p.z - height_basic(b, q), p, OCL_CC_VERTEX);
-    }
-    if (!(cl.z < t.bb[5])) return;
-    for (int e = 0; e < 3; ++e) {
-        if (fl & (TF_EDGE0_SKIP << e)) continue;
-        if (!(fl & (TF_EDGE0_HORIZ << e))) {
-            const EdgeRes* r = planned(tq, e);
-            if (r && r->valid) liftz(cl, r->clz, d3(r->ccx, r->ccy, r->ccz), OCL_CC_EDGE);
-            continue;
-        }
-        double clz;
-        D3 cc;
-        if (edge_contact64(b, cl.x, cl.y, tri_p(t, e), tri_p(t, (e + 1) % 3), clz, cc, &capped))
-            liftz(cl, clz, cc, OCL_CC_EDGE);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// FP64 refinement of the cylinder, ball and bull, one warp per 32 points.
-// For these cutters a triangle's drop from a height is its facet contact if
-// that lifts, else the highest of its vertex and edge contacts, and they
-// agree up to rounding (the handed-back points' block-parallel maximum rests
-// on the same fact): the in-order fold of a point's list equals the in-order
-// fold of the listed triangles whose drop from the floor comes within delta
-// of the highest such drop, Mmax.  So the warp spreads the (point, triangle)
-// pairs of its 32 lists over its lanes, each lane dropping one triangle from
-// its point's floor (no running height: no order), keeps the lifting results
-// in shared memory and each point's maximum; then each lane folds its own
-// point's few triangles near the top in KD order with the reference's code.
-// A point falls back to the in-order fold of its list (refine_point) when
-// its results do not fit the warp's buffer, when more than TOP_MEMBERS
-// triangles lie near the top, when Mmax - delta does not clear the floor, or
-// (bull) when its edge plan overflowed.  Bull: the sloped edges' contacts
-// come from the plan as further items (an edge counts for its triangle: a
-// triangle is kept when its facet/vertex drop or one of its planned edges
-// reaches the top; keeping more triangles than needed leaves the fold
-// unchanged).
-// ---------------------------------------------------------------------------
-constexpr int TOP_BUF = 256;     // lifting results a warp keeps
-constexpr int TOP_MEMBERS = 8;   // triangles near the top a point folds in order
-
-struct TopShared {
-    double z[TOP_BUF];
-    uint32_t tri[TOP_BUF];
-    unsigned long long zmax[32];  // per point: the order-preserving bits of Mmax (0: none)
-    uint8_t owner[TOP_BUF];
-    unsigned lost;                // points with results beyond the buffer
-};
-
-__device__ __forceinline__ unsigned long long ord64(double v) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double unord64(unsigned long long u) {
-    return __longlong_as_double((long long)((u >> 63) ? (u & 0x7FFFFFFFFFFFFFFFull) : ~u));
-}
-
-template <bool BULL>
-__device__ __forceinline__ void refine_warp_top(const DropCtx& ctx, const uint32_t base, TopShared& S) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t i = base + lane;
-    const bool inb = i < (uint32_t)ctx.M;
-    int n = inb ? ctx.ncand[i] : 0;
-    const bool handed = n == 0xFFFF;
-    if (handed) n = 0;
-    const bool mine = inb && !handed;
-    double x = 0.0, y = 0.0, z0 = 0.0;
-    if (mine) {
-        x = ctx.cl[3 * i];
-        y = ctx.cl[3 * i + 1];
-        z0 = ctx.cl[3 * i + 2];
-    }
-    const float cxl = (float)(x - ctx.g.ox), cyl = (float)(y - ctx.g.oy);
-    const float blo = mine ? ctx.blo[i] : NEG_INF32;
-    const float tcut = blo > NEG_INF32 ? blo - ctx.guard : NEG_INF32;
-    const double t64 = tcut > NEG_INF32 ? fmax(z0, (double)tcut + ctx.g.oz) : z0;
-    const int nplan = (BULL && mine) ? ctx.edge_n[i] : 0;
-    bool seq = BULL && nplan > EDGE_SLOTS;
-    const int items = mine && !seq ? n + (BULL ? nplan : 0) : 0;
-    S.zmax[lane] = 0ull;
-    if (lane == 0) S.lost = 0u;
-    int incl = items;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const int P = __shfl_sync(0xffffffffu, incl, 31);
-    __syncwarp();
-    int capped = 0;
-    unsigned nbuf = 0;
-    for (int p0 = 0; p0 < P; p0 += 32) {
-        const int p = p0 + lane;
-        int o = 0;  // the point of item p: lanes whose inclusive count is <= p
-        for (int s = 16; s > 0; s >>= 1)
-            if (__shfl_sync(0xffffffffu, incl, o + s - 1) <= p) o += s;
-        o = min(o, 31);
-        const int q = p - (__shfl_sync(0xffffffffu, incl, o) - __shfl_sync(0xffffffffu, items, o));
-        const double ox = __shfl_sync(0xffffffffu, x, o), oy = __shfl_sync(0xffffffffu, y, o);
-        const double ot = __shfl_sync(0xffffffffu, t64, o);
-        const float ocx = __shfl_sync(0xffffffffu, cxl, o), ocy = __shfl_sync(0xffffffffu, cyl, o);
-        const float otc = __shfl_sync(0xffffffffu, tcut, o);
-        const int on = __shfl_sync(0xffffffffu, n, o);
-        bool lift = false;
-        double z = 0.0;
-        uint32_t tq = 0;
-        if (p < P) {
-            const size_t pi = (size_t)(base + o);
-            if (q < on) {
-                tq = ctx.cand[pi * ctx.cand_cap + q] & ~CAND_VERIFY;
-                CL64 m{ox, oy, ot, d3(0, 0, 0), OCL_CC_NONE};
-                if (BULL)
-                    fold_bull_with(ctx, m, tq, ocx, ocy, [](uint32_t, int) -> const EdgeRes* { return nullptr; },
-                                   capped);
-                else
-                    m = drop_from(ctx, ox, oy, ot, tq, ocx, ocy, capped, otc);
-                lift = m.z > ot;
-                z = m.z;
-            } else {
-                const int k = q - on;
-                const EdgeRes r = ctx.edge_res[pi * EDGE_SLOTS + k];
-                tq = ctx.edge_slots[pi * EDGE_SLOTS + k] >> 2;
-                lift = r.valid && r.clz > ot;
-                z = r.clz;
-            }
-        }
-        if (lift) atomicMax(&S.zmax[o], ord64(z));
-        const unsigned bal = __ballot_sync(0xffffffffu, lift);
-        const unsigned pos = nbuf + (unsigned)__popc(bal & ((1u << lane) - 1u));
-        if (lift) {
-            if (pos < (unsigned)TOP_BUF) {
-                S.z[pos] = z;
-                S.tri[pos] = tq;
-                S.owner[pos] = (uint8_t)o;
-            } else {
-                atomicOr(&S.lost, 1u << o);
-            }
-        }
-        nbuf += (unsigned)__popc(bal);
-    }
-    __syncwarp();
-    if (mine && !seq) {
-        seq = (S.lost >> lane) & 1u;
-        const unsigned long long u = S.zmax[lane];
-        if (u == 0ull && t64 > z0) seq = true;  // nothing above a certified floor: let the fold tell
-        CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
-        if (!seq && u != 0ull) {
-            const double mmax = unord64(u);
-            const double top = mmax - 1e-9 * (1.0 + fabs(mmax));
-            if (!(top > t64)) seq = true;
-            uint32_t rk[TOP_MEMBERS], tr[TOP_MEMBERS];
-            int nm = 0;
-            const int nb = (int)min(nbuf, (unsigned)TOP_BUF);
-            for (int k = 0; k < nb && !seq; ++k) {
-                if (S.owner[k] != (uint8_t)lane || !(S.z[k] >= top)) continue;
-                const uint32_t t = S.tri[k];
-                bool dup = false;
-                for (int j = 0; j < nm; ++j) dup |= tr[j] == t;
-                if (dup) continue;
-                if (nm == TOP_MEMBERS) {
-                    seq = true;
-                    break;
-                }
-                const uint32_t r = ctx.t32[t].kd_rank;
-                int b = nm++;
-                for (; b > 0 && rk[b - 1] > r; --b) {
-                    rk[b] = rk[b - 1];
-                    tr[b] = tr[b - 1];
-                }
-                rk[b] = r;
-                tr[b] = t;
-            }
-            if (!seq) {
-                const uint32_t* slots = ctx.edge_slots + (size_t)i * EDGE_SLOTS;
-                auto lookup = [&](uint32_t t, int e) -> const EdgeRes* {
-                    const uint32_t key = (t << 2) | (uint32_t)e;
-                    for (int s = 0; s < nplan; ++s)
-                        if (slots[s] == key) return ctx.edge_res + (size_t)i * EDGE_SLOTS + s;
-                    return nullptr;
-                };
-                for (int j = 0; j < nm; ++j) {
-                    if (BULL) fold_bull_with(ctx, cl, tr[j], cxl, cyl, lookup, capped);
-                    else fold_one(ctx, cl, tr[j], cxl, cyl, capped);
-                }
-            }
-        }
-        if (!seq) {
-            const uint32_t o = ctx.perm[i];
-            ctx.out_z[o] = cl.z;
-            ctx.out_cc[3 * o] = cl.cc.x;
-            ctx.out_cc[3 * o + 1] = cl.cc.y;
-            ctx.out_cc[3 * o + 2] = cl.cc.z;
-            ctx.out_type[o] = cl.type;
-            const double lb = (double)blo + ctx.g.oz;
-            if (cl.z < lb - 1e-9 * (1.0 + fabs(lb))) atomicAdd(&ctx.counters[C_VIOLATION], 1ull);
-            if (n) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)n);
-        }
-    }
-    if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
-    __syncwarp();
-    if (seq) refine_point<BULL>(ctx, i);
-}
-
-template <bool BULL>
-__global__ void __launch_bounds__(128) k_drop_refine_top(const __grid_constant__ DropCtx ctx) {
-    __shared__ TopShared s_top[4];
-    const uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u;
-    if (base >= (uint32_t)ctx.M) return;
-    refine_warp_top<BULL>(ctx, base, s_top[threadIdx.x >> 5]);
-}
-
-// Batch: the bull launch folds every job this way; the other launch takes
-// the cylinders and balls this way and the rest in order.
-template <bool BULL>
-__global__ void __launch_bounds__(128) k_drop_refine_top_b(const __grid_constant__ BatchView bv) {
-    __shared__ DropCtx s_ctx;
-    __shared__ TileState ts;
-    __shared__ TopShared s_top[TILE_POINTS / 32];
-    if (threadIdx.x == 0) ts.job = 0xFFFFFFFFu;
-    uint2 tile;
-    while (batch_next_tile(bv, ts, s_ctx, tile)) {
-        const uint32_t base = tile.y * TILE_POINTS + (threadIdx.x & ~31u);
-        if (base >= (uint32_t)s_ctx.M) continue;
-        if (BULL || (!s_ctx.composite_screen && s_ctx.cp.kind != OCL_CUTTER_CONE))
-            refine_warp_top<BULL>(s_ctx, base, s_top[threadIdx.x >> 5]);
-        else if (base + (threadIdx.x & 31u) < (uint32_t)s_ctx.M)
-            refine_point<false>(s_ctx, base + (threadIdx.x & 31u));
-    }
 }
 
 // One handed-back point of a cylinder, ball or bull cutter, by the whole
@@ -1610,10 +1363,8 @@ static int enqueue_mixed(DropWork& w, const Mesh& m, const CutterP& cp, DropCtx&
         k_bull_eval<<<eb, 128, 0, stream>>>(h, w.edge_queue.p, cnt + C_EDGEQ);
         launches += 2;
     }
-    const unsigned rb = (unsigned)((M + 127) / 128);
-    if (h.edge_res) k_drop_refine_top<true><<<rb, 128, 0, stream>>>(h);
-    else if (!composite && cp.kind != OCL_CUTTER_CONE) k_drop_refine_top<false><<<rb, 128, 0, stream>>>(h);
-    else k_drop_refine<false><<<rb, 128, 0, stream>>>(h);
+    if (h.edge_res) k_drop_refine<true><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
+    else k_drop_refine<false><<<(unsigned)((M + 127) / 128), 128, 0, stream>>>(h);
     if (ev_refine) CK(cudaEventRecord(ev_refine, stream));
     k_collect_overflow<<<nb, TB, 0, stream>>>(w.ncand.p, (int)M, w.list.p, cnt + C_FALLBACK);
     // the fallback grids stride over however many points were handed back
@@ -1764,8 +1515,8 @@ void batch_launch_bull(const BatchView& plan, const BatchView& eval, unsigned bl
 }
 
 void batch_launch_refine(const BatchView& bv, bool bull_plan, unsigned blocks, cudaStream_t stream) {
-    if (bull_plan) k_drop_refine_top_b<true><<<blocks, TILE_POINTS, 0, stream>>>(bv);
-    else k_drop_refine_top_b<false><<<blocks, TILE_POINTS, 0, stream>>>(bv);
+    if (bull_plan) k_drop_refine_b<true><<<blocks, TILE_POINTS, 0, stream>>>(bv);
+    else k_drop_refine_b<false><<<blocks, TILE_POINTS, 0, stream>>>(bv);
 }
 
 void batch_launch_collect(const BatchView& bv, unsigned blocks, cudaStream_t stream) {
