@@ -5,7 +5,8 @@
 //      32 neighbouring points (lanes = CL points).
 //   2. Mixed precision:
 //      k_drop_screen  one warp per 32 points streams the grid cells under the
-//                     warp's footprint, centre rows first.  Cells and then
+//                     warp's footprint, the rows most likely to lift it
+//                     first.  Cells and then
 //                     triangles are rejected with an FP32 upper bound
 //                     (bbox max z minus a lower bound of the cutter profile at
 //                     the bbox distance); survivors get the FP32

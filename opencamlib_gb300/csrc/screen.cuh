@@ -106,8 +106,12 @@ struct WarpPoints {
 };
 constexpr int PF_OVERFLOW = 1, PF_CHAIN = 2;
 
+constexpr int ROWS_SORTED = 64;  // rows of a level the single pass visits best first
+
 struct ScanShared {
     float hlb[HLB_N];
+    int rkey[SCREEN_WARPS][ROWS_SORTED];       // ordered key: a row's highest upper bound for the warp
+    uint8_t rord[SCREEN_WARPS][ROWS_SORTED];   // rows (from r0) in descending key order
     Cell cel[SCREEN_WARPS][32];  // a row's cells, 32 at a time
     Entry ent[SCREEN_WARPS][32];
     BranchTab br[SCREEN_WARPS];
@@ -154,8 +158,8 @@ __device__ __forceinline__ int prune_list(const DropCtx& ctx, uint32_t self, int
     return w;
 }
 
-// One pass over the cells under the warp's footprint (coarse levels first,
-// centre rows first).  Per chunk of 32 grid entries every lane marks the
+// One pass over the cells under the warp's footprint (coarse levels first;
+// rows best first or centre-out, below).  Per chunk of 32 grid entries every lane marks the
 // entries its own point wants screened; the marked (point, triangle) pairs are
 // then spread over all 32 lanes, and each lane applies its results to the
 // pair's point through shared memory.
@@ -226,8 +230,46 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
         const int nr = r1 - r0 + 1, ncl = c1 - c0 + 1;
         const Cell* cells = ctx.cells + g.cell_off[L];
         const int ncol = g.ncol[L];
+        // the cylinder's, ball's and bull's single pass visits the rows in
+        // descending order of their highest upper bound for the warp (a
+        // cell's maxz less the profile's lower bound at its distance from the
+        // points' rectangle), so the bounds rise early; once a row's bound
+        // lies below every lane's threshold, so do the later rows' and the
+        // level is done.  (The cone's bound falls off steeply with the
+        // distance, so the rectangle's nearest distance misleads the order:
+        // measured, it screened more pairs; it keeps the centre-out order.)
+        const bool best_first = KIND == 0 && phase == PH_SINGLE && nr <= ROWS_SORTED;
+        if (best_first) {
+            for (int k = 0; k < nr; ++k) {
+                float best = NEG_INF32;
+                for (int c = c0 + lane; c <= c1; c += 32) {
+                    const Cell cl = cells[(r0 + k) * ncol + c];
+                    const float ex = fmaxf(0.0f, fmaxf(cl.minx - rx1, rx0 - cl.maxx));
+                    const float ey = fmaxf(0.0f, fmaxf(cl.miny - ry1, ry0 - cl.maxy));
+                    const float de = sqrtf(ex * ex + ey * ey);
+                    if (cl.count > 0 && de <= Rg) best = fmaxf(best, cl.maxz - hlb_at(sh.hlb, de - gd, inv_step));
+                }
+                best = warp_max(best);
+                if (lane == 0) sh.rkey[wl][k] = f2o(best);
+            }
+            __syncwarp();
+            for (int k = lane; k < nr; k += 32) {
+                const int key = sh.rkey[wl][k];
+                int rank = 0;
+                for (int j = 0; j < nr; ++j) {
+                    const int kj = sh.rkey[wl][j];
+                    rank += (kj > key || (kj == key && j < k)) ? 1 : 0;
+                }
+                sh.rord[wl][rank] = (uint8_t)k;
+            }
+            __syncwarp();
+        }
     for (int kr = 0; kr < nr; ++kr) {
-        const int r = centre_out(kr, rc, r0, r1);
+        const int r = best_first ? r0 + sh.rord[wl][kr] : centre_out(kr, rc, r0, r1);
+        if (best_first) {
+            const float wc = warp_min(active ? o2f(P.blo[lane]) : 3.0e38f);
+            if (o2f(sh.rkey[wl][r - r0]) < wc - gd) break;
+        }
         if (phase == PH_RESOLVE) {
             if (P.pending[lane] == 0) active = false;
             if (!__any_sync(0xffffffffu, active)) goto done;
@@ -249,6 +291,21 @@ __device__ __forceinline__ void scan_cells(const DropCtx& ctx, ScanShared& sh, i
                     const float ey = fmaxf(0.0f, fmaxf(cl.miny - sy, sy - cl.maxy));
                     const float de = sqrtf(ex * ex + ey * ey);
                     keep = cl.count > 0 && de <= Rg && cl.maxz - hlb_at(sh.hlb, de - gd, inv_step) >= scut - gd;
+                }
+                cmask = __ballot_sync(0xffffffffu, keep);
+            } else {
+                // one cull per staged cell against the whole warp (the points'
+                // rectangle, the lowest threshold; hlb rises with the
+                // distance): a cell it drops fails every lane's own test
+                const float wc =
+                    warp_min(active ? ((phase == PH_SINGLE) ? o2f(P.blo[lane]) : lthr) : 3.0e38f);
+                bool keep = false;
+                if (lane < nck) {
+                    const Cell& cl = sh.cel[wl][lane];
+                    const float ex = fmaxf(0.0f, fmaxf(cl.minx - rx1, rx0 - cl.maxx));
+                    const float ey = fmaxf(0.0f, fmaxf(cl.miny - ry1, ry0 - cl.maxy));
+                    const float de = sqrtf(ex * ex + ey * ey);
+                    keep = cl.count > 0 && de <= Rg && cl.maxz - hlb_at(sh.hlb, de - gd, inv_step) >= wc - gd;
                 }
                 cmask = __ballot_sync(0xffffffffu, keep);
             }
