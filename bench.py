@@ -548,7 +548,7 @@ def roofline_block(tris, M, cuts, breakdown, stage, args, compute):
             "screen_fp32_tflops": screen_f32 / (float(stage[:, 0].sum()) / args.steps / 1e3) / 1e12,
             "peak_source": "ocl_gb300_fma_peaks on this GPU (MEASURED_PEAKS.json has no FP32/FP64 figure)",
             "ops_source": "opencamlib_gb300/roofline.py (ncu instruction counters per screened pair / refined "
-                          "triangle, profiles/compute_ops_drop_block256.md)",
+                          "triangle; the capture is summarised under profiles/)",
             "hbm": hbm_view}
 
 

@@ -17,8 +17,8 @@ those counts into floating-point operations:
 They are the ncu instruction counters (smsp__sass_thread_inst_executed_op_
 {fadd,fmul,ffma,dadd,dmul,dfma}_pred_on.sum) summed over the kernels of one
 call on the 256 x 256-point block of the benchmark raster, divided by that
-call's own counters; the capture and the arithmetic are in
-profiles/compute_ops_drop_block256.md.  A step's roofline time is then
+call's own counters (the capture and the arithmetic are kept with the ncu
+summaries under profiles/).  A step's roofline time is then
 
   T_roof = sum_c screened_c * FP32_PER_SCREEN[c] / P32
          + sum_c refined_c  * FP64_PER_REFINED[c] / P64
@@ -27,9 +27,9 @@ with P32, P64 the FMA throughput measured on the device
 (ocl_gb300_fma_peaks), and the fraction is T_roof / T_step.
 
 SCREEN_DRAM_BYTES[c] is the DRAM traffic (dram__bytes_read.sum +
-dram__bytes_write.sum) of the screen kernels of one call on the full
-1,000,000-point raster, from a one-pass ncu capture
-(profiles/k_drop_screen_dram_full_size.md).
+dram__bytes_write.sum) of the screen kernels (seeding, dense and sparse
+screen) of one call on the full 1,000,000-point raster, from a one-pass
+ncu capture of `bench.py --profile-step` (summarised under profiles/).
 """
 from __future__ import annotations
 
@@ -38,7 +38,7 @@ FP32_PER_SCREEN = {"cyl": 912.6, "ball": 1111.4, "bull": 1491.2, "cone": 1202.4,
 # cutter -> FP64 operations per refined triangle
 FP64_PER_REFINED = {"cyl": 122.1, "ball": 237.4, "bull": 1274.8, "cone": 295.3, "ballcone": 320.6}
 # cutter -> DRAM bytes of the screen kernels per call on the 1,000,000-point raster
-SCREEN_DRAM_BYTES = {"cyl": None, "ball": None, "bull": None, "cone": None, "ballcone": None}
+SCREEN_DRAM_BYTES = {"cyl": 784473344, "ball": 688323584, "bull": 854738432, "cone": 547958272, "ballcone": 959312384}
 
 
 def measured(names) -> bool:
