@@ -359,7 +359,7 @@ __device__ __forceinline__ void bull_plan_point(const DropCtx& ctx, const uint32
                 }
             }
         }
-        ctx.edge_n[i] = (uint8_t)min(cnt, 255);
+        ctx.edge_n[i] = (uint8_t)min(cnt, EDGE_N_SATURATED);
     }
     // one queue reservation per warp
     const int mine = min(cnt, EDGE_SLOTS);
@@ -521,7 +521,11 @@ __device__ __forceinline__ void refine_point(const DropCtx& ctx, const uint32_t 
     const double tcut = (double)ctx.blo[i] + ctx.g.oz - (double)ctx.guard;
     const float zfloor = ctx.composite_screen || ctx.cp.kind == OCL_CUTTER_CONE ? -3.0e38f : ctx.blo[i];
     int slot = 0;
-    const int nplan = ctx.edge_res ? ctx.edge_n[i] : 0;
+    // planned edges of the point; 255 is a saturated count (more were
+    // planned): past the stored slots the fold repeats the plan's test for
+    // every edge, so it stops only at a count it knows
+    int nplan = ctx.edge_res ? ctx.edge_n[i] : 0;
+    if (nplan == EDGE_N_SATURATED) nplan = 0x7FFFFFFF;
     for (int q = 0; q < n; ++q) {
         const uint32_t tq = tri[q] & ~CAND_VERIFY;
         if (BULL_PLAN) {
@@ -769,141 +773,11 @@ __device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsi
     }
 }
 
-// One triangle's drop from height z (out of line: the scan around it keeps
-// its registers).
-__device__ __noinline__ CL64 drop_from(const DropCtx& ctx, double x, double y, double z, uint32_t tri, float cx,
-                                       float cy, int& capped, float zfloor) {
-    CL64 m{x, y, z, d3(0, 0, 0), OCL_CC_NONE};
-    fold_one(ctx, m, tri, cx, cy, capped, zfloor);
-    return m;
-}
-
-// One handed-back point of a cylinder, ball or bull cutter, by the whole
-// block, when the candidates reaching the fold threshold are many.  A
-// triangle's drop from a height is its facet contact if that lifts, else
-// the highest of its vertex and edge contacts that lifts, and passes over
-// the triangle if its bbox top is not above the height (the reference's
-// short-circuit and below test); the vertex and edge contacts agree with
-// the facet contact up to rounding.  So the fold's result lies within
-// rounding of the highest drop from below, Mmax: every thread evaluates its
-// share of the triangles (FP32 upper bound reaching the threshold) from the
-// threshold in FP64 and the block reduces the maximum; then only the
-// triangles whose drop from below comes within delta (far above rounding) of
-// it can decide the result: they are gathered, sorted by KD rank and folded
-// in order with the exact per-triangle code (a triangle further below lifts
-// the height to below them and cannot stop one of them).  Returns false,
-// with nothing written, when more than EXACT_CAP triangles come within delta
-// (the general path then takes the point).
-__device__ __noinline__ bool exact_point_top(const DropCtx& ctx, const uint32_t i, const ExactShared& S) {
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const GridP& g = ctx.g;
-    const double x = ctx.cl[3 * i], y = ctx.cl[3 * i + 1], z0 = ctx.cl[3 * i + 2];
-    const float cx = (float)(x - g.ox), cy = (float)(y - g.oy);
-    const float z0l = __double2float_rd(z0 - g.oz);
-    const float gd = ctx.guard;
-    const float tcut = ctx.blo[i] > NEG_INF32 ? ctx.blo[i] - gd : NEG_INF32;
-    const double t64 = tcut > NEG_INF32 ? fmax(z0, (double)tcut + g.oz) : z0;
-    const float R = ctx.prof.R, Rg = R + gd, inv_step = (float)HLB_N / R;
-    const double reach = ctx.cp.radius + 1e-9 * (1.0 + ctx.cp.radius);
-    // visits every triangle under the cutter whose FP32 upper bound reaches `cut`
-    auto scan = [&](float cut, auto&& visit) {
-        for (int L = g.nlev - 1; L >= 0; --L) {
-            int c0, c1, r0, r1;
-            if (!warp_rect(g, L, x, x, y, y, reach, c0, c1, r0, r1)) continue;
-            const int ncl = c1 - c0 + 1, ncells = ncl * (r1 - r0 + 1);
-            const Cell* cells = ctx.cells + g.cell_off[L];
-            for (int k = tid; k < ncells; k += blockDim.x) {
-                const Cell cell = cells[(r0 + k / ncl) * g.ncol[L] + c0 + k % ncl];
-                if (cell.count == 0) continue;
-                const float dx = fmaxf(0.0f, fmaxf(cell.minx - cx, cx - cell.maxx));
-                const float dy = fmaxf(0.0f, fmaxf(cell.miny - cy, cy - cell.maxy));
-                const float d = sqrtf(dx * dx + dy * dy);
-                const float cub = cell.maxz - hlb_at(S.hlb, d - gd, inv_step);
-                if (!(d <= Rg && cub > z0l - gd && cub >= cut - gd)) continue;
-                for (uint32_t j = 0; j < cell.count; ++j) {
-                    const Entry e = ctx.entries[cell.start + j];
-                    const float ex = fmaxf(0.0f, fmaxf(e.minx - cx, cx - e.maxx));
-                    const float ey = fmaxf(0.0f, fmaxf(e.miny - cy, cy - e.maxy));
-                    const float de = sqrtf(ex * ex + ey * ey);
-                    const float ub = e.maxz - hlb_at(S.hlb, de - gd, inv_step);
-                    if (!(de <= Rg && ub > z0l - gd && ub >= cut - gd)) continue;
-                    const Tri32 t = ctx.t32[e.tri];
-                    float qt, qth;
-                    const Iv v =
-                        screen_triangle(ctx.prof, t, cx - t.v0[0], cy - t.v0[1], ctx.E, z0l - t.v0[2], qt, qth);
-                    if (!(v.hi > NEG_INF32)) continue;
-                    const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
-                    if (!(hi > z0l - gd && hi >= cut)) continue;
-                    visit((uint32_t)e.tri, t.kd_rank, hi);
-                }
-            }
-        }
-    };
-    double bz = -1e300;
-    int capped = 0;
-    unsigned evals = 0;
-    scan(tcut, [&](uint32_t tri, uint32_t, float) {
-        const CL64 m = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
-        ++evals;
-        if (m.z > t64) bz = fmax(bz, m.z);
-    });
-    for (int o = 16; o > 0; o >>= 1) bz = fmax(bz, __shfl_xor_sync(0xffffffffu, bz, o));
-    double* wz = reinterpret_cast<double*>(S.key);  // per-warp maxima (the key array is idle)
-    if (lane == 0) wz[wid] = bz;
-    __syncthreads();
-    double mmax = -1e300;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mmax = fmax(mmax, wz[w]);
-    if (tid == 0) *S.n = 0;
-    __syncthreads();
-    CL64 cl{x, y, z0, d3(0, 0, 0), OCL_CC_NONE};
-    unsigned ev2 = 0;
-    if (mmax > -1e300) {
-        const double top = mmax - 1e-9 * (1.0 + fabs(mmax));
-        scan(__double2float_rd(top - g.oz), [&](uint32_t tri, uint32_t rank, float hi) {
-            const CL64 m = drop_from(ctx, x, y, t64, tri, cx, cy, capped, tcut);
-            ++ev2;
-            if (!(m.z >= top)) return;
-            const int slot = atomicAdd(S.n, 1);
-            if (slot < EXACT_CAP) {
-                S.key[slot] = ((unsigned long long)rank << 32) | (unsigned)slot;
-                S.tri[slot] = tri;
-                S.hi[slot] = hi;
-            }
-        });
-        __syncthreads();
-        const int n2 = *S.n;
-        __syncthreads();
-        if (n2 > EXACT_CAP) return false;
-        exact_sort(S.key, n2);
-        if (tid < 32) exact_fold<false>(ctx, cl, S.key, n2, S.hi, S.tri, cx, cy, capped, ev2);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        evals += __shfl_xor_sync(0xffffffffu, evals, o);
-        ev2 += __shfl_xor_sync(0xffffffffu, ev2, o);
-        capped += __shfl_xor_sync(0xffffffffu, capped, o);
-    }
-    if (lane == 0) {
-        if (evals + ev2) atomicAdd(&ctx.counters[C_REFINED], (unsigned long long)(evals + ev2));
-        if (capped) atomicAdd(&ctx.counters[C_CAPPED], (unsigned long long)capped);
-    }
-    if (tid == 0) {
-        const uint32_t o = ctx.perm[i];
-        ctx.out_z[o] = cl.z;
-        ctx.out_cc[3 * o] = cl.cc.x;
-        ctx.out_cc[3 * o + 1] = cl.cc.y;
-        ctx.out_cc[3 * o + 2] = cl.cc.z;
-        ctx.out_type[o] = cl.type;
-    }
-    __syncthreads();
-    return true;
-}
-
 // One handed-back point, by the whole block.
 template <bool COMP>
 __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
                                             const ExactGlobal& G, uint32_t* __restrict__ list2,
                                             unsigned long long* __restrict__ nlist2) {
-    if (!COMP && ctx.cp.kind != OCL_CUTTER_CONE && exact_point_top(ctx, i, S)) return;
     unsigned long long* s_key = S.key;
     int& s_red = *S.red;
     const int tid = threadIdx.x, lane = tid & 31;

@@ -10,6 +10,7 @@ constexpr int CAND_K = 256;  // refinement candidates kept per CL point (drop_ru
 constexpr int CAND_K_NOALLOC = 64;  // the same for the no-allocation entry point
 constexpr uint32_t CAND_VERIFY = 0x80000000u;  // list flag: decide this triangle's branch in FP64
 constexpr int EDGE_SLOTS = 8;  // bull edge contacts evaluated ahead of the fold, per CL point
+constexpr int EDGE_N_SATURATED = 255;  // per-point planned-edge count: this many or more
 
 struct EdgeRes {  // one edge contact (MillingCutter::singleEdgeDrop), running-height independent
     double clz, ccx, ccy, ccz;
@@ -62,7 +63,7 @@ struct DropCtx {
     unsigned long long* sparse_n;
     // bull: edge contacts evaluated ahead of the fold (null: evaluated inline)
     uint32_t* edge_slots;   // M x EDGE_SLOTS: (triangle << 2 | edge) in fold order
-    uint8_t* edge_n;        // per CL: planned edges (may exceed EDGE_SLOTS)
+    uint8_t* edge_n;        // per CL: planned edges (may exceed EDGE_SLOTS; EDGE_N_SATURATED: that many or more)
     struct EdgeRes* edge_res;  // M x EDGE_SLOTS results
     unsigned long long* counters;
     // hand-back lists and the bull edge queue of this call (read from here by

@@ -68,3 +68,29 @@ def test_mixed_equals_fp64_and_oracle(ocl, oracle_lib, cname, seed):
     _cmp(z64, cc64, ty64, zr, ccr, tyr)
     # the FP64 path evaluates exactly the reference's overlap pairs
     assert s64.pairs == oracle_lib.overlap_pairs(tris, c.radius, cl)
+
+
+def test_bull_near_a_sphere_pole(ocl, oracle_lib):
+    """Near the pole of a UV sphere hundreds of thin triangles share one
+    vertex, and a bull's point plans more edges than the per-point count
+    holds (it saturates at 255): the fold must keep testing the edges past
+    the count itself.  Three points whose highest contact lies on such an
+    edge; mixed must equal plain FP64 bit for bit, and the oracle."""
+    from opencamlib_gb300 import cutters as cu
+    tris = w.mesh_of_size("sphere", 213172, 3034)
+    d = 8.047591839070233
+    c = cu.BullCutter(d, d / 6.0, 20.0)
+    pts = np.array([[48.36041448314995, 47.790720164255156, -50.0],
+                    [48.196455931464946, 47.95437052245848, -50.0],
+                    [47.86853882809494, 48.28167123886512, -50.0]])
+    mesh = ocl.DeviceMesh(tris)
+    z, cc, ty, st = mesh.drop(c, pts, precision="mixed")
+    assert st.violations == 0
+    z64, cc64, ty64, _ = mesh.drop(c, pts, precision="fp64")
+    np.testing.assert_array_equal(z, z64)
+    np.testing.assert_array_equal(cc, cc64)
+    np.testing.assert_array_equal(ty, ty64)
+    # the bull's device trigonometry may differ from the host's by an ulp
+    zr, ccr, tyr = oracle_lib.drop(tris, c, pts, "port")[:3]
+    np.testing.assert_allclose(z, zr, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(ty, tyr)

@@ -77,8 +77,7 @@ LARGE = {
     # global scratch and folded one rank window at a time
     "compcyl": lambda: cu.CompCylCutter(6.0, 20.0),
     "cylcone": lambda: cu.CylConeCutter(2.0, 6.0, math.pi / 4),
-    # the block-parallel maximum, then the in-order fold of the triangles
-    # near it (all of the ~10,000 ties here: the general path takes over)
+    # the flat-bottomed basic cutters the same way
     "cyl": lambda: cu.CylCutter(6.0, 20.0),
     "bull": lambda: cu.BullCutter(6.0, 1.0, 20.0),
 }
@@ -101,8 +100,7 @@ def test_exact_kernel_windows_over_large_lists(ocl, oracle_lib, name):
 
 def test_plain_kernel_takes_the_largest_lists(ocl, oracle_lib):
     # 1024 x 1024 cells over 12 mm: ~400,000 tied triangles under a 6 mm
-    # flat bottom, more than the exact kernel's global scratch holds (and,
-    # for the cylinder, more ties at the top than its shared memory holds)
+    # flat bottom, more than the exact kernel's global scratch holds
     tris = flat_plate(1025)
     cl = points(16, 6)
     mesh = ocl.DeviceMesh(tris)
@@ -148,11 +146,10 @@ def test_handed_back_points_on_the_bump_field(ocl):
 @pytest.mark.parametrize("name,cutter", [("cyl20", lambda: cu.CylCutter(20.0, 40.0)),
                                          ("bull12", lambda: cu.BullCutter(12.0, 2.0, 24.0)),
                                          ("ball10", lambda: cu.BallCutter(10.0, 20.0))])
-def test_exact_max_path_with_tiny_lists(ocl, name, cutter):
+def test_exact_kernel_with_tiny_lists(ocl, name, cutter):
     """Lists of 16 candidates hand almost every point of a box with fillets
-    back to the exact kernel; its block-parallel maximum (with the replay of
-    the below test where a contact lies above its own triangle's top) must
-    equal the plain FP64 kernel, which folds every candidate in KD order."""
+    back to the exact kernel; its gather-sort-fold must equal the plain FP64
+    kernel, which folds every candidate in KD order."""
     import torch
     tris = w.mesh_of_size("box", 30000, 7)
     c = cutter()
@@ -169,5 +166,32 @@ def test_exact_max_path_with_tiny_lists(ocl, name, cutter):
     torch.cuda.synchronize()
     assert st.violations == 0
     assert st.fallback > 0 or name == "ball10"  # a ball's lists rarely reach 16
+    z64, cc64, ty64, _ = mesh.drop(c, pts, precision="fp64")
+    _same((d_z.cpu().numpy(), d_cc.cpu().numpy(), d_ty.cpu().numpy()), (z64, cc64, ty64))
+
+
+@pytest.mark.parametrize("name,cutter", [("cyl17", lambda: cu.CylCutter(17.0, 40.0)),
+                                         ("bull18", lambda: cu.BullCutter(18.0, 3.0, 40.0)),
+                                         ("ballcone", lambda: cu.BallConeCutter(2.0, 12.0, math.pi / 4))])
+def test_large_cutters_on_a_heightfield_with_short_lists(ocl, name, cutter):
+    """Large cutters over a heightfield with lists of 16 candidates (the
+    batch autotuner's shortest): thousands of triangles under each cutter,
+    points refined or handed back as their lists allow; the batch must equal
+    the plain FP64 kernel bit for bit."""
+    import torch
+    tris = w.mesh_of_size("heightfield", 60000, 5)
+    c = cutter()
+    pts = w.batch_points(tris, 6000, c.radius)
+    mesh = ocl.DeviceMesh(tris)
+    d_cl = torch.from_numpy(pts).cuda()
+    M = len(pts)
+    d_z = torch.empty(M, dtype=torch.float64, device="cuda")
+    d_cc = torch.empty((M, 3), dtype=torch.float64, device="cuda")
+    d_ty = torch.empty(M, dtype=torch.int32, device="cuda")
+    b = ocl.DropBatch([(mesh, c, d_cl.data_ptr(), M, d_z.data_ptr(), d_cc.data_ptr(), d_ty.data_ptr())],
+                      list_capacity=16)
+    st = b.run(stats=True)
+    torch.cuda.synchronize()
+    assert st.violations == 0
     z64, cc64, ty64, _ = mesh.drop(c, pts, precision="fp64")
     _same((d_z.cpu().numpy(), d_cc.cpu().numpy(), d_ty.cpu().numpy()), (z64, cc64, ty64))
