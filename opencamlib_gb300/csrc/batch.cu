@@ -566,9 +566,12 @@ int prepare(Batch& b, cudaStream_t stream) {
 
 // Candidate-list capacity and screen grid size per variant, timed on a
 // probe: the middle 4,096 points of up to 32 chunks of the variant, each
-// configuration run twice (the second run timed).
+// configuration run twice (the second run timed).  Lists of 64 are not
+// tried: the probe's contiguous middles miss the regions whose lists
+// overflow (flat faces, fans of thin triangles), and on the 64-job workload
+// 64-entry lists handed back 1.36M points instead of 0.30M.
 int autotune(Batch& b, const std::vector<SubJob>& all, cudaStream_t stream) {
-    const int caps[3] = {64, 128, 256};
+    const int caps[2] = {128, 256};
     const int mults[2] = {1, 2};
     std::vector<Variant> vs;
     for (const SubJob& s : all)
