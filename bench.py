@@ -369,6 +369,19 @@ def batch_measurements(steps=2, warmup=1, njobs=64, autotune=True):
     st = batch.run(stream.cuda_stream, stats=True)
     torch.cuda.synchronize()
     same = all(torch.equal(j["out"][k], j["ref"][k]) for j in jobs for k in range(3))
+    # every job's mixed results against the plain FP64 kernel on a seeded
+    # sample of its points (the batch equals the single calls, so this pins
+    # both to the reference's arithmetic)
+    rng = np.random.default_rng(11)
+    sample_points = sample_bad = 0
+    for j in jobs:
+        idx = np.sort(rng.choice(j["M"], size=min(j["M"], 2000), replace=False))
+        pts = j["cl"].cpu().numpy()[idx]
+        z64, cc64, ty64, _ = j["mesh"].drop(j["cutter"], pts, precision="fp64")
+        zb, ccb, tyb = (j["out"][0].cpu().numpy()[idx], j["out"][1].cpu().numpy()[idx],
+                        j["out"][2].cpu().numpy()[idx])
+        sample_points += len(idx)
+        sample_bad += int(np.sum((zb != z64) | (tyb != ty64) | np.any(ccb != cc64, axis=1)))
     info = batch.info()
     out = {"jobs": len(jobs), "points": int(total), "triangles": int(sum(j["tris"] for j in jobs)),
            "setup_s": setup_s, "batch_create_s": create_s,
@@ -376,6 +389,8 @@ def batch_measurements(steps=2, warmup=1, njobs=64, autotune=True):
            "one_call_per_job_points_per_s": total / (np.median(t_single) / 1e3),
            "batch_points_per_s": total / (np.median(t_batch) / 1e3),
            "speedup": float(np.median(t_single) / np.median(t_batch)), "bit_identical": bool(same),
+           "fp64_sample": {"points": sample_points, "mismatched": sample_bad,
+                           "sample": "2,000 seeded points per job (all of a smaller job), plain FP64 kernel"},
            "violations": int(st.violations), "handed_back_points": int(st.fallback), "plain_points": int(st.plain_points),
            "launches_per_run": info["launches_per_run"], "waves": info["waves"], "chunks": info["chunks"],
            "workspace_bytes": info["workspace_bytes"], "tuned": info["variants"],

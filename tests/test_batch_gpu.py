@@ -134,3 +134,30 @@ def test_batch_errors(env):
     assert e.value.status == _abi.BAD_ARG
     with pytest.raises(ocl.OclError):
         _batch(ocl, dev, jobs[:2], bufs, list_capacity=4)
+
+
+def test_batching_workload_sample_against_fp64(env):
+    """Jobs of the 64-job batching workload (seeded heightfield, sphere and
+    box meshes; the five cutter families at diameters up to 20 mm): each
+    job's mixed results on a seeded sample of its points (scattered, so the
+    sparse screen runs too) must equal the plain FP64 kernel's bit for bit.
+    Every job whose mesh has at most 250,000 triangles (47 of the 64; job 34
+    among them: a sphere whose pole fans out hundreds of thin triangles)."""
+    ocl, torch = env
+    specs = w.batch_jobs(seed=3, njobs=64)
+    chosen = [k for k in range(len(specs)) if specs[k]["N"] <= 250000]
+    rng = np.random.default_rng(5)
+    for k in chosen:
+        sp = specs[k]
+        tris = w.mesh_of_size(sp["mesh"], sp["N"], sp["seed"])
+        c = w.batch_cutter(sp["cutter"], sp["d"])
+        pts = w.batch_points(tris, sp["M"], c.radius)
+        sel = pts[np.sort(rng.choice(len(pts), size=min(len(pts), 1500), replace=False))]
+        mesh = ocl.DeviceMesh(tris)
+        z, cc, ty, st = mesh.drop(c, sel, precision="mixed")
+        assert st.violations == 0, f"job {k}"
+        z64, cc64, ty64, _ = mesh.drop(c, sel, precision="fp64")
+        np.testing.assert_array_equal(z, z64, err_msg=f"job {k} z")
+        np.testing.assert_array_equal(cc, cc64, err_msg=f"job {k} cc")
+        np.testing.assert_array_equal(ty, ty64, err_msg=f"job {k} type")
+        mesh.release()
