@@ -600,6 +600,7 @@ struct ExactShared {
     float* hlb;
     int* n;
     int* red;
+    unsigned long long* pre;  // two words: the pre-fold's lowest key, its running height
 };
 
 // Per-block global scratch of the exact kernel for points with more than
@@ -619,13 +620,16 @@ constexpr int EXACT_BINS = 1024;          // rank histogram of the large path's 
 
 // (Out of line: one copy serves the shared-memory and the global path.)
 // Gather every triangle whose certified FP32 upper bound lies above the start
-// height and reaches tcut into (key, tri, hi, qt)[slot] for slot < cap (one
-// thread per grid cell under the cutter, all levels); returns the number found
-// (may exceed cap).
+// height and reaches tcut into (key, tri, hi, qt)[slot] for slot < cap, and
+// into the global scratch (gkey, ...)[slot] for cap <= slot < gcap (gkey may
+// be null); one thread per grid cell under the cutter, all levels.  Returns
+// the number found (may exceed both).
 template <bool COMP>
 __device__ __noinline__ int exact_gather(const DropCtx& ctx, double x, double y, float cx, float cy, float z0l,
                                             float tcut, const float* s_hlb, int& s_n, unsigned long long* key,
-                                            uint32_t* tri, float* hiv, float* qtv, int cap) {
+                                            uint32_t* tri, float* hiv, float* qtv, int cap,
+                                            unsigned long long* gkey, uint32_t* gtri, float* ghi, float* gqt,
+                                            int gcap) {
     const int tid = threadIdx.x;
     const GridP& g = ctx.g;
     const float R = ctx.prof.R, gd = ctx.guard, Rg = R + gd, inv_step = (float)HLB_N / R;
@@ -660,11 +664,18 @@ __device__ __noinline__ int exact_gather(const DropCtx& ctx, double x, double y,
                 const float hi = fminf(v.hi + t.v0[2] + ctx.E, ub + gd);
                 if (!(hi > z0l - gd && hi >= tcut)) continue;
                 const int slot = atomicAdd(&s_n, 1);
+                const unsigned long long kk = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
+                const float qv = qt < 3.0e38f ? qt + t.v0[2] - ctx.E : 3.0e38f;
                 if (slot < cap) {
-                    key[slot] = ((unsigned long long)t.kd_rank << 32) | (unsigned)slot;
+                    key[slot] = kk;
                     tri[slot] = (uint32_t)e.tri;
                     hiv[slot] = hi;
-                    qtv[slot] = qt < 3.0e38f ? qt + t.v0[2] - ctx.E : 3.0e38f;
+                    qtv[slot] = qv;
+                } else if (gkey && slot < gcap) {
+                    gkey[slot] = kk;
+                    gtri[slot] = (uint32_t)e.tri;
+                    ghi[slot] = hi;
+                    gqt[slot] = qv;
                 }
             }
         }
@@ -773,6 +784,84 @@ __device__ __noinline__ void exact_fold(const DropCtx& ctx, CL64& cl, const unsi
     }
 }
 
+// Entries of the exact kernel's key arrays that are out of the fold: the
+// rank word all ones (they sort after every kept key), the slot kept.
+constexpr unsigned long long EXACT_DROPPED = 0xFFFFFFFF00000000ull;
+constexpr int EXACT_PREFOLD = 4;   // pre-fold rounds at most
+constexpr int EXACT_FEW = 64;      // kept triangles the sorted fold takes on cheaply
+
+// Pre-fold of a handed-back point, by the whole block, before its kept
+// triangles are sorted: warp 0 folds the lowest-ranked kept triangle (the
+// first step of the in-order fold), then every kept triangle that can no
+// longer lift is dropped -- its bbox top at or below the running height (the
+// reference's below test skips it at this and every higher height) or its
+// FP32 upper bound below the running height less the guard (the sorted
+// fold's own skip) -- and the lowest-ranked of the rest is next, while many
+// remain.  On a flat face under a flat-bottomed cutter, hundreds of
+// triangles tie at the face's height; the first fold reaches it and drops
+// them all, so they are neither sorted nor folded.  cl (warp 0's running
+// point) carries on into the sorted fold.  Returns the kept count.
+template <bool COMP>
+__device__ __noinline__ int exact_prefold(const DropCtx& ctx, CL64& cl, unsigned long long* key, const float* hiv,
+                                          const uint32_t* tri, int n, float cx, float cy, int& capped,
+                                          unsigned& evals, unsigned long long* s_min, int& s_cnt) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const float gd = ctx.guard;
+    int nk = n;
+    double* s_z = reinterpret_cast<double*>(s_min + 1);
+    for (int it = 0; it < EXACT_PREFOLD; ++it) {
+        if (tid == 0) *s_min = ~0ull;
+        __syncthreads();
+        unsigned long long m = ~0ull;
+        for (int k = tid; k < n; k += blockDim.x) {
+            const unsigned long long kk = key[k];
+            if ((kk >> 32) != 0xFFFFFFFFull && kk < m) m = kk;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+            if (v < m) m = v;
+        }
+        if (lane == 0 && m != ~0ull) atomicMin(s_min, m);
+        __syncthreads();
+        const unsigned long long best = *s_min;
+        if (best == ~0ull) {
+            nk = 0;
+            break;
+        }
+        if (tid < 32) {
+            // every lane of warp 0 folds it (cl stays the same across the warp)
+            int c1 = 0;
+            fold_one(ctx, cl, tri[(uint32_t)best], cx, cy, c1);
+            if (lane == 0) {
+                ++evals;
+                capped += c1;
+            }
+        }
+        if (tid == 0) {
+            *s_z = cl.z;
+            s_cnt = 0;
+        }
+        __syncthreads();
+        const double Z = *s_z;
+        const float zl = __double2float_rd(Z - ctx.g.oz);
+        int kept = 0;
+        for (int k = tid; k < n; k += blockDim.x) {
+            const unsigned long long kk = key[k];
+            if ((kk >> 32) == 0xFFFFFFFFull) continue;
+            const uint32_t slot = (uint32_t)kk;
+            if (kk == best || !(hiv[slot] + gd >= zl) || !(Z < ctx.t64[tri[slot]].bb[5])) key[k] = EXACT_DROPPED | slot;
+            else ++kept;
+        }
+        for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+        if (lane == 0 && kept) atomicAdd(&s_cnt, kept);
+        __syncthreads();
+        nk = s_cnt;
+        __syncthreads();
+        if (nk <= EXACT_FEW) break;
+    }
+    return nk;
+}
+
 // One handed-back point, by the whole block.
 template <bool COMP>
 __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i, const ExactShared& S,
@@ -800,7 +889,9 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
     float T = NEG_INF32;
     bool in_shared = true;
     for (int pass = 0;; ++pass) {
-        n = exact_gather<COMP>(ctx, x, y, cx, cy, z0l, tcut, S.hlb, *S.n, s_key, S.tri, S.hi, S.qt, EXACT_CAP);
+        // the global scratch takes what shared memory cannot hold
+        n = exact_gather<COMP>(ctx, x, y, cx, cy, z0l, tcut, S.hlb, *S.n, s_key, S.tri, S.hi, S.qt, EXACT_CAP,
+                               G.key ? gk : nullptr, gt, gh, gq, G.cap);
         in_shared = n <= EXACT_CAP;
         if (!in_shared) {
             if (!(G.key && n <= G.cap)) {
@@ -808,7 +899,15 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
                 __syncthreads();
                 return;
             }
-            exact_gather<COMP>(ctx, x, y, cx, cy, z0l, tcut, S.hlb, *S.n, gk, gt, gh, gq, G.cap);
+            // the first EXACT_CAP entries are in shared memory: all into the
+            // global scratch (the slot in a key's low word is its index there)
+            for (int k = tid; k < EXACT_CAP; k += blockDim.x) {
+                gk[k] = s_key[k];
+                gt[k] = S.tri[k];
+                gh[k] = S.hi[k];
+                gq[k] = S.qt[k];
+            }
+            __syncthreads();
         }
         T = in_shared ? exact_threshold(ctx, i, S.hi, S.qt, n, s_red) : exact_threshold(ctx, i, gh, gq, n, s_red);
         if (!(T < tcut)) break;
@@ -823,11 +922,14 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
         int kept = 0;
         for (int k = tid; k < n; k += blockDim.x) {
             if (S.hi[k] >= T) ++kept;
-            else s_key[k] = ~0ull;  // sorts after the kept keys
+            else s_key[k] = EXACT_DROPPED | (unsigned)k;  // sorts after the kept keys
         }
         if (kept) atomicAdd(&s_red, kept);
         __syncthreads();
-        const int nk = s_red;
+        int nk = s_red;
+        __syncthreads();
+        if (nk > EXACT_FEW)
+            nk = exact_prefold<COMP>(ctx, cl, s_key, S.hi, S.tri, n, cx, cy, capped, evals, S.pre, s_red);
         exact_sort(s_key, n);
         if (tid < 32) exact_fold<COMP>(ctx, cl, s_key, nk, S.hi, S.tri, cx, cy, capped, evals);
     } else {
@@ -835,10 +937,10 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
         // block's global scratch and folded in KD order one rank window at a
         // time (each window's ranks chosen so it fits shared memory), the
         // running height carried from window to window.
-        constexpr unsigned long long DROPPED = 0xFFFFFFFF00000000ull;
         for (int k = tid; k < n; k += blockDim.x)
-            if (!(gh[k] >= T)) gk[k] = DROPPED | (unsigned)k;
+            if (!(gh[k] >= T)) gk[k] = EXACT_DROPPED | (unsigned)k;
         __syncthreads();
+        exact_prefold<COMP>(ctx, cl, gk, gh, gt, n, cx, cy, capped, evals, S.pre, s_red);
         int* hist = reinterpret_cast<int*>(S.qt);  // the shared thresholds are not used on this path
         uint64_t cur = 0;
         for (;;) {
@@ -936,6 +1038,7 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
     extern __shared__ unsigned long long s_key[];                                            \
     __shared__ float s_hlb[HLB_N];                                                           \
     __shared__ int s_n, s_red;                                                               \
+    __shared__ unsigned long long s_pre[2];                                                  \
     ExactShared S;                                                                           \
     S.key = s_key;                                                                           \
     S.tri = reinterpret_cast<uint32_t*>(s_key + EXACT_CAP);                                  \
@@ -943,7 +1046,8 @@ __device__ __forceinline__ void exact_point(const DropCtx& ctx, const uint32_t i
     S.qt = S.hi + EXACT_CAP;                                                                 \
     S.hlb = s_hlb;                                                                           \
     S.n = &s_n;                                                                              \
-    S.red = &s_red;
+    S.red = &s_red;                                                                          \
+    S.pre = s_pre;
 
 template <bool COMP>
 __global__ void __launch_bounds__(EXACT_THREADS) k_drop_exact(const __grid_constant__ DropCtx ctx,
