@@ -27,3 +27,13 @@ def test_step_roofline_arithmetic():
     assert r["frac"] == pytest.approx(r["t_roof_s"] / 0.01)
     # one FP32-equivalent rate against the FP32 peak gives the same fraction
     assert r["achieved_flops_fp32_equiv"] / p32 == pytest.approx(r["frac"])
+
+
+def test_every_benchmark_cutter_has_screen_traffic():
+    """roofline.traffic: the screens' DRAM bytes per call on the full raster,
+    from a one-pass ncu capture; at least the algorithmic bytes of a call
+    (every triangle's FP64 vertices once, 24 B in and 36 B out per point)."""
+    algorithmic = 1_048_576 * 72 + 1_000_000 * (24 + 36)
+    for n in cu.standard_cutters():
+        b = rf.SCREEN_DRAM_BYTES[n]
+        assert b is not None and algorithmic <= b < 20 * algorithmic
