@@ -71,7 +71,32 @@ def parse():
     ap.add_argument("--wl-cutters", default="ball,bull", help="waterline cutters (ball, bull)")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one device step with statistics, print its counters and exit (for ncu)")
+    ap.add_argument("--serve-request", type=int, default=-1,
+                    help="drop the middle --serve-points points of this drop request of the serving workload "
+                         "once, print its counters and exit (a small case for profiling)")
+    ap.add_argument("--serve-points", type=int, default=8192)
     return ap.parse_args()
+
+
+def serve_request_case(k: int, npts: int) -> dict:
+    """One drop request of the serving workload (workloads.serving_requests(5,
+    200)[k] on its resident mesh), cut to its middle npts points, dropped once
+    in mixed precision; returns the call's counters."""
+    from opencamlib_gb300 import _native, workloads as w
+    meshes = w.serving_meshes(5, 8)
+    r = w.serving_requests(5, 200)[k]
+    if r["kind"] != "drop":
+        raise SystemExit(f"request {k} is not a drop request")
+    tris = meshes[r["mesh"]]
+    c = w.batch_cutter(r["cutter"], r["d"])
+    pts = w.serving_payload(r, tris)
+    mid = len(pts) // 2
+    pts = pts[max(0, mid - npts // 2): mid + npts // 2]
+    z, cc, ty, st = _native.DeviceMesh(tris).drop(c, pts, "mixed")
+    return {"request": k, "triangles": int(len(tris)), "cutter": r["cutter"], "d": r["d"], "points": int(len(pts)),
+            "handed_back": int(st.fallback), "plain_points": int(st.plain_points), "refined": int(st.refined),
+            "kernel_ms": st.kernel_ms, "screen_ms": st.screen_ms, "refine_ms": st.refine_ms,
+            "fallback_ms": st.fallback_ms}
 
 
 class ClockSampler:
@@ -609,6 +634,9 @@ def main():
     if args.waterline_only:
         wl = aux_measurements(None, None, not args.no_cpu_baseline, args.wl_levels, args.wl_cutters.split(","))
         print(json.dumps({"waterline": wl["waterline"]}), flush=True)
+        return
+    if args.serve_request >= 0:
+        print(json.dumps({"serve_request": serve_request_case(args.serve_request, args.serve_points)}), flush=True)
         return
     import opencamlib_gb300 as ocl
     from opencamlib_gb300 import _abi
