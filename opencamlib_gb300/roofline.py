@@ -34,9 +34,9 @@ ncu capture of `bench.py --profile-step` (summarised under profiles/).
 from __future__ import annotations
 
 # cutter -> FP32 operations per screened pair
-FP32_PER_SCREEN = {"cyl": 912.6, "ball": 1111.4, "bull": 1491.2, "cone": 1202.4, "ballcone": 1995.2}
+FP32_PER_SCREEN = {"cyl": 565.2, "ball": 694.0, "bull": 1214.0, "cone": 748.6, "ballcone": 1567.1}
 # cutter -> FP64 operations per refined triangle
-FP64_PER_REFINED = {"cyl": 122.1, "ball": 237.4, "bull": 1274.8, "cone": 295.3, "ballcone": 320.6}
+FP64_PER_REFINED = {"cyl": 129.5, "ball": 256.8, "bull": 1274.3, "cone": 295.6, "ballcone": 320.6}
 # cutter -> DRAM bytes of the screen kernels per call on the 1,000,000-point raster
 SCREEN_DRAM_BYTES = {"cyl": 784473344, "ball": 688323584, "bull": 854738432, "cone": 547958272, "ballcone": 959312384}
 
